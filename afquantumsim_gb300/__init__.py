@@ -1,0 +1,416 @@
+"""afquantumsim_gb300 — GB300-native state-vector engine (Python binding).
+
+The engine is ``libaqsg.so`` (CUDA, sm_103a, C ABI declared in
+include/aqsg.h).  This module binds it with ctypes for tests, benchmarks and
+scripting.  There is no CPU fallback: importing works without a GPU (so the
+ABI can be inspected), but every call that needs the device fails loudly
+when the library or the GPU is missing.
+
+Gate constructors mirror the reference's gate classes (include/quantum.h):
+``X(t)``, ``CX(c, t)``, ``CPhase(c, t, angle)``, ... each returning an
+``aqsg_op``; ``Simulator`` mirrors QSimulator's state/measure members.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+from . import _abi
+from . import _abi as kinds  # op kind constants: kinds.X, kinds.CPHASE, ...
+from ._abi import (C64, C128, EXEC_AUTO, EXEC_PER_GATE, EXEC_TILED, SAMPLE_CLAMP,
+                   SAMPLE_REFERENCE, Op, make_op, op_array)
+
+PKG_DIR = Path(__file__).resolve().parent
+LIB_PATH = PKG_DIR / "_build" / "libaqsg.so"
+
+EXPORTS = [
+    "aqsg_version", "aqsg_last_error", "aqsg_init", "aqsg_shutdown",
+    "aqsg_set_exec_mode", "aqsg_synchronize", "aqsg_ctx_stream", "aqsg_launch_count",
+    "aqsg_state_alloc", "aqsg_state_free", "aqsg_state_info",
+    "aqsg_state_set_basis_index", "aqsg_state_set_product", "aqsg_state_upload",
+    "aqsg_state_download", "aqsg_state_download_range", "aqsg_state_copy",
+    "aqsg_check_ops", "aqsg_apply_ops", "aqsg_qubit_prob", "aqsg_state_prob",
+    "aqsg_probs", "aqsg_norm2", "aqsg_sample", "aqsg_sample_seeded",
+    "aqsg_collapse_qubit", "aqsg_collapse_all", "aqsg_expect_z",
+]
+
+_lib = None
+
+
+class AqsgError(RuntimeError):
+    """Error status from libaqsg; `.code` is the aqsg_status."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+        self.msg = msg
+
+
+# status -> Python exception class (std::out_of_range ~ IndexError, ...)
+class OutOfRange(AqsgError, IndexError):
+    pass
+
+
+class InvalidArgument(AqsgError, ValueError):
+    pass
+
+
+class DomainError(AqsgError, ValueError):
+    pass
+
+
+_EXC = {_abi.ERR_OUT_OF_RANGE: OutOfRange, _abi.ERR_INVALID_ARGUMENT: InvalidArgument,
+        _abi.ERR_DOMAIN: DomainError}
+
+
+def load_library(path: os.PathLike | str | None = None) -> C.CDLL:
+    """Load libaqsg.so (built in-tree by __graft_entry__.build())."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"libaqsg.so not built at {p}; run __graft_entry__.build()")
+    lib = C.CDLL(str(p))
+    P, I, U64, D = C.c_void_p, C.c_int, C.c_uint64, C.c_double
+    sig = {
+        "aqsg_version": ([], I),
+        "aqsg_last_error": ([C.c_char_p, C.c_size_t], C.c_size_t),
+        "aqsg_init": ([I, C.POINTER(P)], I),
+        "aqsg_shutdown": ([P], I),
+        "aqsg_set_exec_mode": ([P, I], I),
+        "aqsg_synchronize": ([P], I),
+        "aqsg_ctx_stream": ([P, C.POINTER(P)], I),
+        "aqsg_launch_count": ([P, C.POINTER(U64)], I),
+        "aqsg_state_alloc": ([P, I, I, C.POINTER(P)], I),
+        "aqsg_state_free": ([P], I),
+        "aqsg_state_info": ([P, C.POINTER(I), C.POINTER(I)], I),
+        "aqsg_state_set_basis_index": ([P, U64], I),
+        "aqsg_state_set_product": ([P, C.POINTER(C.c_float)], I),
+        "aqsg_state_upload": ([P, P, I], I),
+        "aqsg_state_download": ([P, P], I),
+        "aqsg_state_download_range": ([P, U64, U64, P], I),
+        "aqsg_state_copy": ([P, P], I),
+        "aqsg_check_ops": ([I, C.POINTER(Op), I], I),
+        "aqsg_apply_ops": ([P, C.POINTER(Op), I, I], I),
+        "aqsg_qubit_prob": ([P, I, C.POINTER(D)], I),
+        "aqsg_state_prob": ([P, U64, C.POINTER(D)], I),
+        "aqsg_probs": ([P, P, I], I),
+        "aqsg_norm2": ([P, C.POINTER(D)], I),
+        "aqsg_sample": ([P, C.POINTER(D), U64, I, C.POINTER(U64)], I),
+        "aqsg_sample_seeded": ([P, U64, U64, I, C.POINTER(U64)], I),
+        "aqsg_collapse_qubit": ([P, I, D, C.POINTER(I), C.POINTER(D)], I),
+        "aqsg_collapse_all": ([P, D, C.POINTER(U64)], I),
+        "aqsg_expect_z": ([P, C.POINTER(D), C.POINTER(D)], I),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def last_error() -> str:
+    lib = load_library()
+    buf = C.create_string_buffer(1024)
+    lib.aqsg_last_error(buf, len(buf))
+    return buf.value.decode()
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise _EXC.get(rc, AqsgError)(rc, last_error())
+
+
+# ---- gate constructors (reference class names, include/quantum.h:857-1589) ----
+# Each returns one aqsg_op.  Keyword `controls` / `control_values` add extra
+# controls (the lowering of ControlGate / NControl_Gate).
+
+def Barrier():
+    return make_op(kinds.BARRIER)
+
+
+def X(target, **kw):
+    return make_op(kinds.X, (target,), **kw)
+
+
+def Y(target, **kw):
+    return make_op(kinds.Y, (target,), **kw)
+
+
+def Z(target, **kw):
+    return make_op(kinds.Z, (target,), **kw)
+
+
+def H(target, **kw):
+    return make_op(kinds.H, (target,), **kw)
+
+
+def Phase(target, angle, **kw):
+    return make_op(kinds.PHASE, (target,), angle=angle, **kw)
+
+
+def RotX(target, angle, **kw):
+    return make_op(kinds.RX, (target,), angle=angle, **kw)
+
+
+def RotY(target, angle, **kw):
+    return make_op(kinds.RY, (target,), angle=angle, **kw)
+
+
+def RotZ(target, angle, **kw):
+    return make_op(kinds.RZ, (target,), angle=angle, **kw)
+
+
+def Swap(a, b, **kw):
+    return make_op(kinds.SWAP, (a, b), **kw)
+
+
+def CX(c, t, **kw):
+    return make_op(kinds.CX, (c, t), **kw)
+
+
+def CY(c, t, **kw):
+    return make_op(kinds.CY, (c, t), **kw)
+
+
+def CZ(c, t, **kw):
+    return make_op(kinds.CZ, (c, t), **kw)
+
+
+def CH(c, t, **kw):
+    return make_op(kinds.CH, (c, t), **kw)
+
+
+def CPhase(c, t, angle, **kw):
+    return make_op(kinds.CPHASE, (c, t), angle=angle, **kw)
+
+
+def CSwap(c, a, b, **kw):
+    return make_op(kinds.CSWAP, (c, a, b), **kw)
+
+
+def CRotX(c, t, angle, **kw):
+    return make_op(kinds.CRX, (c, t), angle=angle, **kw)
+
+
+def CRotY(c, t, angle, **kw):
+    return make_op(kinds.CRY, (c, t), angle=angle, **kw)
+
+
+def CRotZ(c, t, angle, **kw):
+    return make_op(kinds.CRZ, (c, t), angle=angle, **kw)
+
+
+def CCNot(a, b, t, **kw):
+    return make_op(kinds.CCX, (a, b, t), **kw)
+
+
+def Or(a, b, t, **kw):
+    return make_op(kinds.OR, (a, b, t), **kw)
+
+
+def Unitary(targets, matrix, **kw):
+    return make_op(kinds.UNITARY, tuple(targets), matrix=matrix, **kw)
+
+
+Not = X          # using Not = X        (quantum.h)
+CNot = Xor = CX  # using CNot = CX; using Xor = CX
+And = CCNot      # using And = CCNot
+
+
+def fourier_transform(n: int, swaps: bool = False, angle_dtype=np.float32):
+    """QFT gate list of aqs::fourier_transform (src/quantum_algo.cpp:103-114):
+    for i = n-1..0: H(i), then CPhase(j, i, pi / 2^(i-j)) for j < i, the angle
+    computed in float as the reference does (aqs::pi is a float).  swaps=True
+    appends Swap(i, n-1-i) for i < n/2 (the textbook output order)."""
+    pi = np.float32(3.14159265358979323846)
+    ops = []
+    for i in range(n - 1, -1, -1):
+        ops.append(H(i))
+        for j in range(i):
+            ops.append(CPhase(j, i, float(pi / np.float32(1 << (i - j)))))
+    if swaps:
+        for i in range(n // 2):
+            ops.append(Swap(i, n - 1 - i))
+    return ops
+
+
+# ---- engine objects ---------------------------------------------------------------
+
+class Context:
+    """An aqsg_ctx: one CUDA device + one stream."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = C.c_void_p()
+        _check(self.lib.aqsg_init(device, C.byref(h)))
+        self.h = h
+        self.device = device
+
+    def set_exec_mode(self, mode: int) -> None:
+        _check(self.lib.aqsg_set_exec_mode(self.h, mode))
+
+    def synchronize(self) -> None:
+        _check(self.lib.aqsg_synchronize(self.h))
+
+    def stream_handle(self) -> int:
+        """The context's cudaStream_t as an integer."""
+        v = C.c_void_p()
+        _check(self.lib.aqsg_ctx_stream(self.h, C.byref(v)))
+        return v.value or 0
+
+    def launch_count(self) -> int:
+        v = C.c_uint64()
+        _check(self.lib.aqsg_launch_count(self.h, C.byref(v)))
+        return v.value
+
+    def close(self) -> None:
+        if self.h:
+            _check(self.lib.aqsg_shutdown(self.h))
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class State:
+    """An n-qubit register on the device (aqsg_state)."""
+
+    def __init__(self, ctx: Context, n: int, dtype: int = C64):
+        self.ctx, self.lib = ctx, ctx.lib
+        self.n, self.dtype = n, dtype
+        h = C.c_void_p()
+        _check(self.lib.aqsg_state_alloc(ctx.h, n, dtype, C.byref(h)))
+        self.h = h
+
+    @property
+    def np_dtype(self):
+        return np.complex64 if self.dtype == C64 else np.complex128
+
+    def free(self) -> None:
+        if self.h:
+            _check(self.lib.aqsg_state_free(self.h))
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.free()
+
+    # preparation
+    def set_basis(self, k: int) -> "State":
+        _check(self.lib.aqsg_state_set_basis_index(self.h, k))
+        return self
+
+    def set_product(self, qubit_amps) -> "State":
+        a = np.ascontiguousarray(np.asarray(qubit_amps, dtype=np.float32).reshape(-1))
+        _check(self.lib.aqsg_state_set_product(self.h, a.ctypes.data_as(C.POINTER(C.c_float))))
+        return self
+
+    def upload(self, sv, normalize: bool = False) -> "State":
+        a = np.ascontiguousarray(np.asarray(sv, dtype=self.np_dtype))
+        assert a.size == 1 << self.n
+        _check(self.lib.aqsg_state_upload(self.h, a.ctypes.data, 1 if normalize else 0))
+        self.ctx.synchronize()
+        return self
+
+    def upload_ptr(self, ptr: int, normalize: bool = False) -> None:
+        _check(self.lib.aqsg_state_upload(self.h, ptr, 1 if normalize else 0))
+
+    def download(self, out=None) -> np.ndarray:
+        if out is None:
+            out = np.empty(1 << self.n, dtype=self.np_dtype)
+        _check(self.lib.aqsg_state_download(self.h, out.ctypes.data))
+        return out
+
+    def download_ptr(self, ptr: int) -> None:
+        _check(self.lib.aqsg_state_download(self.h, ptr))
+
+    def copy_from(self, other: "State") -> None:
+        _check(self.lib.aqsg_state_copy(self.h, other.h))
+
+    # simulation
+    def apply(self, ops, mode: int = -1) -> None:
+        arr = ops if isinstance(ops, C.Array) else op_array(list(ops))
+        _check(self.lib.aqsg_apply_ops(self.h, arr, len(arr), mode))
+
+    # measurement
+    def qubit_prob(self, q: int) -> float:
+        v = C.c_double()
+        _check(self.lib.aqsg_qubit_prob(self.h, q, C.byref(v)))
+        return v.value
+
+    def state_prob(self, k: int) -> float:
+        v = C.c_double()
+        _check(self.lib.aqsg_state_prob(self.h, k, C.byref(v)))
+        return v.value
+
+    def probs(self, dtype=np.float64) -> np.ndarray:
+        out = np.empty(1 << self.n, dtype=dtype)
+        _check(self.lib.aqsg_probs(self.h, out.ctypes.data, 1 if dtype == np.float64 else 0))
+        return out
+
+    def norm2(self) -> float:
+        v = C.c_double()
+        _check(self.lib.aqsg_norm2(self.h, C.byref(v)))
+        return v.value
+
+    def sample(self, u, rule: int = SAMPLE_REFERENCE) -> np.ndarray:
+        u = np.ascontiguousarray(np.asarray(u, dtype=np.float64).reshape(-1))
+        out = np.empty(u.size, dtype=np.uint64)
+        _check(self.lib.aqsg_sample(self.h, u.ctypes.data_as(C.POINTER(C.c_double)), u.size, rule,
+                                    out.ctypes.data_as(C.POINTER(C.c_uint64))))
+        return out
+
+    def sample_seeded(self, seed: int, count: int, rule: int = SAMPLE_REFERENCE) -> np.ndarray:
+        out = np.empty(count, dtype=np.uint64)
+        _check(self.lib.aqsg_sample_seeded(self.h, seed, count, rule,
+                                           out.ctypes.data_as(C.POINTER(C.c_uint64))))
+        return out
+
+    def collapse_qubit(self, q: int, u: float):
+        o, p = C.c_int(), C.c_double()
+        _check(self.lib.aqsg_collapse_qubit(self.h, q, u, C.byref(o), C.byref(p)))
+        return o.value, p.value
+
+    def collapse_all(self, u: float) -> int:
+        k = C.c_uint64()
+        _check(self.lib.aqsg_collapse_all(self.h, u, C.byref(k)))
+        return k.value
+
+    def expect_z(self):
+        z = np.empty(self.n, dtype=np.float64)
+        zz = np.empty(max(self.n - 1, 1), dtype=np.float64)
+        _check(self.lib.aqsg_expect_z(self.h, z.ctypes.data_as(C.POINTER(C.c_double)),
+                                      zz.ctypes.data_as(C.POINTER(C.c_double))))
+        return z, zz[: self.n - 1]
+
+
+def check_ops(n: int, ops) -> None:
+    lib = load_library()
+    arr = op_array(list(ops))
+    _check(lib.aqsg_check_ops(n, arr, len(arr)))
+
+
+def qstate(zero, one):
+    """Normalised single-qubit amplitudes as QState::force_normalize does
+    (quantum.cpp:145-157, float arithmetic).  Returns 4 floats."""
+    z, o = complex(zero), complex(one)
+    q = np.array([z.real, z.imag, o.real, o.imag], dtype=np.float32)
+    mag2 = np.float32(q[0] * q[0]) + np.float32(q[1] * q[1])
+    mag2 = np.float32(mag2 + np.float32(q[2] * q[2]))
+    mag2 = np.float32(mag2 + np.float32(q[3] * q[3]))
+    if mag2 == 0:
+        raise ValueError("Cannot normalize a null state")
+    mag = np.float32(np.sqrt(mag2))
+    return (q / mag).astype(np.float32)

@@ -1,0 +1,118 @@
+// Internal declarations of libaqsg: context/state objects, the lowered gate
+// form the kernels consume, and the kernel launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/aqsg.h"
+
+namespace aqsg {
+
+// ---- errors ---------------------------------------------------------------
+int set_error(int code, const std::string& msg);
+int cuda_error(cudaError_t e, const char* where);
+#define AQSG_CUDA_TRY(expr)                                     \
+    do {                                                        \
+        cudaError_t e__ = (expr);                               \
+        if (e__ != cudaSuccess) return ::aqsg::cuda_error(e__, #expr); \
+    } while (0)
+
+// ---- lowered gate form ------------------------------------------------------
+// Every reference gate lowers to one of these classes acting on index bits
+// (bit = n-1-qubit).  Coefficients for c64 are float values (computed with
+// float trig exactly as src/quantum.cpp does) stored in double; for c128
+// they are the double-precision values of the same formulas.
+enum LCls : int {
+    L_NOP = 0,
+    L_PERM_X = 1,    // swap the pair (t=0, t=1) where the condition holds
+    L_PERM_OR = 2,   // as PERM_X, condition: (i & amask) != 0
+    L_PERM_SWAP = 3, // swap (a=0,b=1) <-> (a=1,b=0) where the condition holds
+    L_DIAG1 = 4,     // multiply amplitudes with (i & pmask) == pval by m[0]
+    L_DIAG2 = 5,     // target t: multiply t=0 by m[0], t=1 by m[1]
+    L_MAT2 = 6,      // 2x2 matrix on target t
+    L_MATK = 7       // 2^k x 2^k matrix on bits tb[0..k) (tb[0] = MSB)
+};
+
+struct LOp {
+    int cls = L_NOP;
+    int t0 = -1, t1 = -1;       // target bits
+    int k = 0;                  // MATK
+    int tb[AQSG_MAX_UNITARY_QUBITS] = {0, 0, 0, 0, 0};
+    uint64_t cmask = 0, cval = 0;  // all-of condition on other bits
+    uint64_t amask = 0;            // any-of condition (Or)
+    double m[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // complex coefficients (re, im)
+    std::vector<double> mk;        // MATK: row-major complex matrix
+    // diagonal ops do not force their bits into a tile
+    bool diagonal() const { return cls == L_DIAG1 || cls == L_DIAG2; }
+};
+
+// Validate one op against an n-qubit register with the reference's check()
+// messages; returns AQSG_OK or an error code (message set).
+int check_op(int n, const aqsg_op& op);
+// Lower one op (already checked).  dtype selects the coefficient precision.
+int lower_op(int n, int dtype, const aqsg_op& op, LOp* out);
+
+// ---- objects ------------------------------------------------------------------
+struct Scratch {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace aqsg
+
+struct aqsg_ctx_s {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    int exec_mode = AQSG_EXEC_AUTO;
+    uint64_t launches = 0;
+    int live_states = 0;
+    aqsg::Scratch partial;   // FP64 partial sums of reductions
+    aqsg::Scratch prefix;    // FP64 chunk prefix sums for sampling
+    aqsg::Scratch sample_u;  // uniforms of one sampling call
+    aqsg::Scratch sample_o;  // outcomes of one sampling call
+    aqsg::Scratch ops;       // device copy of tile-pass op tables
+    aqsg::Scratch probs;     // probability download staging
+    double* host_result = nullptr;  // pinned FP64 results
+};
+
+struct aqsg_state_s {
+    aqsg_ctx ctx = nullptr;
+    int n = 0;
+    int dtype = AQSG_C64;
+    uint64_t amps = 0;
+    void* d = nullptr;
+};
+
+namespace aqsg {
+
+int ensure_scratch(Scratch& s, size_t bytes);
+inline size_t amp_bytes(int dtype) { return dtype == AQSG_C128 ? 16 : 8; }
+
+// ---- kernel launchers (gate_kernels.cu) -------------------------------------
+int launch_lop(aqsg_state_s* st, const LOp& op);
+
+// ---- tile passes (tile_kernels.cu) ---------------------------------------------
+// Runs ops through shared-memory tile passes; returns AQSG_OK.
+int run_tiled(aqsg_state_s* st, const std::vector<LOp>& ops);
+// Largest tile (log2 amplitudes) the tile kernel holds for a dtype.
+int tile_max_bits(int dtype);
+
+// ---- init / measurement launchers (measure_kernels.cu) -------------------------
+int launch_set_basis(aqsg_state_s* st, uint64_t k);
+int launch_set_product(aqsg_state_s* st, const float* amps);
+int launch_scale(aqsg_state_s* st, double scale);
+// sum of |a_i|^2 over i with (i & mask) == val, FP64; result on host
+int reduce_prob(aqsg_state_s* st, uint64_t mask, uint64_t val, double* out);
+int launch_probs(aqsg_state_s* st, void* dev_out, int out_dtype);
+int sample(aqsg_state_s* st, const double* host_u, uint64_t seed, bool seeded,
+           uint64_t count, int rule, uint64_t* host_out);
+int launch_collapse_qubit(aqsg_state_s* st, uint64_t mask, int outcome,
+                          double scale);
+int expect_z(aqsg_state_s* st, double* z, double* zz);
+
+}  // namespace aqsg

@@ -1,0 +1,400 @@
+// One-gate-per-pass kernels: each launch streams the amplitudes a gate can
+// change once through HBM, in place.
+//
+// A gate with target/control bits F touches the index set
+//   { expand(k) : k in [0, 2^(n-|F|)) }
+// where expand() inserts the fixed bits of F (targets at 0, controls at their
+// required value).  Consecutive k give consecutive indices between fixed bits,
+// so whenever bit 0 is free two neighbouring c64 amplitudes share one 128-bit
+// access (VEC = 2); c128 amplitudes are 128-bit on their own.
+//
+// These replace the per-gate operator builds + af::matmul of the reference
+// (src/quantum.cpp:540-1950): the operators there are 2^n x 2^n (dense
+// Kronecker or CSR); here a gate is a handful of coefficients.
+#include <algorithm>
+
+#include "aqsg_internal.h"
+#include "common.cuh"
+
+namespace aqsg {
+
+constexpr int kThreads = 256;
+
+enum PairOp { P_MAT2 = 0, P_DIAG2 = 1, P_PERMX = 2, P_PERMOR = 3 };
+
+template <typename R>
+struct M2 {
+    typename Cx<R>::T m[4];
+};
+
+// ---- unit load / store: VEC consecutive amplitudes starting at index i -----
+template <typename R, int VEC>
+struct Unit {
+    typename Cx<R>::T a[VEC];
+};
+
+template <typename R, int VEC>
+__device__ __forceinline__ Unit<R, VEC> load_unit(const typename Cx<R>::T* sv, uint64_t i) {
+    Unit<R, VEC> u;
+    if constexpr (VEC == 2) {
+        const float4 f = __ldcs(reinterpret_cast<const float4*>(sv) + (i >> 1));
+        u.a[0] = make_float2(f.x, f.y);
+        u.a[1] = make_float2(f.z, f.w);
+    } else {
+        u.a[0] = __ldcs(sv + i);
+    }
+    return u;
+}
+
+template <typename R, int VEC>
+__device__ __forceinline__ void store_unit(typename Cx<R>::T* sv, uint64_t i, const Unit<R, VEC>& u) {
+    if constexpr (VEC == 2) {
+        __stcs(reinterpret_cast<float4*>(sv) + (i >> 1),
+               make_float4(u.a[0].x, u.a[0].y, u.a[1].x, u.a[1].y));
+    } else {
+        __stcs(sv + i, u.a[0]);
+    }
+}
+
+// ---- pair kernels: MAT2 / DIAG2 / PERM_X / PERM_OR ---------------------------
+// PACKED: c64 with target bit 0 — the pair is one 128-bit access.
+template <typename R, int VEC, bool PACKED, int OP, typename FX>
+__global__ void __launch_bounds__(kThreads)
+k_pair(typename Cx<R>::T* __restrict__ sv, FX fx, uint64_t tmask, uint64_t amask,
+       uint64_t units, M2<R> m) {
+    using T = typename Cx<R>::T;
+    constexpr int IT = 2;
+    const uint64_t first = (uint64_t)blockIdx.x * (kThreads * IT) + threadIdx.x;
+    Unit<R, VEC> lo[IT], hi[IT];
+    uint64_t i0[IT];
+    bool ok[IT];
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+        const uint64_t u = first + (uint64_t)it * kThreads;
+        ok[it] = u < units;
+        if (ok[it]) {
+            if constexpr (PACKED) {
+                i0[it] = fx.expand(u);
+                const float4 f = __ldcs(reinterpret_cast<const float4*>(sv) + (i0[it] >> 1));
+                lo[it].a[0] = make_float2(f.x, f.y);
+                hi[it].a[0] = make_float2(f.z, f.w);
+            } else {
+                i0[it] = fx.expand(u * VEC);
+                lo[it] = load_unit<R, VEC>(sv, i0[it]);
+                hi[it] = load_unit<R, VEC>(sv, i0[it] | tmask);
+            }
+        }
+    }
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+        if (!ok[it]) continue;
+        bool changed = true;
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) {
+            const T a = lo[it].a[v], b = hi[it].a[v];
+            if constexpr (OP == P_MAT2) {
+                lo[it].a[v] = cmul2(m.m[0], a, m.m[1], b);
+                hi[it].a[v] = cmul2(m.m[2], a, m.m[3], b);
+            } else if constexpr (OP == P_DIAG2) {
+                lo[it].a[v] = cmul(m.m[0], a);
+                hi[it].a[v] = cmul(m.m[3], b);
+            } else if constexpr (OP == P_PERMX) {
+                lo[it].a[v] = b;
+                hi[it].a[v] = a;
+            } else {  // P_PERMOR: flip unless all of amask are 0
+                const bool fire = ((i0[it] + v) & amask) != 0;
+                lo[it].a[v] = fire ? b : a;
+                hi[it].a[v] = fire ? a : b;
+            }
+        }
+        if constexpr (OP == P_PERMOR) {
+            changed = ((i0[it] & amask) != 0) || (VEC == 2 && ((i0[it] + 1) & amask) != 0);
+        }
+        if (!changed) continue;
+        if constexpr (PACKED) {
+            __stcs(reinterpret_cast<float4*>(sv) + (i0[it] >> 1),
+                   make_float4(lo[it].a[0].x, lo[it].a[0].y, hi[it].a[0].x, hi[it].a[0].y));
+        } else {
+            store_unit<R, VEC>(sv, i0[it], lo[it]);
+            store_unit<R, VEC>(sv, i0[it] | tmask, hi[it]);
+        }
+    }
+}
+
+// ---- DIAG1: multiply the amplitudes of one index pattern by a phase --------
+template <typename R, int VEC, typename FX>
+__global__ void __launch_bounds__(kThreads)
+k_diag1(typename Cx<R>::T* __restrict__ sv, FX fx, uint64_t units, typename Cx<R>::T ph) {
+    constexpr int IT = 4;
+    const uint64_t first = (uint64_t)blockIdx.x * (kThreads * IT) + threadIdx.x;
+    Unit<R, VEC> a[IT];
+    uint64_t idx[IT];
+    bool ok[IT];
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+        const uint64_t u = first + (uint64_t)it * kThreads;
+        ok[it] = u < units;
+        if (ok[it]) {
+            idx[it] = fx.expand(u * VEC);
+            a[it] = load_unit<R, VEC>(sv, idx[it]);
+        }
+    }
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+        if (!ok[it]) continue;
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) a[it].a[v] = cmul(ph, a[it].a[v]);
+        store_unit<R, VEC>(sv, idx[it], a[it]);
+    }
+}
+
+// ---- PERM_SWAP: exchange (a=0,b=1) with (a=1,b=0) ---------------------------
+template <typename R, int VEC, typename FX>
+__global__ void __launch_bounds__(kThreads)
+k_swap(typename Cx<R>::T* __restrict__ sv, FX fx, uint64_t xmask, uint64_t units) {
+    constexpr int IT = 2;
+    const uint64_t first = (uint64_t)blockIdx.x * (kThreads * IT) + threadIdx.x;
+    Unit<R, VEC> p[IT], q[IT];
+    uint64_t idx[IT];
+    bool ok[IT];
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+        const uint64_t u = first + (uint64_t)it * kThreads;
+        ok[it] = u < units;
+        if (ok[it]) {
+            idx[it] = fx.expand(u * VEC);
+            p[it] = load_unit<R, VEC>(sv, idx[it]);
+            q[it] = load_unit<R, VEC>(sv, idx[it] ^ xmask);
+        }
+    }
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+        if (!ok[it]) continue;
+        store_unit<R, VEC>(sv, idx[it], q[it]);
+        store_unit<R, VEC>(sv, idx[it] ^ xmask, p[it]);
+    }
+}
+
+// ---- MATK: dense 2^K x 2^K matrix on K target bits ---------------------------
+template <typename R, int K>
+struct MK {
+    typename Cx<R>::T m[(1 << K) * (1 << K)];
+    uint64_t off[1 << K];
+};
+
+template <typename R, int K, typename FX>
+__global__ void __launch_bounds__(kThreads)
+k_matk(typename Cx<R>::T* __restrict__ sv, FX fx, uint64_t units, const MK<R, K> mk) {
+    using T = typename Cx<R>::T;
+    constexpr int D = 1 << K;
+    const uint64_t u = (uint64_t)blockIdx.x * kThreads + threadIdx.x;
+    if (u >= units) return;
+    const uint64_t base = fx.expand(u);
+    T v[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) v[c] = sv[base + mk.off[c]];
+    for (int r = 0; r < D; ++r) {
+        T acc;
+        acc.x = 0;
+        acc.y = 0;
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            const T mm = mk.m[r * D + c];
+            acc.x += mm.x * v[c].x - mm.y * v[c].y;
+            acc.y += mm.x * v[c].y + mm.y * v[c].x;
+        }
+        sv[base + mk.off[r]] = acc;
+    }
+}
+
+// ---- host-side dispatch -----------------------------------------------------------
+
+struct FixedBits {
+    int nf = 0;
+    uint32_t pos[64];
+    uint64_t val = 0;
+    uint64_t mask = 0;
+};
+
+static FixedBits make_fixed(uint64_t mask, uint64_t val) {
+    FixedBits f;
+    f.mask = mask;
+    f.val = val & mask;
+    for (int b = 0; b < 64; ++b)
+        if ((mask >> b) & 1ull) f.pos[f.nf++] = (uint32_t)b;
+    return f;
+}
+
+template <int NF>
+static Fix<NF> to_fix(const FixedBits& f) {
+    Fix<NF> x;
+    for (int i = 0; i < NF; ++i) x.pos[i] = f.pos[i];
+    x.val = f.val;
+    return x;
+}
+
+static FixN to_fixn(const FixedBits& f) {
+    FixN x;
+    x.nf = f.nf;
+    for (int i = 0; i < f.nf; ++i) x.pos[i] = f.pos[i];
+    x.val = f.val;
+    return x;
+}
+
+static inline unsigned grid_for(uint64_t units, int per_block) {
+    return (unsigned)((units + per_block - 1) / per_block);
+}
+
+// Calls fn(fixer) with the narrowest fixer type for f.nf.
+template <typename Fn>
+static void with_fix(const FixedBits& f, Fn&& fn) {
+    switch (f.nf) {
+        case 1: fn(to_fix<1>(f)); break;
+        case 2: fn(to_fix<2>(f)); break;
+        case 3: fn(to_fix<3>(f)); break;
+        case 4: fn(to_fix<4>(f)); break;
+        default: fn(to_fixn(f)); break;
+    }
+}
+
+template <typename R>
+static typename Cx<R>::T cval(double re, double im) {
+    typename Cx<R>::T t;
+    t.x = (R)re;
+    t.y = (R)im;
+    return t;
+}
+
+template <typename R, int VEC, bool PACKED, int OP>
+static void launch_pair_v(aqsg_state_s* st, const FixedBits& f, uint64_t tmask, uint64_t amask,
+                          uint64_t units, const M2<R>& m) {
+    using T = typename Cx<R>::T;
+    const unsigned grid = grid_for(units, kThreads * 2);
+    with_fix(f, [&](auto fx) {
+        k_pair<R, VEC, PACKED, OP, decltype(fx)><<<grid, kThreads, 0, st->ctx->stream>>>(
+            (T*)st->d, fx, tmask, amask, units, m);
+    });
+}
+
+template <typename R>
+static int launch_typed(aqsg_state_s* st, const LOp& op) {
+    using T = typename Cx<R>::T;
+    const bool is_f = sizeof(R) == 4;
+    const uint64_t N = st->amps;
+    switch (op.cls) {
+        case L_MAT2: case L_DIAG2: case L_PERM_X: case L_PERM_OR: {
+            const uint64_t tmask = 1ull << op.t0;
+            FixedBits f = make_fixed(op.cmask | tmask, op.cval);
+            M2<R> m;
+            for (int e = 0; e < 4; ++e) m.m[e] = cval<R>(op.m[2 * e], op.m[2 * e + 1]);
+            const int OPK = op.cls == L_MAT2 ? P_MAT2 : op.cls == L_DIAG2 ? P_DIAG2
+                          : op.cls == L_PERM_X ? P_PERMX : P_PERMOR;
+            uint64_t units = N >> f.nf;
+            const bool packed = is_f && op.t0 == 0;
+            const bool vec2 = is_f && !packed && (f.mask & 1ull) == 0;
+            auto go = [&](auto vec_tag, auto packed_tag) {
+                constexpr int V = decltype(vec_tag)::value;
+                constexpr bool P = decltype(packed_tag)::value;
+                switch (OPK) {
+                    case P_MAT2: launch_pair_v<R, V, P, P_MAT2>(st, f, tmask, op.amask, units, m); break;
+                    case P_DIAG2: launch_pair_v<R, V, P, P_DIAG2>(st, f, tmask, op.amask, units, m); break;
+                    case P_PERMX: launch_pair_v<R, V, P, P_PERMX>(st, f, tmask, op.amask, units, m); break;
+                    default: launch_pair_v<R, V, P, P_PERMOR>(st, f, tmask, op.amask, units, m); break;
+                }
+            };
+            if constexpr (sizeof(R) == 4) {
+                if (packed) go(std::integral_constant<int, 1>(), std::true_type());
+                else if (vec2) { units >>= 1; go(std::integral_constant<int, 2>(), std::false_type()); }
+                else go(std::integral_constant<int, 1>(), std::false_type());
+            } else {
+                go(std::integral_constant<int, 1>(), std::false_type());
+            }
+            break;
+        }
+        case L_DIAG1: {
+            FixedBits f = make_fixed(op.cmask, op.cval);
+            uint64_t units = N >> f.nf;
+            const T ph = cval<R>(op.m[0], op.m[1]);
+            const bool vec2 = is_f && (f.mask & 1ull) == 0;
+            if (vec2) {
+                units >>= 1;
+                const unsigned grid = grid_for(units, kThreads * 4);
+                with_fix(f, [&](auto fx) {
+                    k_diag1<R, (sizeof(R) == 4 ? 2 : 1), decltype(fx)>
+                        <<<grid, kThreads, 0, st->ctx->stream>>>((T*)st->d, fx, units, ph);
+                });
+            } else {
+                const unsigned grid = grid_for(units, kThreads * 4);
+                with_fix(f, [&](auto fx) {
+                    k_diag1<R, 1, decltype(fx)><<<grid, kThreads, 0, st->ctx->stream>>>(
+                        (T*)st->d, fx, units, ph);
+                });
+            }
+            break;
+        }
+        case L_PERM_SWAP: {
+            const uint64_t ma = 1ull << op.t0, mb = 1ull << op.t1;
+            FixedBits f = make_fixed(op.cmask | ma | mb, op.cval | mb);
+            uint64_t units = N >> f.nf;
+            const bool vec2 = is_f && (f.mask & 1ull) == 0;
+            if (vec2) {
+                units >>= 1;
+                const unsigned grid = grid_for(units, kThreads * 2);
+                with_fix(f, [&](auto fx) {
+                    k_swap<R, (sizeof(R) == 4 ? 2 : 1), decltype(fx)>
+                        <<<grid, kThreads, 0, st->ctx->stream>>>((T*)st->d, fx, ma | mb, units);
+                });
+            } else {
+                const unsigned grid = grid_for(units, kThreads * 2);
+                with_fix(f, [&](auto fx) {
+                    k_swap<R, 1, decltype(fx)><<<grid, kThreads, 0, st->ctx->stream>>>(
+                        (T*)st->d, fx, ma | mb, units);
+                });
+            }
+            break;
+        }
+        case L_MATK: {
+            uint64_t tm = 0;
+            for (int j = 0; j < op.k; ++j) tm |= 1ull << op.tb[j];
+            FixedBits f = make_fixed(op.cmask | tm, op.cval);
+            const uint64_t units = N >> f.nf;
+            const unsigned grid = grid_for(units, kThreads);
+            auto go = [&](auto k_tag) {
+                constexpr int K = decltype(k_tag)::value;
+                constexpr int D = 1 << K;
+                auto* mk = new MK<R, K>();
+                for (int r = 0; r < D; ++r) {
+                    uint64_t off = 0;
+                    for (int j = 0; j < K; ++j)
+                        if ((r >> (K - 1 - j)) & 1) off |= 1ull << op.tb[j];
+                    mk->off[r] = off;
+                }
+                for (int e = 0; e < D * D; ++e) mk->m[e] = cval<R>(op.mk[2 * e], op.mk[2 * e + 1]);
+                with_fix(f, [&](auto fx) {
+                    k_matk<R, K, decltype(fx)><<<grid, kThreads, 0, st->ctx->stream>>>(
+                        (T*)st->d, fx, units, *mk);
+                });
+                delete mk;
+            };
+            switch (op.k) {
+                case 2: go(std::integral_constant<int, 2>()); break;
+                case 3: go(std::integral_constant<int, 3>()); break;
+                case 4: go(std::integral_constant<int, 4>()); break;
+                case 5: go(std::integral_constant<int, 5>()); break;
+                default: return set_error(AQSG_ERR_INVALID_ARGUMENT, "Unsupported unitary size");
+            }
+            break;
+        }
+        default: return AQSG_OK;
+    }
+    st->ctx->launches++;
+    AQSG_CUDA_TRY(cudaGetLastError());
+    return AQSG_OK;
+}
+
+int launch_lop(aqsg_state_s* st, const LOp& op) {
+    if (op.cls == L_NOP) return AQSG_OK;
+    return st->dtype == AQSG_C64 ? launch_typed<float>(st, op) : launch_typed<double>(st, op);
+}
+
+}  // namespace aqsg

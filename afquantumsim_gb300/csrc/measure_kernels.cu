@@ -1,0 +1,588 @@
+// State preparation and measurement kernels.
+//
+// Reductions are FP64 and deterministic (fixed two-level trees, no atomics).
+// They replace the ArrayFire reductions of the reference's measurement
+// members (src/quantum.cpp:308-531), which sum in FP32.
+#include <cmath>
+
+#include "aqsg_internal.h"
+#include "common.cuh"
+
+namespace aqsg {
+
+constexpr int kRedThreads = 256;
+
+// ---- preparation ---------------------------------------------------------------
+
+template <typename T>
+__global__ void k_set_one(T* sv, uint64_t k) {
+    T one;
+    one.x = 1;
+    one.y = 0;
+    sv[k] = one;
+}
+
+int launch_set_basis(aqsg_state_s* st, uint64_t k) {
+    cudaStream_t s = st->ctx->stream;
+    AQSG_CUDA_TRY(cudaMemsetAsync(st->d, 0, st->amps * amp_bytes(st->dtype), s));
+    if (st->dtype == AQSG_C64)
+        k_set_one<float2><<<1, 1, 0, s>>>((float2*)st->d, k);
+    else
+        k_set_one<double2><<<1, 1, 0, s>>>((double2*)st->d, k);
+    st->ctx->launches++;
+    AQSG_CUDA_TRY(cudaGetLastError());
+    return AQSG_OK;
+}
+
+struct QAmps {
+    float v[4 * AQSG_MAX_QUBITS];
+};
+
+// Product state: the Kronecker chain of generate_statevector
+// (quantum.cpp:261-275, tensor_product utils.cpp:16-30): after step i the
+// amplitude is q_i[b_i] * (previous), multiplied without contraction so c64
+// results equal the reference's float arithmetic bit for bit.
+__global__ void k_product_f32(float2* sv, int n, uint64_t N, QAmps q) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    int b = (int)((i >> (n - 1)) & 1);
+    float2 acc = make_float2(q.v[2 * b], q.v[2 * b + 1]);
+    for (int k = 1; k < n; ++k) {
+        b = (int)((i >> (n - 1 - k)) & 1);
+        const float ar = q.v[4 * k + 2 * b], ai = q.v[4 * k + 2 * b + 1];
+        float2 r;
+        r.x = __fsub_rn(__fmul_rn(ar, acc.x), __fmul_rn(ai, acc.y));
+        r.y = __fadd_rn(__fmul_rn(ar, acc.y), __fmul_rn(ai, acc.x));
+        acc = r;
+    }
+    sv[i] = acc;
+}
+
+__global__ void k_product_f64(double2* sv, int n, uint64_t N, QAmps q) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    int b = (int)((i >> (n - 1)) & 1);
+    double2 acc = make_double2(q.v[2 * b], q.v[2 * b + 1]);
+    for (int k = 1; k < n; ++k) {
+        b = (int)((i >> (n - 1 - k)) & 1);
+        const double ar = q.v[4 * k + 2 * b], ai = q.v[4 * k + 2 * b + 1];
+        double2 r;
+        r.x = __dsub_rn(__dmul_rn(ar, acc.x), __dmul_rn(ai, acc.y));
+        r.y = __dadd_rn(__dmul_rn(ar, acc.y), __dmul_rn(ai, acc.x));
+        acc = r;
+    }
+    sv[i] = acc;
+}
+
+int launch_set_product(aqsg_state_s* st, const float* amps) {
+    QAmps q;
+    for (int i = 0; i < 4 * st->n; ++i) q.v[i] = amps[i];
+    const unsigned grid = (unsigned)((st->amps + 255) / 256);
+    if (st->dtype == AQSG_C64)
+        k_product_f32<<<grid, 256, 0, st->ctx->stream>>>((float2*)st->d, st->n, st->amps, q);
+    else
+        k_product_f64<<<grid, 256, 0, st->ctx->stream>>>((double2*)st->d, st->n, st->amps, q);
+    st->ctx->launches++;
+    AQSG_CUDA_TRY(cudaGetLastError());
+    return AQSG_OK;
+}
+
+template <typename T, typename R>
+__global__ void k_scale(T* sv, uint64_t N, R s) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        T a = sv[i];
+        a.x *= s;
+        a.y *= s;
+        sv[i] = a;
+    }
+}
+
+static unsigned stream_grid(aqsg_state_s* st, uint64_t items, int threads) {
+    uint64_t want = (items + threads - 1) / threads;
+    uint64_t cap = (uint64_t)st->ctx->sm_count * 8;
+    if (want > cap) want = cap;
+    return (unsigned)(want < 1 ? 1 : want);
+}
+
+int launch_scale(aqsg_state_s* st, double scale) {
+    const unsigned grid = stream_grid(st, st->amps, 256);
+    if (st->dtype == AQSG_C64)
+        k_scale<float2, float><<<grid, 256, 0, st->ctx->stream>>>((float2*)st->d, st->amps, (float)scale);
+    else
+        k_scale<double2, double><<<grid, 256, 0, st->ctx->stream>>>((double2*)st->d, st->amps, scale);
+    st->ctx->launches++;
+    AQSG_CUDA_TRY(cudaGetLastError());
+    return AQSG_OK;
+}
+
+// ---- block reduction helpers ---------------------------------------------------
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sum over the block; result valid in thread 0.
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    v = warp_sum(v);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0;
+    if (w == 0) {
+        r = (l < (int)(blockDim.x >> 5)) ? sh[l] : 0.0;
+        r = warp_sum(r);
+    }
+    __syncthreads();
+    return r;
+}
+
+// ---- masked probability sum: sum |a_i|^2 over (i & mask) == val --------------
+
+template <typename R, int VEC, typename FX>
+__global__ void __launch_bounds__(kRedThreads)
+k_prob_partial(const typename Cx<R>::T* __restrict__ sv, FX fx, uint64_t units, double* partial) {
+    __shared__ double sh[32];
+    double acc = 0;
+    for (uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < units;
+         u += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = fx.expand(u * VEC);
+        if constexpr (VEC == 2) {
+            const float4 f = __ldcs(reinterpret_cast<const float4*>(sv) + (i >> 1));
+            acc += (double)f.x * f.x + (double)f.y * f.y + (double)f.z * f.z + (double)f.w * f.w;
+        } else {
+            const auto a = __ldcs(sv + i);
+            acc += (double)a.x * a.x + (double)a.y * a.y;
+        }
+    }
+    const double s = block_sum(acc, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+// Deterministic final sum of `count` partials into out[0].
+__global__ void k_sum_partials(const double* partial, int count, double* out) {
+    __shared__ double sh[32];
+    double acc = 0;
+    for (int i = threadIdx.x; i < count; i += blockDim.x) acc += partial[i];
+    const double s = block_sum(acc, sh);
+    if (threadIdx.x == 0) out[0] = s;
+}
+
+template <typename R>
+static int reduce_prob_t(aqsg_state_s* st, uint64_t mask, uint64_t val, double* out) {
+    using T = typename Cx<R>::T;
+    aqsg_ctx_s* c = st->ctx;
+    int nf = __builtin_popcountll(mask);
+    uint64_t units = st->amps >> nf;
+    const bool vec2 = sizeof(R) == 4 && (mask & 1ull) == 0 && units >= 2;
+    if (vec2) units >>= 1;
+    const unsigned grid = stream_grid(st, units, kRedThreads);
+    if (int rc = ensure_scratch(c->partial, sizeof(double) * (grid + 1))) return rc;
+    double* partial = (double*)c->partial.ptr;
+    auto go = [&](auto fx) {
+        if (vec2) {
+            if constexpr (sizeof(R) == 4)
+                k_prob_partial<R, 2, decltype(fx)><<<grid, kRedThreads, 0, c->stream>>>(
+                    (const T*)st->d, fx, units, partial);
+        } else {
+            k_prob_partial<R, 1, decltype(fx)><<<grid, kRedThreads, 0, c->stream>>>(
+                (const T*)st->d, fx, units, partial);
+        }
+    };
+    if (nf == 0) {
+        Fix<0> fx;
+        fx.pos[0] = 0;
+        fx.val = 0;
+        go(fx);
+    } else {
+        FixN fx;
+        fx.nf = 0;
+        for (int b = 0; b < 64; ++b)
+            if ((mask >> b) & 1ull) fx.pos[fx.nf++] = (uint32_t)b;
+        fx.val = val & mask;
+        go(fx);
+    }
+    k_sum_partials<<<1, 256, 0, c->stream>>>(partial, (int)grid, partial + grid);
+    c->launches += 2;
+    AQSG_CUDA_TRY(cudaGetLastError());
+    AQSG_CUDA_TRY(cudaMemcpyAsync(c->host_result, partial + grid, sizeof(double),
+                                  cudaMemcpyDeviceToHost, c->stream));
+    AQSG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    *out = c->host_result[0];
+    return AQSG_OK;
+}
+
+int reduce_prob(aqsg_state_s* st, uint64_t mask, uint64_t val, double* out) {
+    return st->dtype == AQSG_C64 ? reduce_prob_t<float>(st, mask, val, out)
+                                 : reduce_prob_t<double>(st, mask, val, out);
+}
+
+// ---- all probabilities ------------------------------------------------------------
+
+// float output follows af::real(sv * af::conjg(sv)) (quantum.cpp:408):
+// re*re - im*(-im), uncontracted.
+template <typename T>
+__global__ void k_probs(const T* __restrict__ sv, uint64_t N, void* out, int out_dtype) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const T a = sv[i];
+        if (out_dtype == 0) {
+            const float re = (float)a.x, im = (float)a.y;
+            ((float*)out)[i] = __fsub_rn(__fmul_rn(re, re), __fmul_rn(im, -im));
+        } else {
+            ((double*)out)[i] = (double)a.x * (double)a.x + (double)a.y * (double)a.y;
+        }
+    }
+}
+
+int launch_probs(aqsg_state_s* st, void* dev_out, int out_dtype) {
+    const unsigned grid = stream_grid(st, st->amps, 256);
+    if (st->dtype == AQSG_C64)
+        k_probs<float2><<<grid, 256, 0, st->ctx->stream>>>((const float2*)st->d, st->amps, dev_out, out_dtype);
+    else
+        k_probs<double2><<<grid, 256, 0, st->ctx->stream>>>((const double2*)st->d, st->amps, dev_out, out_dtype);
+    st->ctx->launches++;
+    AQSG_CUDA_TRY(cudaGetLastError());
+    return AQSG_OK;
+}
+
+// ---- sampling ----------------------------------------------------------------------
+//
+// The reference draws u ~ U[0,1) and returns the first index whose inclusive
+// cumulative probability exceeds u (af::accum + af::where, quantum.cpp:344-359;
+// profile_measure_all repeats this per shot with R x 2^n temporaries,
+// quantum.cpp:467-501).  Here: (1) FP64 sums of 2^CB-amplitude chunks,
+// (2) an inclusive scan of the chunk sums, (3) one warp per shot: binary
+// search over chunks, then a warp-level prefix scan inside the chunk.
+
+constexpr int kChunkBits = 12;
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_chunk_sums(const T* __restrict__ sv, int cb, double* sums) {
+    __shared__ double sh[32];
+    const uint64_t base = (uint64_t)blockIdx.x << cb;
+    const uint64_t len = 1ull << cb;
+    double acc = 0;
+    for (uint64_t j = threadIdx.x; j < len; j += blockDim.x) {
+        const T a = sv[base + j];
+        acc += (double)a.x * a.x + (double)a.y * a.y;
+    }
+    const double s = block_sum(acc, sh);
+    if (threadIdx.x == 0) sums[blockIdx.x] = s;
+}
+
+// Inclusive scan of `count` values by one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_scan(const double* in, double* out, uint64_t count) {
+    __shared__ double sh[1024];
+    const uint64_t per = (count + blockDim.x - 1) / blockDim.x;
+    const uint64_t b = threadIdx.x * per;
+    const uint64_t e = b + per < count ? b + per : count;
+    double s = 0;
+    for (uint64_t i = b; i < e; ++i) s += in[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    // Hillis-Steele scan over the thread totals
+    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+        double v = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0.0;
+        __syncthreads();
+        sh[threadIdx.x] += v;
+        __syncthreads();
+    }
+    double run = threadIdx.x ? sh[threadIdx.x - 1] : 0.0;
+    for (uint64_t i = b; i < e; ++i) {
+        run += in[i];
+        out[i] = run;
+    }
+}
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy
+// as 1, 2, 3", SC'11): counter (shot, 0, 0, 0), key = seed.
+__host__ __device__ inline void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+    for (int r = 0; r < 10; ++r) {
+        if (r) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+        const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0;
+        c[1] = lo1;
+        c[2] = n2;
+        c[3] = lo0;
+    }
+}
+
+__device__ inline double philox_uniform(uint64_t seed, uint64_t shot) {
+    uint32_t c[4] = {(uint32_t)shot, (uint32_t)(shot >> 32), 0u, 0u};
+    philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    const uint64_t m = ((uint64_t)(c[0] >> 5) << 26) | (uint64_t)(c[1] >> 6);
+    return (double)m * (1.0 / 9007199254740992.0);
+}
+
+template <typename T>
+__device__ __forceinline__ double pr(const T a) {
+    return (double)a.x * a.x + (double)a.y * a.y;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_sample(const T* __restrict__ sv, int cb, uint64_t nchunks, const double* __restrict__ prefix,
+         const double* __restrict__ us, uint64_t seed, int seeded, uint64_t count, int rule,
+         uint64_t* out) {
+    const uint64_t shot = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (shot >= count) return;
+    const double u = seeded ? philox_uniform(seed, shot) : us[shot];
+    const double total = prefix[nchunks - 1];
+    const uint64_t clen = 1ull << cb;
+    uint64_t result = 0;
+    if (u < total) {
+        // first chunk with inclusive prefix > u
+        uint64_t lo = 0, hi = nchunks - 1;
+        while (lo < hi) {
+            const uint64_t mid = (lo + hi) >> 1;
+            if (prefix[mid] > u) hi = mid; else lo = mid + 1;
+        }
+        const uint64_t c = lo;
+        double run = c ? prefix[c - 1] : 0.0;
+        const uint64_t base = c << cb;
+        uint64_t found = base + clen - 1;  // rounding fallback: chunk's last index
+        for (uint64_t s = 0; s < clen; s += 64) {
+            // lane holds amplitudes base+s+2*lane and +1 (chunks have >= 2 amps)
+            const uint64_t j = base + s + 2 * lane;
+            const bool in = s + 2 * lane < clen;
+            const double p0 = in ? pr(sv[j]) : 0.0;
+            const double p1 = (in && s + 2 * lane + 1 < clen) ? pr(sv[j + 1]) : 0.0;
+            double incl = p0 + p1;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const double v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            const unsigned hit = __ballot_sync(0xffffffffu, run + incl > u);
+            if (hit) {
+                const int L = __ffs(hit) - 1;
+                const double excl = __shfl_sync(0xffffffffu, incl - p0 - p1, L);
+                const double q0 = __shfl_sync(0xffffffffu, p0, L);
+                found = base + s + 2 * L + ((run + excl + q0 > u) ? 0 : 1);
+                break;
+            }
+            run += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        result = found;
+    } else if (rule == AQSG_SAMPLE_CLAMP) {
+        // last index of non-zero probability: first chunk reaching the total
+        uint64_t lo = 0, hi = nchunks - 1;
+        while (lo < hi) {
+            const uint64_t mid = (lo + hi) >> 1;
+            if (prefix[mid] >= total) hi = mid; else lo = mid + 1;
+        }
+        const uint64_t base = lo << cb;
+        uint64_t last = base;
+        for (uint64_t s = 0; s < clen; s += 32) {
+            const uint64_t j = base + s + lane;
+            const bool nz = (s + lane < clen) && pr(sv[j]) > 0.0;
+            const unsigned m = __ballot_sync(0xffffffffu, nz);
+            if (m) last = base + s + (31 - __clz(m));
+        }
+        result = last;
+    }
+    if (lane == 0) out[shot] = result;
+}
+
+template <typename T>
+static int sample_t(aqsg_state_s* st, const double* host_u, uint64_t seed, bool seeded,
+                    uint64_t count, int rule, uint64_t* host_out) {
+    aqsg_ctx_s* c = st->ctx;
+    const int cb = st->n < kChunkBits ? st->n : kChunkBits;
+    const uint64_t nchunks = st->amps >> cb;
+    if (int rc = ensure_scratch(c->partial, sizeof(double) * nchunks)) return rc;
+    if (int rc = ensure_scratch(c->prefix, sizeof(double) * nchunks)) return rc;
+    if (int rc = ensure_scratch(c->sample_o, sizeof(uint64_t) * count)) return rc;
+    if (!seeded) {
+        if (int rc = ensure_scratch(c->sample_u, sizeof(double) * count)) return rc;
+        AQSG_CUDA_TRY(cudaMemcpyAsync(c->sample_u.ptr, host_u, sizeof(double) * count,
+                                      cudaMemcpyHostToDevice, c->stream));
+    }
+    k_chunk_sums<T><<<(unsigned)nchunks, 256, 0, c->stream>>>((const T*)st->d, cb, (double*)c->partial.ptr);
+    k_scan<<<1, 1024, 0, c->stream>>>((const double*)c->partial.ptr, (double*)c->prefix.ptr, nchunks);
+    const uint64_t threads = count * 32;
+    const unsigned grid = (unsigned)((threads + 255) / 256);
+    k_sample<T><<<grid, 256, 0, c->stream>>>((const T*)st->d, cb, nchunks, (const double*)c->prefix.ptr,
+                                              seeded ? nullptr : (const double*)c->sample_u.ptr, seed,
+                                              seeded ? 1 : 0, count, rule, (uint64_t*)c->sample_o.ptr);
+    c->launches += 3;
+    AQSG_CUDA_TRY(cudaGetLastError());
+    AQSG_CUDA_TRY(cudaMemcpyAsync(host_out, c->sample_o.ptr, sizeof(uint64_t) * count,
+                                  cudaMemcpyDeviceToHost, c->stream));
+    AQSG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return AQSG_OK;
+}
+
+int sample(aqsg_state_s* st, const double* host_u, uint64_t seed, bool seeded, uint64_t count,
+           int rule, uint64_t* host_out) {
+    return st->dtype == AQSG_C64 ? sample_t<float2>(st, host_u, seed, seeded, count, rule, host_out)
+                                 : sample_t<double2>(st, host_u, seed, seeded, count, rule, host_out);
+}
+
+// ---- collapse of one qubit: one pass, reads only the kept branch -------------------
+
+template <typename T, typename R>
+__global__ void k_collapse(T* sv, uint64_t units, int bitpos, int outcome, R scale) {
+    for (uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < units;
+         u += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t lo = u & ((1ull << bitpos) - 1ull);
+        const uint64_t i0 = ((u - lo) << 1) | lo;  // bit = 0
+        const uint64_t keep = outcome ? (i0 | (1ull << bitpos)) : i0;
+        const uint64_t drop = outcome ? i0 : (i0 | (1ull << bitpos));
+        T a = sv[keep];
+        a.x *= scale;
+        a.y *= scale;
+        sv[keep] = a;
+        T z;
+        z.x = 0;
+        z.y = 0;
+        sv[drop] = z;
+    }
+}
+
+int launch_collapse_qubit(aqsg_state_s* st, uint64_t mask, int outcome, double scale) {
+    int bitpos = 0;
+    while (!((mask >> bitpos) & 1ull)) ++bitpos;
+    const uint64_t units = st->amps >> 1;
+    const unsigned grid = stream_grid(st, units, 256);
+    if (st->dtype == AQSG_C64)
+        k_collapse<float2, float><<<grid, 256, 0, st->ctx->stream>>>((float2*)st->d, units, bitpos,
+                                                                     outcome, (float)scale);
+    else
+        k_collapse<double2, double><<<grid, 256, 0, st->ctx->stream>>>((double2*)st->d, units, bitpos,
+                                                                       outcome, scale);
+    st->ctx->launches++;
+    AQSG_CUDA_TRY(cudaGetLastError());
+    return AQSG_OK;
+}
+
+// ---- <Z_q> and <Z_q Z_q+1> in one pass -----------------------------------------------
+//
+// Block b owns the contiguous range [b 2^RB, (b+1) 2^RB).  Thread t reads
+// j = s * nthreads + t, so index bits below TB = log2(nthreads) are the
+// thread's own (constant), bits TB..RB-1 are the loop counter s, bits >= RB
+// are the block's.  Per thread: total T, per-s-bit sums S and neighbour-pair
+// parity sums X (at most 12 + 11 doubles).  Each block writes
+// [T, S1[0..RB), X[0..RB-1)] over its bits; a final kernel folds in the block
+// bits and sums blocks in a fixed order.
+
+constexpr int kZMaxS = 12;
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_expz_partial(const T* __restrict__ sv, int tb, int rb, double* partial) {
+    __shared__ double sh[32];
+    const int sb = rb - tb;
+    const uint64_t base = (uint64_t)blockIdx.x << rb;
+    const uint64_t nt = 1ull << tb;  // threads that own indices (<= blockDim.x)
+    double tot = 0, S[kZMaxS], X[kZMaxS];
+#pragma unroll
+    for (int i = 0; i < kZMaxS; ++i) { S[i] = 0; X[i] = 0; }
+    const uint64_t iters = threadIdx.x < nt ? (1ull << sb) : 0;
+    for (uint64_t s = 0; s < iters; ++s) {
+        const double p = pr(sv[base + s * nt + threadIdx.x]);
+        tot += p;
+#pragma unroll
+        for (int i = 0; i < kZMaxS; ++i) {
+            if (i < sb) {
+                const uint64_t bi = (s >> i) & 1ull;
+                if (bi) S[i] += p;
+                if (i + 1 < sb && (bi ^ ((s >> (i + 1)) & 1ull))) X[i] += p;
+            }
+        }
+    }
+    const int stride = 2 * rb;
+    double* out = partial + (uint64_t)blockIdx.x * stride;
+    const double btot = block_sum(tot, sh);
+    if (threadIdx.x == 0) out[0] = btot;
+    // S1[q] for q < rb
+    for (int q = 0; q < rb; ++q) {
+        double v;
+        if (q < tb) v = ((threadIdx.x >> q) & 1) ? tot : 0.0;
+        else v = S[q - tb < kZMaxS ? q - tb : 0];
+        const double r = block_sum(v, sh);
+        if (threadIdx.x == 0) out[1 + q] = r;
+    }
+    // X[q] for pairs (q, q+1), q < rb - 1
+    for (int q = 0; q + 1 < rb; ++q) {
+        double v;
+        if (q + 1 < tb) v = (((threadIdx.x >> q) ^ (threadIdx.x >> (q + 1))) & 1) ? tot : 0.0;
+        else if (q + 1 == tb) v = ((threadIdx.x >> q) & 1) ? tot - S[0] : S[0];
+        else v = X[q - tb < kZMaxS ? q - tb : 0];
+        const double r = block_sum(v, sh);
+        if (threadIdx.x == 0) out[1 + rb + q] = r;
+    }
+}
+
+// One thread per output value: threads [0, n) -> S1 over index bits,
+// [n, 2n-1) -> X over neighbour bit pairs, thread 2n-1 -> total.
+__global__ void k_expz_final(const double* partial, int n, int rb, uint64_t nblocks, double* res) {
+    const int t = threadIdx.x;
+    if (t >= 2 * n) return;
+    const int stride = 2 * rb;
+    double acc = 0;
+    for (uint64_t b = 0; b < nblocks; ++b) {
+        const double* p = partial + b * stride;
+        const uint64_t base = b << rb;
+        const double T = p[0];
+        if (t < n) {
+            const int q = t;
+            acc += q < rb ? p[1 + q] : (((base >> q) & 1ull) ? T : 0.0);
+        } else if (t < 2 * n - 1) {
+            const int q = t - n;
+            if (q + 1 < rb) acc += p[1 + rb + q];
+            else if (q + 1 == rb) acc += ((base >> rb) & 1ull) ? T - p[1 + q] : p[1 + q];
+            else acc += ((((base >> q) ^ (base >> (q + 1))) & 1ull) ? T : 0.0);
+        } else {
+            acc += T;
+        }
+    }
+    res[t] = acc;
+}
+
+template <typename T>
+static int expect_z_t(aqsg_state_s* st, double* z, double* zz) {
+    aqsg_ctx_s* c = st->ctx;
+    const int n = st->n;
+    const int rb = n < 20 ? n : 20;
+    int tb = rb < 8 ? rb : 8;
+    if (rb - tb > kZMaxS) tb = rb - kZMaxS;
+    const uint64_t nblocks = st->amps >> rb;
+    const size_t pbytes = sizeof(double) * (nblocks * 2 * rb + 2 * n + 1);
+    if (int rc = ensure_scratch(c->partial, pbytes)) return rc;
+    double* partial = (double*)c->partial.ptr;
+    double* res = partial + nblocks * 2 * rb;
+    // at least one full warp: the block reductions shuffle over all 32 lanes
+    const int threads = (1 << tb) < 32 ? 32 : (1 << tb);
+    k_expz_partial<T><<<(unsigned)nblocks, threads, 0, c->stream>>>((const T*)st->d, tb, rb, partial);
+    k_expz_final<<<1, 128, 0, c->stream>>>(partial, n, rb, nblocks, res);
+    c->launches += 2;
+    AQSG_CUDA_TRY(cudaGetLastError());
+    std::vector<double> h(2 * n);
+    AQSG_CUDA_TRY(cudaMemcpyAsync(h.data(), res, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, c->stream));
+    AQSG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    const double tot = h[2 * n - 1];
+    for (int q = 0; q < n; ++q) {
+        const int bq = n - 1 - q;
+        if (z) z[q] = tot - 2.0 * h[bq];
+        if (zz && q + 1 < n) zz[q] = tot - 2.0 * h[n + (n - 2 - q)];
+    }
+    return AQSG_OK;
+}
+
+int expect_z(aqsg_state_s* st, double* z, double* zz) {
+    return st->dtype == AQSG_C64 ? expect_z_t<float2>(st, z, zz) : expect_z_t<double2>(st, z, zz);
+}
+
+}  // namespace aqsg

@@ -1,0 +1,427 @@
+#!/usr/bin/env python3
+"""Benchmark of the engine's hot path: QSimulator::simulate on the full
+quantum Fourier transform.
+
+Workload (default): 30-qubit complex64 register holding i.i.d. standard-normal
+complex amplitudes (normalised, seed 3); circuit = aqs::fourier_transform(30)
+(H + controlled-phase ladder, src/quantum_algo.cpp:103-114) plus the final
+Swap(i, 29-i) for i < 15: 30 H + 435 CPhase + 15 Swap = 480 gate
+applications, one gate per kernel pass over HBM.  A "step" is one pass of the
+whole circuit over the resident register.  The register (8 GiB) is larger
+than L2, so no L2 flush is needed between steps.
+
+Printed: one JSON line (rank 0).  `value` is gate applications per second
+with the register resident in HBM; `e2e` is the same metric through the
+public C-ABI with the register uploaded from pinned host memory and the result
+downloaded every step; `roofline` is the dominant kernel (controlled-phase
+pass) against the measured HBM copy bandwidth; `cpu_baseline` is the
+per-gate CPU restatement (oracle port, all host threads) on a bounded sample
+of the same workload.
+
+`--impl reference` times the CPU implementation instead (rank 0 only).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+GiB = 1 << 30
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=30, help="qubits")
+    ap.add_argument("--dtype", choices=["c64", "c128"], default="c64")
+    ap.add_argument("--mode", choices=["per_gate", "tiled"], default="per_gate")
+    ap.add_argument("--cpu-sample-ops", type=int, default=8,
+                    help="QFT gates in the CPU-baseline sample")
+    ap.add_argument("--no-extras", action="store_true")
+    return ap.parse_args()
+
+
+# ---- workload ---------------------------------------------------------------------
+
+def qft_ops(n):
+    import afquantumsim_gb300 as aq
+    return aq.fourier_transform(n, swaps=True)
+
+
+def algorithmic_bytes(n, amp_bytes):
+    """Bytes a gate can change (read + write) summed over the QFT:
+    H: N amplitudes, CPhase: N/4 (control = target = 1), Swap: N/2."""
+    N = 1 << n
+    nh, ncp, nsw = n, n * (n - 1) // 2, n // 2
+    per = {"H": 2 * amp_bytes * N, "CPhase": 2 * amp_bytes * N // 4, "Swap": 2 * amp_bytes * N // 2}
+    total = nh * per["H"] + ncp * per["CPhase"] + nsw * per["Swap"]
+    return total, per, (nh, ncp, nsw)
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---- clocks -------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid: str | None):
+        self.uuid = uuid
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            if self.uuid and self.uuid not in f[0]:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---- CPU baseline -----------------------------------------------------------------
+
+def cpu_baseline(n, host_sv, sample_ops, dtype):
+    """Per-gate CPU restatement of the reference's simulate (oracle port) on
+    the first `sample_ops` gates of the workload, all host threads."""
+    from oracle import oracle
+    threads = len(os.sched_getaffinity(0))
+    oracle.set_threads(threads)
+    ops = qft_ops(n)[:sample_ops]
+    t0 = time.perf_counter()
+    if dtype == "c64":
+        oracle.apply_f32(host_sv, ops)
+    else:
+        oracle.apply_f64(host_sv, ops)
+    dt = time.perf_counter() - t0
+    kinds = {}
+    for o in ops:
+        kinds[o.kind] = kinds.get(o.kind, 0) + 1
+    return {"value": len(ops) / dt, "unit": "gate-apps/s", "cores": threads, "kind": "port",
+            "sample": f"first {len(ops)} gates of the {n}-qubit QFT ({kinds.get(4, 0)} H, "
+                      f"{kinds.get(14, 0)} CPhase) on the full 2^{n} register, {dtype}, "
+                      f"{dt:.1f} s", "seconds": dt}
+
+
+def reference_algorithm_small(n=12):
+    """The reference ALGORITHM (dense Kronecker / CSR operators, faithful FP32
+    restatement) on the n-qubit QFT: context for how the reference scales."""
+    from oracle import oracle
+    ops = qft_ops(n)
+    v = np.zeros(1 << n, dtype=np.complex64)
+    v[0] = 1
+    t0 = time.perf_counter()
+    oracle.ref32_apply(v, n, ops)
+    dt = time.perf_counter() - t0
+    return {"n": n, "gate_apps_per_s": len(ops) / dt, "seconds": dt}
+
+
+# ---- our arm ------------------------------------------------------------------------
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import afquantumsim_gb300 as aq
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    n = args.n
+    N = 1 << n
+    dt_np = np.complex64 if args.dtype == "c64" else np.complex128
+    dt_t = torch.complex64 if args.dtype == "c64" else torch.complex128
+    amp_b = 8 if args.dtype == "c64" else 16
+    mode = aq.EXEC_PER_GATE if args.mode == "per_gate" else aq.EXEC_TILED
+
+    ctx = aq.Context(local_rank)
+    st = aq.State(ctx, n, aq.C64 if args.dtype == "c64" else aq.C128)
+
+    # seeded input, normalised, staged in pinned host memory (not timed)
+    g = torch.Generator(device=dev)
+    g.manual_seed(3 + rank)
+    x = torch.randn(N, dtype=dt_t, device=dev, generator=g)
+    x /= torch.linalg.vector_norm(x)
+    host_in = torch.empty(N, dtype=dt_t, pin_memory=True)
+    host_in.copy_(x)
+    del x
+    torch.cuda.synchronize()
+    host_out = torch.empty(N, dtype=dt_t, pin_memory=True)
+
+    ops = aq.op_array(qft_ops(n))
+    total_bytes, per_kind, counts = algorithmic_bytes(n, amp_b)
+    gates = len(ops)
+
+    stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=dev)
+
+    st.upload_ptr(host_in.data_ptr())
+    for _ in range(args.warmup):
+        st.apply(ops, mode)
+    ctx.synchronize()
+
+    uuid = None
+    try:
+        uuid = str(torch.cuda.get_device_properties(local_rank).uuid)
+    except Exception:
+        pass
+
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = ctx.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(uuid) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            st.apply(ops, mode)
+        ev1.record(stream)
+        ev1.synchronize()
+    torch.cuda.synchronize()
+    launches = ctx.launch_count() - launches0
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        torch.distributed.barrier()
+    ms_per_step = ms / args.steps
+    value = world * gates * args.steps / (ms / 1e3)
+    hbm_gbs = world * total_bytes * args.steps / (ms / 1e3) / 1e9
+
+    # dominant kernel in isolation: the controlled-phase pass (N/4 amplitudes)
+    cp_ops = aq.op_array([o for o in qft_ops(n) if o.kind == aq.kinds.CPHASE])
+    h_ops = aq.op_array([o for o in qft_ops(n) if o.kind == aq.kinds.H])
+    sw_ops = aq.op_array([o for o in qft_ops(n) if o.kind == aq.kinds.SWAP])
+
+    def per_launch_ms(arr, reps=1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        st.apply(arr, aq.EXEC_PER_GATE)
+        e0.record(stream)
+        for _ in range(reps):
+            st.apply(arr, aq.EXEC_PER_GATE)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / (reps * len(arr))
+
+    cp_ms = per_launch_ms(cp_ops)
+    h_ms = per_launch_ms(h_ops, 2)
+    sw_ms = per_launch_ms(sw_ops, 2)
+    peak, peak_kind = measured_peaks()
+    cp_achieved = per_kind["CPhase"] / (cp_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "k_diag1 (CPhase pass)",
+                "achieved": round(cp_achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(cp_achieved / peak, 4), "peak_source": peak_kind,
+                "traffic": TRAFFIC_PER_LAUNCH.get((n, args.dtype)),
+                "algorithmic_bytes_per_launch": per_kind["CPhase"],
+                "ms_per_launch": round(cp_ms, 4)}
+    kernels = {
+        "H_pass": {"ms": round(h_ms, 4), "GBps": round(per_kind["H"] / (h_ms / 1e3) / 1e9, 1)},
+        "CPhase_pass": {"ms": round(cp_ms, 4), "GBps": round(cp_achieved, 1)},
+        "Swap_pass": {"ms": round(sw_ms, 4), "GBps": round(per_kind["Swap"] / (sw_ms / 1e3) / 1e9, 1)},
+    }
+
+    # end to end through the C-ABI with host buffers: upload, simulate, download
+    e2e_steps = max(2, min(args.steps, 3))
+    st.upload_ptr(host_in.data_ptr())
+    st.apply(ops, mode)
+    st.download_ptr(host_out.data_ptr())
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        st.upload_ptr(host_in.data_ptr())
+        st.apply(ops, mode)
+        st.download_ptr(host_out.data_ptr())
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": round(world * gates * e2e_steps / e2e_s, 3), "unit": "gate-apps/s",
+           "h2d_bytes_per_step": N * amp_b, "d2h_bytes_per_step": N * amp_b,
+           "ms_per_step": round(e2e_s / e2e_steps * 1e3, 3)}
+
+    extras = {}
+    if not args.no_extras and rank == 0:
+        # the same circuit in shared-memory tiled mode, for comparison
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        st.apply(ops, aq.EXEC_TILED)
+        e0.record(stream)
+        for _ in range(2):
+            st.apply(ops, aq.EXEC_TILED)
+        e1.record(stream)
+        e1.synchronize()
+        extras["tiled_ms_per_step"] = round(e0.elapsed_time(e1) / 2, 3)
+
+    cpu = None
+    if rank == 0:
+        host_np = host_out.numpy()  # scratch register for the CPU sample
+        cpu = cpu_baseline(n, host_np, args.cpu_sample_ops, args.dtype)
+        if not args.no_extras:
+            extras["reference_algorithm_qft12"] = reference_algorithm_small(12)
+
+    st.free()
+    ctx.close()
+    if rank != 0:
+        return None
+    return {
+        "metric": f"QFT gate-apps/s at {n}q ({args.dtype}, one gate per pass) + HBM GB/s",
+        "value": round(value, 3),
+        "unit": "gate-apps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_per_step, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": args.dtype,
+        "data": "synthetic (seeded standard-normal complex amplitudes)",
+        "config": {"workload": f"qft{n}+swaps", "qubits": n, "gates": gates,
+                   "gate_mix": {"H": counts[0], "CPhase": counts[1], "Swap": counts[2]},
+                   "exec_mode": args.mode, "parallelism": f"replicas{world}",
+                   "l2": "register (2^%d x %d B) larger than L2; no flush" % (n, amp_b)},
+        "hbm_gbs": round(hbm_gbs, 1),
+        "hbm_frac": round(hbm_gbs / world / measured_peaks()[0], 4),
+        "algorithmic_bytes_per_step": total_bytes,
+        "e2e": e2e,
+        "roofline": roofline,
+        "kernels": kernels,
+        "cpu_baseline": {k: v for k, v in cpu.items() if k != "seconds"},
+        "clocks": clk.summary(),
+        "gpu_launches": int(launches),
+        "extras": extras,
+    }
+
+
+# DRAM bytes (read + write) of one controlled-phase launch from an ncu capture,
+# keyed by (qubits, dtype); see profiles/.
+TRAFFIC_PER_LAUNCH: dict = {}
+
+
+def run_reference(args):
+    """CPU implementation of the path (oracle port, all host threads) on the
+    same workload: a bounded sample of its gates per step."""
+    n = args.n
+    N = 1 << n
+    dt_np = np.complex64 if args.dtype == "c64" else np.complex128
+    rng = np.random.default_rng(3)
+    sv = np.empty(N, dtype=dt_np)
+    chunk = 1 << 24
+    for i in range(0, N, chunk):
+        m = min(chunk, N - i)
+        sv[i:i + m] = (rng.standard_normal(m) + 1j * rng.standard_normal(m)).astype(dt_np)
+    sv /= np.sqrt(np.vdot(sv, sv).real)
+    res = []
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        cpu_baseline(n, sv, 1, args.dtype)
+    for _ in range(args.steps):
+        res.append(cpu_baseline(n, sv, args.cpu_sample_ops, args.dtype))
+    tot_ops = sum(args.cpu_sample_ops for _ in res)
+    tot_s = sum(r["seconds"] for r in res)
+    value = tot_ops / tot_s
+    cb = {k: v for k, v in res[0].items() if k != "seconds"}
+    cb["value"] = value
+    return {
+        "impl": "reference",
+        "metric": f"QFT gate-apps/s at {n}q ({args.dtype}, one gate per pass) + HBM GB/s",
+        "value": round(value, 4),
+        "unit": "gate-apps/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(tot_s / args.steps * 1e3, 1),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": args.dtype,
+        "data": "synthetic (seeded standard-normal complex amplitudes)",
+        "config": {"workload": f"qft{n}+swaps", "qubits": n, "exec_mode": "cpu per-gate",
+                   "sample": cb["sample"]},
+        "cpu_baseline": cb,
+        "e2e": {"value": round(value, 4), "unit": "gate-apps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        print(json.dumps(run_reference(args)), flush=True)
+        return 0
+    if world > 1:
+        import torch
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl")
+    out = run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

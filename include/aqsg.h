@@ -1,0 +1,264 @@
+/*
+ * aqsg.h — C ABI of the GB300 state-vector engine (libaqsg.so).
+ *
+ * This is the drop-in boundary for the hot path of arrayfire/afQuantumSim:
+ * `aqs::QSimulator::simulate(const QCircuit&)` (src/quantum.cpp:277-291) and
+ * the state / measurement members of QSimulator that read the same state
+ * vector (src/quantum.cpp:212-531).  The reference has no C ABI: its callers
+ * use the C++ classes of include/quantum.h.  Each entry point below names the
+ * reference member it replaces.  The C++ layer `aqs::` (quantum.h of this
+ * project) binds these calls exactly as the reference's classes did.
+ *
+ * Conventions
+ *  - Qubit q of an n-qubit state is index bit (n-1-q): qubit 0 is the most
+ *    significant bit (src/quantum.cpp:546, :261-275).
+ *  - A state holds 2^n interleaved complex amplitudes, {float re, float im}
+ *    (AQSG_C64, the reference's c32 dtype, include/quantum.h:107-111) or
+ *    {double re, double im} (AQSG_C128).
+ *  - Every call returns an aqsg_status; 0 is success.  The negative codes map
+ *    one-to-one onto the exception classes the reference throws
+ *    (std::out_of_range, std::invalid_argument, std::domain_error,
+ *    std::runtime_error); aqsg_last_error() returns the message text.
+ *  - The library owns device buffers; the caller owns host buffers.  Work is
+ *    ordered on the context's CUDA stream; calls that return host data
+ *    synchronise that stream.
+ *  - A context and its states are used from one host thread at a time.
+ */
+#ifndef AQSG_H
+#define AQSG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AQSG_VERSION_MAJOR 0
+#define AQSG_VERSION_MINOR 1
+
+/* Largest register the engine allocates (c64: 2^34 * 8 B = 128 GiB). The
+ * reference caps circuits at 30 qubits (include/quantum.h:122); the C++ layer
+ * keeps that cap, the ABI allows a little more. */
+#define AQSG_MAX_QUBITS 34
+/* Largest dense unitary accepted by AQSG_OP_UNITARY (32 x 32). */
+#define AQSG_MAX_UNITARY_QUBITS 5
+/* Operand slots of one op. */
+#define AQSG_OP_MAX_QUBITS 5
+#define AQSG_OP_MAX_CONTROLS 16
+
+typedef enum aqsg_status {
+    AQSG_OK = 0,
+    AQSG_ERR_OUT_OF_RANGE = -1,     /* std::out_of_range in the reference   */
+    AQSG_ERR_INVALID_ARGUMENT = -2, /* std::invalid_argument                */
+    AQSG_ERR_DOMAIN = -3,           /* std::domain_error                    */
+    AQSG_ERR_RUNTIME = -4,          /* std::runtime_error                   */
+    AQSG_ERR_CUDA = -5,             /* CUDA runtime failure                 */
+    AQSG_ERR_OUT_OF_MEMORY = -6,    /* device allocation failed             */
+    AQSG_ERR_TIMEOUT = -7,          /* a bounded device wait gave up        */
+    AQSG_ERR_NULL = -8              /* NULL handle or buffer                */
+} aqsg_status;
+
+typedef enum aqsg_dtype {
+    AQSG_C64 = 0,  /* complex float32 (af::cfloat, the reference's c32) */
+    AQSG_C128 = 1  /* complex float64 */
+} aqsg_dtype;
+
+/* Gate kinds.  Values 0..20 follow QGate::GateTypes (include/quantum.h:
+ * 776-800) so a gate's type() maps straight onto a kind. */
+typedef enum aqsg_op_kind {
+    AQSG_OP_BARRIER = 0, /* Barrier          quantum.h:857-876 (no-op)           */
+    AQSG_OP_X = 1,       /* X(t)             quantum.cpp:540-562                 */
+    AQSG_OP_Y = 2,       /* Y(t)             quantum.cpp:580-609                 */
+    AQSG_OP_Z = 3,       /* Z(t)             quantum.cpp:627-653                 */
+    AQSG_OP_H = 4,       /* H(t)             quantum.cpp:812-831                 */
+    AQSG_OP_PHASE = 5,   /* Phase(t, a)      quantum.cpp:849-877                 */
+    AQSG_OP_SWAP = 6,    /* Swap(a, b)       quantum.cpp:912-952                 */
+    AQSG_OP_RX = 7,      /* RotX(t, a)       quantum.cpp:671-699                 */
+    AQSG_OP_RY = 8,      /* RotY(t, a)       quantum.cpp:718-746                 */
+    AQSG_OP_RZ = 9,      /* RotZ(t, a)       quantum.cpp:765-793                 */
+    AQSG_OP_CX = 10,     /* CX(c, t)         quantum.cpp:979-1014                */
+    AQSG_OP_CY = 11,     /* CY(c, t)         quantum.cpp:1041-1088               */
+    AQSG_OP_CZ = 12,     /* CZ(c, t)         quantum.cpp:1115-1152               */
+    AQSG_OP_CH = 13,     /* CH(c, t)         quantum.cpp:1342-1400               */
+    AQSG_OP_CPHASE = 14, /* CPhase(c, t, a)  quantum.cpp:1179-1218               */
+    AQSG_OP_CSWAP = 15,  /* CSwap(c, a, b)   quantum.cpp:1265-1313               */
+    AQSG_OP_CRX = 16,    /* CRotX(c, t, a)   quantum.cpp:1424-1436               */
+    AQSG_OP_CRY = 17,    /* CRotY(c, t, a)   quantum.cpp:1461-1473               */
+    AQSG_OP_CRZ = 18,    /* CRotZ(c, t, a)   quantum.cpp:1498-1510               */
+    AQSG_OP_CCX = 19,    /* CCNot(a, b, t)   quantum.cpp:1542-1580               */
+    AQSG_OP_OR = 20,     /* Or(a, b, t)      quantum.cpp:1614-1653               */
+    /* Dense k-qubit unitary, k = num_qubits <= AQSG_MAX_UNITARY_QUBITS.  The
+     * engine's form of Gate / ControlGate (quantum.cpp:1760-1814, 1888-1950):
+     * `matrix` is 2^k x 2^k complex, row-major, (re, im) pairs, and qubits[0]
+     * is the most significant bit of the matrix index, as in the reference's
+     * gen_index embedding (src/utils.cpp:157-167). */
+    AQSG_OP_UNITARY = 32
+} aqsg_op_kind;
+
+/* One gate application.  Fixed-arity kinds take their operands in the
+ * reference constructor's order in qubits[] (e.g. CX: {control, target};
+ * CCX: {control_a, control_b, target}; CSwap: {control, a, b}).  Any kind may
+ * carry extra controls: the op then acts only on basis states whose
+ * controls[i] bit equals bit i of control_values (the lowering of ControlGate
+ * and NControl_Gate, src/quantum_gates.cpp:80-182). */
+typedef struct aqsg_op {
+    int32_t kind;            /* aqsg_op_kind                                   */
+    int32_t num_qubits;      /* operands in qubits[] (UNITARY: k)              */
+    int32_t num_controls;    /* extra controls in controls[]                   */
+    uint32_t control_values; /* bit i: 1 = controls[i] fires on |1>, 0 on |0>  */
+    float angle;             /* radians, float like the reference's gates      */
+    int32_t qubits[AQSG_OP_MAX_QUBITS];
+    int32_t controls[AQSG_OP_MAX_CONTROLS];
+    const double* matrix;    /* UNITARY only                                   */
+} aqsg_op;
+
+/* Execution modes of aqsg_apply_ops.  All modes give the same results within
+ * the precision of the state's dtype. */
+typedef enum aqsg_exec_mode {
+    AQSG_EXEC_AUTO = 0,     /* planner picks (currently: TILED)               */
+    AQSG_EXEC_PER_GATE = 1, /* one kernel pass over HBM per gate               */
+    AQSG_EXEC_TILED = 2     /* gate runs staged in shared-memory tiles         */
+} aqsg_exec_mode;
+
+/* Sampling rule for aqsg_sample. */
+typedef enum aqsg_sample_rule {
+    /* First index whose inclusive cumulative probability exceeds u; 0 when no
+     * index does (u >= total).  This is peek_measure_all, quantum.cpp:344-359. */
+    AQSG_SAMPLE_REFERENCE = 0,
+    /* As above but an unmatched u returns the last index of non-zero
+     * probability instead of 0. */
+    AQSG_SAMPLE_CLAMP = 1
+} aqsg_sample_rule;
+
+typedef struct aqsg_ctx_s* aqsg_ctx;
+typedef struct aqsg_state_s* aqsg_state;
+
+/* ---- library / context -------------------------------------------------- */
+
+/* Version as major*100 + minor. */
+int aqsg_version(void);
+
+/* Copy the calling thread's last error message into buf (NUL-terminated,
+ * truncated to len).  Returns the full message length. */
+size_t aqsg_last_error(char* buf, size_t len);
+
+/* Open a context on CUDA device `device`, with its own stream.
+ * Replaces aqs::initialize(argc, argv, backend): include/quantum.h:138-139,
+ * src/quantum.cpp:69-86 (device selection; RNG seeding is explicit here). */
+int aqsg_init(int device, aqsg_ctx* out);
+
+/* Release a context.  States of the context must be freed first. */
+int aqsg_shutdown(aqsg_ctx ctx);
+
+/* Default execution mode for aqsg_apply_ops on this context. */
+int aqsg_set_exec_mode(aqsg_ctx ctx, int mode);
+
+/* Wait for all work queued on the context's stream. */
+int aqsg_synchronize(aqsg_ctx ctx);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that order their
+ * own work or timing events with the engine's. */
+int aqsg_ctx_stream(aqsg_ctx ctx, void** stream);
+
+/* Number of kernels this library launched on the context so far. */
+int aqsg_launch_count(aqsg_ctx ctx, uint64_t* out);
+
+/* ---- states -------------------------------------------------------------- */
+
+/* Allocate an n-qubit register (uninitialised).  The storage of
+ * QSimulator::statevector_ (include/quantum.h:738; quantum.cpp:212-259). */
+int aqsg_state_alloc(aqsg_ctx ctx, int n, int dtype, aqsg_state* out);
+int aqsg_state_free(aqsg_state st);
+int aqsg_state_info(aqsg_state st, int* n, int* dtype);
+
+/* Set the register to basis state |k>.  QSimulator(n, QState::zero()/one()):
+ * quantum.cpp:219-222 (zero -> k=0, one -> k=2^n-1). */
+int aqsg_state_set_basis_index(aqsg_state st, uint64_t k);
+
+/* Set the register to the product state q_0 (x) q_1 (x) ... (x) q_{n-1}.
+ * `amps` holds 4n floats: {re0, im0, re1, im1} per qubit, qubit 0 first.
+ * QSimulator::generate_statevector, quantum.cpp:261-275. */
+int aqsg_state_set_product(aqsg_state st, const float* amps);
+
+/* Copy 2^n host amplitudes (the state's dtype, interleaved) into the register.
+ * normalize != 0 divides by the 2-norm (computed in FP64) and rejects a null
+ * vector with AQSG_ERR_INVALID_ARGUMENT, as QSimulator(n, af::array)
+ * does (quantum.cpp:242-259). */
+int aqsg_state_upload(aqsg_state st, const void* host, int normalize);
+
+/* Copy the register to 2^n host amplitudes (the state's dtype).  Replaces
+ * QSimulator::statevector() / state(k) (include/quantum.h:726-734, 694-697). */
+int aqsg_state_download(aqsg_state st, void* host);
+
+/* Copy amplitudes [begin, begin+count) to the host. */
+int aqsg_state_download_range(aqsg_state st, uint64_t begin, uint64_t count,
+                              void* host);
+
+/* Copy src into dst (same n and dtype). */
+int aqsg_state_copy(aqsg_state dst, aqsg_state src);
+
+/* ---- simulation ----------------------------------------------------------- */
+
+/* Validate ops against an n-qubit register without running them.  Returns the
+ * status the reference's QGate::check would raise (src/quantum.cpp, the
+ * check() of each gate), with its message. */
+int aqsg_check_ops(int n, const aqsg_op* ops, int count);
+
+/* Apply ops in order to the register: the gate loop of
+ * QSimulator::simulate, quantum.cpp:285-290, with QGate::operator() of every
+ * gate class (quantum.cpp:533-1950) replaced by in-place kernels.
+ * mode: an aqsg_exec_mode, or -1 for the context default. */
+int aqsg_apply_ops(aqsg_state st, const aqsg_op* ops, int count, int mode);
+
+/* ---- measurement ---------------------------------------------------------- */
+
+/* Probability that `qubit` reads |1>, summed in FP64.
+ * QSimulator::qubit_probability_true, quantum.cpp:372-391. */
+int aqsg_qubit_prob(aqsg_state st, int qubit, double* out);
+
+/* |a_k|^2.  QSimulator::state_probability, quantum.cpp:393-402. */
+int aqsg_state_prob(aqsg_state st, uint64_t k, double* out);
+
+/* All 2^n probabilities |a_k|^2 to the host as float (out_dtype 0) or double
+ * (out_dtype 1).  QSimulator::probabilities, quantum.cpp:404-414. */
+int aqsg_probs(aqsg_state st, void* host, int out_dtype);
+
+/* Total probability sum_k |a_k|^2 in FP64. */
+int aqsg_norm2(aqsg_state st, double* out);
+
+/* Draw `count` outcomes for the uniforms u[0..count) from the FP64
+ * cumulative distribution of |a_k|^2 (rule: aqsg_sample_rule).  The index
+ * of each outcome goes to out[i].  peek_measure_all (quantum.cpp:344-359)
+ * is count = 1 with rule AQSG_SAMPLE_REFERENCE; profile_measure_all
+ * (quantum.cpp:467-501) is a histogram of count outcomes. */
+int aqsg_sample(aqsg_state st, const double* u, uint64_t count, int rule,
+                uint64_t* out);
+
+/* As aqsg_sample with the uniforms drawn on the device by Philox4x32-10
+ * from (seed, stream counter 0..count). */
+int aqsg_sample_seeded(aqsg_state st, uint64_t seed, uint64_t count, int rule,
+                       uint64_t* out);
+
+/* Measure `qubit` with uniform u: outcome = (u < p1), then zero the other
+ * branch and renormalise the kept one, in one pass.  The outcome goes to
+ * *outcome and its probability to *prob.  QSimulator::measure,
+ * quantum.cpp:308-342. */
+int aqsg_collapse_qubit(aqsg_state st, int qubit, double u, int* outcome,
+                        double* prob);
+
+/* Measure all qubits with uniform u (rule AQSG_SAMPLE_REFERENCE) and set the
+ * register to the basis state drawn.  QSimulator::measure_all,
+ * quantum.cpp:361-370. */
+int aqsg_collapse_all(aqsg_state st, double u, uint64_t* outcome);
+
+/* <Z_q> for every qubit q (z[n]) and <Z_q Z_{q+1}> for q = 0..n-2 (zz[n-1]),
+ * summed in FP64 in one pass.  Either pointer may be NULL.  <Z_q> is
+ * 1 - 2 * qubit_probability_true(q) (quantum.cpp:372-391). */
+int aqsg_expect_z(aqsg_state st, double* z, double* zz);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AQSG_H */
