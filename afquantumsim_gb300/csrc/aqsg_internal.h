@@ -32,7 +32,7 @@ enum LCls : int {
     L_PERM_OR = 2,   // as PERM_X, condition: (i & amask) != 0
     L_PERM_SWAP = 3, // swap (a=0,b=1) <-> (a=1,b=0) where the condition holds
     L_DIAG1 = 4,     // multiply amplitudes with (i & pmask) == pval by m[0]
-    L_DIAG2 = 5,     // target t: multiply t=0 by m[0], t=1 by m[1]
+    L_DIAG2 = 5,     // target t: multiply t=0 by m[0], t=1 by m[1] (complex slots)
     L_MAT2 = 6,      // 2x2 matrix on target t
     L_MATK = 7       // 2^k x 2^k matrix on bits tb[0..k) (tb[0] = MSB)
 };

@@ -95,9 +95,9 @@ k_pair(typename Cx<R>::T* __restrict__ sv, FX fx, uint64_t tmask, uint64_t amask
             if constexpr (OP == P_MAT2) {
                 lo[it].a[v] = cmul2(m.m[0], a, m.m[1], b);
                 hi[it].a[v] = cmul2(m.m[2], a, m.m[3], b);
-            } else if constexpr (OP == P_DIAG2) {
+            } else if constexpr (OP == P_DIAG2) {  // m[0] on t=0, m[1] on t=1
                 lo[it].a[v] = cmul(m.m[0], a);
-                hi[it].a[v] = cmul(m.m[3], b);
+                hi[it].a[v] = cmul(m.m[1], b);
             } else if constexpr (OP == P_PERMX) {
                 lo[it].a[v] = b;
                 hi[it].a[v] = a;
