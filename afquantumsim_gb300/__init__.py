@@ -34,7 +34,7 @@ EXPORTS = [
     "aqsg_state_download", "aqsg_state_download_range", "aqsg_state_copy",
     "aqsg_check_ops", "aqsg_apply_ops", "aqsg_qubit_prob", "aqsg_state_prob",
     "aqsg_probs", "aqsg_norm2", "aqsg_sample", "aqsg_sample_seeded",
-    "aqsg_collapse_qubit", "aqsg_collapse_all", "aqsg_expect_z",
+    "aqsg_collapse_qubit", "aqsg_collapse_all", "aqsg_expect_z", "aqsg_sample_noalloc",
 ]
 
 _lib = None
@@ -105,6 +105,7 @@ def load_library(path: os.PathLike | str | None = None) -> C.CDLL:
         "aqsg_collapse_qubit": ([P, I, D, C.POINTER(I), C.POINTER(D)], I),
         "aqsg_collapse_all": ([P, D, C.POINTER(U64)], I),
         "aqsg_expect_z": ([P, C.POINTER(D), C.POINTER(D)], I),
+        "aqsg_sample_noalloc": ([P, C.POINTER(D), U64, I, C.POINTER(U64)], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -370,6 +371,16 @@ class State:
         out = np.empty(u.size, dtype=np.uint64)
         _check(self.lib.aqsg_sample(self.h, u.ctypes.data_as(C.POINTER(C.c_double)), u.size, rule,
                                     out.ctypes.data_as(C.POINTER(C.c_uint64))))
+        return out
+
+    def sample_noalloc(self, u, rule: int = SAMPLE_REFERENCE) -> np.ndarray:
+        """aqsg_sample_noalloc: as sample(), with the library's static device
+        scratch instead of allocated buffers (for callers that cannot allocate
+        device memory while running)."""
+        u = np.ascontiguousarray(np.asarray(u, dtype=np.float64).reshape(-1))
+        out = np.empty(u.size, dtype=np.uint64)
+        _check(self.lib.aqsg_sample_noalloc(self.h, u.ctypes.data_as(C.POINTER(C.c_double)), u.size,
+                                            rule, out.ctypes.data_as(C.POINTER(C.c_uint64))))
         return out
 
     def sample_seeded(self, seed: int, count: int, rule: int = SAMPLE_REFERENCE) -> np.ndarray:

@@ -4,6 +4,8 @@
 // They replace the ArrayFire reductions of the reference's measurement
 // members (src/quantum.cpp:308-531), which sum in FP32.
 #include <cmath>
+#include <mutex>
+#include <string>
 
 #include "aqsg_internal.h"
 #include "common.cuh"
@@ -429,6 +431,96 @@ int sample(aqsg_state_s* st, const double* host_u, uint64_t seed, bool seeded, u
     return st->dtype == AQSG_C64 ? sample_t<float2>(st, host_u, seed, seeded, count, rule, host_out)
                                  : sample_t<double2>(st, host_u, seed, seeded, count, rule, host_out);
 }
+
+// ---- allocation-free sampling ----------------------------------------------------
+//
+// aqsg_sample_noalloc runs the three sampling kernels above on scratch carved
+// from one static device array instead of context buffers grown with
+// cudaMalloc.  Layout: chunk sums and chunk prefix sums (2^(30-12) doubles
+// each), then the call's uniforms and outcomes (AQSG_NOALLOC_MAX_SHOTS each).
+// Every buffer is fully written before it is read within a call, so nothing
+// has to be cleared between calls.
+
+constexpr uint64_t kNoallocChunks = 1ull << (AQSG_NOALLOC_MAX_QUBITS - kChunkBits);
+static_assert(AQSG_NOALLOC_SCRATCH_BYTES ==
+                  2 * sizeof(double) * kNoallocChunks + 16 * (size_t)AQSG_NOALLOC_MAX_SHOTS,
+              "scratch layout");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[AQSG_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kNoallocMaxDevices = 256;
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_addr[kNoallocMaxDevices];
+
+// Device address of the static scratch on `device`, looked up once per device
+// with that device current.  (In host code g_noalloc_scratch names a host-side
+// stand-in, not device memory, so only the looked-up address is passed on.)
+static int noalloc_scratch(int device, unsigned char** out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (device < 0 || device >= kNoallocMaxDevices)
+        return set_error(AQSG_ERR_OUT_OF_RANGE, "Device index beyond the allocation-free table");
+    if (!g_noalloc_addr[device]) {
+        AQSG_CUDA_TRY(cudaSetDevice(device));
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(allocation-free scratch)");
+        g_noalloc_addr[device] = p;
+    }
+    *out = (unsigned char*)g_noalloc_addr[device];
+    return AQSG_OK;
+}
+
+template <typename T>
+static int sample_noalloc_t(aqsg_state_s* st, const double* host_u, uint64_t count, int rule,
+                            uint64_t* host_out) {
+    aqsg_ctx_s* c = st->ctx;
+    unsigned char* base = nullptr;
+    if (int rc = noalloc_scratch(c->device, &base)) return rc;
+    const int cb = st->n < kChunkBits ? st->n : kChunkBits;
+    const uint64_t nchunks = st->amps >> cb;
+    double* sums = (double*)base;
+    double* prefix = sums + kNoallocChunks;
+    double* us = prefix + kNoallocChunks;
+    uint64_t* outs = (uint64_t*)(us + AQSG_NOALLOC_MAX_SHOTS);
+    AQSG_CUDA_TRY(cudaMemcpyAsync(us, host_u, sizeof(double) * count, cudaMemcpyHostToDevice, c->stream));
+    k_chunk_sums<T><<<(unsigned)nchunks, 256, 0, c->stream>>>((const T*)st->d, cb, sums);
+    k_scan<<<1, 1024, 0, c->stream>>>(sums, prefix, nchunks);
+    const unsigned grid = (unsigned)((count * 32 + 255) / 256);
+    k_sample<T><<<grid, 256, 0, c->stream>>>((const T*)st->d, cb, nchunks, prefix, us, 0, 0, count,
+                                              rule, outs);
+    c->launches += 3;
+    AQSG_CUDA_TRY(cudaGetLastError());
+    AQSG_CUDA_TRY(cudaMemcpyAsync(host_out, outs, sizeof(uint64_t) * count, cudaMemcpyDeviceToHost,
+                                  c->stream));
+    AQSG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return AQSG_OK;
+}
+
+}  // namespace aqsg
+
+extern "C" int aqsg_sample_noalloc(aqsg_state st, const double* u, uint64_t count, int rule,
+                                   uint64_t* out) {
+    using namespace aqsg;
+    if (!st || !st->d) return set_error(AQSG_ERR_NULL, "NULL state");
+    if (count == 0) return AQSG_OK;
+    if (!u || !out) return set_error(AQSG_ERR_NULL, "NULL buffer");
+    if (rule != AQSG_SAMPLE_REFERENCE && rule != AQSG_SAMPLE_CLAMP)
+        return set_error(AQSG_ERR_INVALID_ARGUMENT, "Unknown sampling rule");
+    if (st->n > AQSG_NOALLOC_MAX_QUBITS)
+        return set_error(AQSG_ERR_INVALID_ARGUMENT,
+                         "Allocation-free sampling supports at most " +
+                             std::to_string(AQSG_NOALLOC_MAX_QUBITS) + " qubits, register has " +
+                             std::to_string(st->n));
+    if (count > AQSG_NOALLOC_MAX_SHOTS)
+        return set_error(AQSG_ERR_INVALID_ARGUMENT,
+                         "Allocation-free sampling takes at most " +
+                             std::to_string(AQSG_NOALLOC_MAX_SHOTS) + " shots per call, got " +
+                             std::to_string(count));
+    return st->dtype == AQSG_C64 ? sample_noalloc_t<float2>(st, u, count, rule, out)
+                                 : sample_noalloc_t<double2>(st, u, count, rule, out);
+}
+
+namespace aqsg {
 
 // ---- collapse of one qubit: one pass, reads only the kept branch -------------------
 

@@ -240,6 +240,29 @@ int aqsg_sample(aqsg_state st, const double* u, uint64_t count, int rule,
 int aqsg_sample_seeded(aqsg_state st, uint64_t seed, uint64_t count, int rule,
                        uint64_t* out);
 
+/* Allocation-free sampling.  No counterpart in the reference: it exists for
+ * callers that must not allocate device memory once they are running — for
+ * example a serving loop that admits work against a fixed HBM budget, or a
+ * host that embeds the engine next to a framework's caching allocator — since
+ * cudaMalloc/cudaFree can synchronise the whole device and stall unrelated
+ * streams.  Same rule and results as aqsg_sample, but its device scratch is
+ * one static array of the library (AQSG_NOALLOC_SCRATCH_BYTES, held on every
+ * GPU that loads the library until the process exits) instead of buffers
+ * grown on demand.  The register must have at most AQSG_NOALLOC_MAX_QUBITS
+ * qubits and count must be at most AQSG_NOALLOC_MAX_SHOTS; larger requests
+ * fail with AQSG_ERR_INVALID_ARGUMENT.  The first call on a device looks up
+ * the array's device address; make that first call before any stream
+ * capture.  All calls on a device share the array: calls whose GPU work
+ * overlaps (other threads or streams) race and must be serialised by the
+ * caller. */
+#define AQSG_NOALLOC_MAX_QUBITS 30
+#define AQSG_NOALLOC_MAX_SHOTS 16384
+#define AQSG_NOALLOC_SCRATCH_BYTES \
+    ((size_t)2 * 8 * ((size_t)1 << (AQSG_NOALLOC_MAX_QUBITS - 12)) + \
+     (size_t)16 * AQSG_NOALLOC_MAX_SHOTS)
+int aqsg_sample_noalloc(aqsg_state st, const double* u, uint64_t count, int rule,
+                        uint64_t* out);
+
 /* Measure `qubit` with uniform u: outcome = (u < p1), then zero the other
  * branch and renormalise the kept one, in one pass.  The outcome goes to
  * *outcome and its probability to *prob.  QSimulator::measure,
