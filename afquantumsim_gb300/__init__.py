@@ -28,13 +28,16 @@ LIB_PATH = PKG_DIR / "_build" / "libaqsg.so"
 
 EXPORTS = [
     "aqsg_version", "aqsg_last_error", "aqsg_init", "aqsg_shutdown",
-    "aqsg_set_exec_mode", "aqsg_synchronize", "aqsg_ctx_stream", "aqsg_launch_count",
+    "aqsg_set_exec_mode", "aqsg_set_tensor_cores", "aqsg_synchronize", "aqsg_ctx_stream",
+    "aqsg_launch_count",
     "aqsg_state_alloc", "aqsg_state_free", "aqsg_state_info",
     "aqsg_state_set_basis_index", "aqsg_state_set_product", "aqsg_state_upload",
     "aqsg_state_download", "aqsg_state_download_range", "aqsg_state_copy",
     "aqsg_check_ops", "aqsg_apply_ops", "aqsg_qubit_prob", "aqsg_state_prob",
     "aqsg_probs", "aqsg_norm2", "aqsg_sample", "aqsg_sample_seeded",
     "aqsg_collapse_qubit", "aqsg_collapse_all", "aqsg_expect_z", "aqsg_sample_noalloc",
+    "aqsg_state_compare", "aqsg_compile", "aqsg_program_info", "aqsg_run_program", "aqsg_program_export",
+    "aqsg_program_free",
 ]
 
 _lib = None
@@ -82,6 +85,7 @@ def load_library(path: os.PathLike | str | None = None) -> C.CDLL:
         "aqsg_init": ([I, C.POINTER(P)], I),
         "aqsg_shutdown": ([P], I),
         "aqsg_set_exec_mode": ([P, I], I),
+        "aqsg_set_tensor_cores": ([P, I], I),
         "aqsg_synchronize": ([P], I),
         "aqsg_ctx_stream": ([P, C.POINTER(P)], I),
         "aqsg_launch_count": ([P, C.POINTER(U64)], I),
@@ -106,6 +110,7 @@ def load_library(path: os.PathLike | str | None = None) -> C.CDLL:
         "aqsg_collapse_all": ([P, D, C.POINTER(U64)], I),
         "aqsg_expect_z": ([P, C.POINTER(D), C.POINTER(D)], I),
         "aqsg_sample_noalloc": ([P, C.POINTER(D), U64, I, C.POINTER(U64)], I),
+        "aqsg_state_compare": ([P, P] + [C.POINTER(D)] * 5, I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -257,6 +262,9 @@ class Context:
     def set_exec_mode(self, mode: int) -> None:
         _check(self.lib.aqsg_set_exec_mode(self.h, mode))
 
+    def set_tensor_cores(self, enable: bool) -> None:
+        _check(self.lib.aqsg_set_tensor_cores(self.h, 1 if enable else 0))
+
     def synchronize(self) -> None:
         _check(self.lib.aqsg_synchronize(self.h))
 
@@ -336,6 +344,12 @@ class State:
 
     def download_ptr(self, ptr: int) -> None:
         _check(self.lib.aqsg_state_download(self.h, ptr))
+
+    def compare(self, other: "State"):
+        """(max |a - b|, <a|b>, |a|^2, |b|^2) in FP64, on the device."""
+        v = [C.c_double() for _ in range(5)]
+        _check(self.lib.aqsg_state_compare(self.h, other.h, *[C.byref(x) for x in v]))
+        return v[0].value, complex(v[1].value, v[2].value), v[3].value, v[4].value
 
     def copy_from(self, other: "State") -> None:
         _check(self.lib.aqsg_state_copy(self.h, other.h))
@@ -425,3 +439,57 @@ def qstate(zero, one):
         raise ValueError("Cannot normalize a null state")
     mag = np.float32(np.sqrt(mag2))
     return (q / mag).astype(np.float32)
+
+
+# ---- compiled programs (gate fusion) ----------------------------------------------
+
+def _bind_programs(lib):
+    P, I = C.c_void_p, C.c_int
+    lib.aqsg_compile.argtypes = [I, I, C.POINTER(Op), I, I, C.POINTER(P)]
+    lib.aqsg_program_info.argtypes = [P, C.POINTER(I), C.POINTER(I)]
+    lib.aqsg_run_program.argtypes = [P, P, I]
+    lib.aqsg_program_export.argtypes = [P, C.POINTER(Op), I, C.POINTER(I)]
+    lib.aqsg_program_free.argtypes = [P]
+    for f in ("aqsg_compile", "aqsg_program_info", "aqsg_run_program", "aqsg_program_export",
+              "aqsg_program_free"):
+        getattr(lib, f).restype = I
+
+
+class Program:
+    """aqsg_compile: ops fused into dense unitaries on <= max_qubits qubits."""
+
+    def __init__(self, n: int, ops, dtype: int = C64, max_qubits: int = 5):
+        self.lib = load_library()
+        _bind_programs(self.lib)
+        arr = op_array(list(ops))
+        h = C.c_void_p()
+        _check(self.lib.aqsg_compile(n, dtype, arr, len(arr), max_qubits, C.byref(h)))
+        self.h, self.n, self.dtype = h, n, dtype
+
+    def info(self):
+        f, s = C.c_int(), C.c_int()
+        _check(self.lib.aqsg_program_info(self.h, C.byref(f), C.byref(s)))
+        return f.value, s.value
+
+    def export(self):
+        """The fused ops as aqsg_op structs (matrices point into the program)."""
+        cnt = C.c_int()
+        _check(self.lib.aqsg_program_export(self.h, None, 0, C.byref(cnt)))
+        arr = (Op * cnt.value)()
+        _check(self.lib.aqsg_program_export(self.h, arr, cnt.value, C.byref(cnt)))
+        arr._prog = self  # keep the program (and its matrices) alive
+        return arr
+
+    def run(self, state: "State", mode: int = -1) -> None:
+        _check(self.lib.aqsg_run_program(state.h, self.h, mode))
+
+    def free(self) -> None:
+        if self.h:
+            _check(self.lib.aqsg_program_free(self.h))
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

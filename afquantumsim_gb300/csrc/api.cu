@@ -299,6 +299,8 @@ int aqsg_init(int device, aqsg_ctx* out) {
     cudaError_t e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMallocHost((void**)&c->host_result, 4096);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_err, 256);
+    if (e == cudaSuccess) e = cudaMemset(c->d_err, 0, 256);
     if (e != cudaSuccess) {
         if (c->stream) cudaStreamDestroy(c->stream);
         delete c;
@@ -319,6 +321,7 @@ int aqsg_shutdown(aqsg_ctx ctx) {
     for (Scratch* s : all)
         if (s->ptr) cudaFree(s->ptr);
     if (ctx->host_result) cudaFreeHost(ctx->host_result);
+    if (ctx->d_err) cudaFree(ctx->d_err);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
     return AQSG_OK;
@@ -329,6 +332,12 @@ int aqsg_set_exec_mode(aqsg_ctx ctx, int mode) {
     if (mode < AQSG_EXEC_AUTO || mode > AQSG_EXEC_TILED)
         return set_error(AQSG_ERR_INVALID_ARGUMENT, "Unknown execution mode");
     ctx->exec_mode = mode;
+    return AQSG_OK;
+}
+
+int aqsg_set_tensor_cores(aqsg_ctx ctx, int enable) {
+    if (!ctx) return set_error(AQSG_ERR_NULL, "NULL context");
+    ctx->tensor_cores = enable ? 1 : 0;
     return AQSG_OK;
 }
 

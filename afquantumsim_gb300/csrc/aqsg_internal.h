@@ -78,6 +78,8 @@ struct aqsg_ctx_s {
     aqsg::Scratch ops;       // device copy of tile-pass op tables
     aqsg::Scratch probs;     // probability download staging
     double* host_result = nullptr;  // pinned FP64 results
+    int* d_err = nullptr;           // device flag: a bounded kernel wait gave up
+    int tensor_cores = 1;           // fused unitaries on tcgen05 (c64 tiles)
 };
 
 struct aqsg_state_s {

@@ -1,0 +1,305 @@
+// Gate fusion: the engine's compile().
+//
+// The reference folds every gate of a circuit into one dense 2^n x 2^n
+// matrix (QCircuit::compile, src/quantum.cpp:199-210); that is O(8^n) work
+// and O(4^n) memory.  Here consecutive gates are folded into dense unitaries
+// on at most K <= 5 qubits (32 x 32), which the tile engine then applies as
+// one operation each (tensor-core contractions on the tile).
+//
+// Greedy in-order grouping.  A group may absorb the next gate when (1) no
+// later group touches any of the gate's qubits — then moving the gate up to
+// the group only crosses gates it commutes with — and (2) the union of the
+// qubits stays within K.  Each group's unitary is built on the host in FP64
+// by applying its gates to the 2^k basis vectors.
+#include <algorithm>
+#include <complex>
+#include <cstring>
+
+#include "aqsg_internal.h"
+
+struct aqsg_program_s {
+    int n = 0;
+    int dtype = AQSG_C64;
+    int source_ops = 0;
+    std::vector<aqsg::LOp> ops;
+    // the same ops in ABI form (fused groups as AQSG_OP_UNITARY whose matrix
+    // points into `mats`)
+    std::vector<aqsg_op> exported;
+    std::vector<std::vector<double>> mats;
+};
+
+namespace aqsg {
+
+using cd = std::complex<double>;
+
+static uint64_t support(const LOp& o) {
+    uint64_t s = o.cmask | o.amask;
+    if (o.t0 >= 0) s |= 1ull << o.t0;
+    if (o.t1 >= 0) s |= 1ull << o.t1;
+    for (int j = 0; j < o.k; ++j) s |= 1ull << o.tb[j];
+    return s;
+}
+
+// Apply one lowered op to a small host vector of 2^k amplitudes whose index
+// bits are the op's bits already remapped to local positions.
+static void host_apply(std::vector<cd>& v, const LOp& o) {
+    const uint64_t N = v.size();
+    auto coef = [&](int i) { return cd(o.m[2 * i], o.m[2 * i + 1]); };
+    auto ok = [&](uint64_t i) { return (i & o.cmask) == o.cval; };
+    switch (o.cls) {
+        case L_PERM_X: case L_PERM_OR: case L_MAT2: case L_DIAG2: {
+            const uint64_t t = 1ull << o.t0;
+            for (uint64_t i = 0; i < N; ++i) {
+                if ((i & t) || !ok(i)) continue;
+                const cd a = v[i], b = v[i | t];
+                if (o.cls == L_PERM_X || (o.cls == L_PERM_OR && (i & o.amask))) {
+                    v[i] = b;
+                    v[i | t] = a;
+                } else if (o.cls == L_MAT2) {
+                    v[i] = coef(0) * a + coef(1) * b;
+                    v[i | t] = coef(2) * a + coef(3) * b;
+                } else if (o.cls == L_DIAG2) {
+                    v[i] = coef(0) * a;
+                    v[i | t] = coef(1) * b;
+                }
+            }
+            break;
+        }
+        case L_DIAG1:
+            for (uint64_t i = 0; i < N; ++i)
+                if (ok(i)) v[i] *= coef(0);
+            break;
+        case L_PERM_SWAP: {
+            const uint64_t a = 1ull << o.t0, b = 1ull << o.t1;
+            for (uint64_t i = 0; i < N; ++i)
+                if (!(i & a) && (i & b) && ok(i)) std::swap(v[i], v[i ^ (a | b)]);
+            break;
+        }
+        case L_MATK: {
+            const int D = 1 << o.k;
+            uint64_t tm = 0, off[32];
+            for (int j = 0; j < o.k; ++j) tm |= 1ull << o.tb[j];
+            for (int r = 0; r < D; ++r) {
+                off[r] = 0;
+                for (int j = 0; j < o.k; ++j)
+                    if ((r >> (o.k - 1 - j)) & 1) off[r] |= 1ull << o.tb[j];
+            }
+            std::vector<cd> in(D);
+            for (uint64_t i = 0; i < N; ++i) {
+                if ((i & tm) || !ok(i)) continue;
+                for (int c = 0; c < D; ++c) in[c] = v[i | off[c]];
+                for (int r = 0; r < D; ++r) {
+                    cd acc = 0;
+                    for (int c = 0; c < D; ++c)
+                        acc += cd(o.mk[2 * (r * D + c)], o.mk[2 * (r * D + c) + 1]) * in[c];
+                    v[i | off[r]] = acc;
+                }
+            }
+            break;
+        }
+        default: break;
+    }
+}
+
+static uint64_t remap_mask(uint64_t m, const int* local) {
+    uint64_t r = 0;
+    for (int b = 0; b < 64; ++b)
+        if ((m >> b) & 1ull) r |= 1ull << local[b];
+    return r;
+}
+
+static LOp remap(const LOp& o, const int* local) {
+    LOp r = o;
+    if (r.t0 >= 0) r.t0 = local[r.t0];
+    if (r.t1 >= 0) r.t1 = local[r.t1];
+    for (int j = 0; j < r.k; ++j) r.tb[j] = local[r.tb[j]];
+    r.cmask = remap_mask(o.cmask, local);
+    r.cval = remap_mask(o.cval, local);
+    r.amask = remap_mask(o.amask, local);
+    return r;
+}
+
+struct Group {
+    uint64_t bits = 0;
+    std::vector<int> ops;  // indices into the input
+};
+
+// in[i] is the lowering of src[i].  Fills out (lowered) and exported (ABI
+// form) in parallel.
+static int fuse(int n, const std::vector<LOp>& in, const std::vector<aqsg_op>& src, int K,
+                aqsg_program_s* prog) {
+    std::vector<LOp>* out = &prog->ops;
+    std::vector<Group> groups;
+    int last[64];
+    std::fill(last, last + 64, -1);
+    for (int oi = 0; oi < (int)in.size(); ++oi) {
+        const LOp& o = in[oi];
+        if (o.cls == L_NOP) continue;
+        const uint64_t s = support(o);
+        int cand = -1;
+        for (int b = 0; b < 64; ++b)
+            if ((s >> b) & 1ull) cand = std::max(cand, last[b]);
+        int g;
+        if (cand >= 0 && __builtin_popcountll(groups[cand].bits | s) <= K) {
+            g = cand;
+        } else {
+            g = (int)groups.size();
+            groups.emplace_back();
+        }
+        groups[g].bits |= s;
+        groups[g].ops.push_back(oi);
+        for (int b = 0; b < 64; ++b)
+            if ((s >> b) & 1ull) last[b] = g;
+    }
+    out->clear();
+    prog->exported.clear();
+    prog->mats.clear();
+    prog->mats.reserve(groups.size());
+    for (const Group& gr : groups) {
+        bool all_diag = true;
+        for (int oi : gr.ops) all_diag = all_diag && in[oi].diagonal();
+        const int k = __builtin_popcountll(gr.bits);
+        // keep lone gates, diagonal-only groups and groups too wide to fuse
+        // (a gate with many controls) as they are
+        if (gr.ops.size() == 1 || all_diag || k > K) {
+            for (int oi : gr.ops) {
+                out->push_back(in[oi]);
+                prog->exported.push_back(src[oi]);
+                if (src[oi].kind == AQSG_OP_UNITARY) {  // point at a private copy
+                    if (in[oi].cls == L_MATK) prog->mats.push_back(in[oi].mk);
+                    else prog->mats.emplace_back(in[oi].m, in[oi].m + 8);
+                    prog->exported.back().matrix = prog->mats.back().data();
+                }
+            }
+            continue;
+        }
+        int local[64];
+        std::fill(local, local + 64, 0);
+        std::vector<int> bits;  // ascending global bits = local bit positions
+        for (int b = 0; b < 64; ++b)
+            if ((gr.bits >> b) & 1ull) {
+                local[b] = (int)bits.size();
+                bits.push_back(b);
+            }
+        std::vector<LOp> lops;
+        for (int oi : gr.ops) lops.push_back(remap(in[oi], local));
+        const int D = 1 << k;
+        LOp f;
+        f.k = k;
+        // matrix index MSB = highest global bit
+        for (int j = 0; j < k; ++j) f.tb[j] = bits[k - 1 - j];
+        f.mk.assign(2 * D * D, 0.0);
+        for (int c = 0; c < D; ++c) {
+            std::vector<cd> v(D, 0.0);
+            v[c] = 1.0;
+            for (const LOp& o : lops) host_apply(v, o);
+            // local index i has bit j <-> bits[j]; the matrix index r has
+            // bit (k-1-j') <-> tb[j'] = bits[k-1-j'], i.e. r == i
+            for (int r = 0; r < D; ++r) {
+                f.mk[2 * (r * D + c)] = v[r].real();
+                f.mk[2 * (r * D + c) + 1] = v[r].imag();
+            }
+        }
+        prog->mats.push_back(f.mk);
+        aqsg_op ex;
+        std::memset(&ex, 0, sizeof(ex));
+        ex.kind = AQSG_OP_UNITARY;
+        ex.num_qubits = k;
+        for (int j = 0; j < k; ++j) ex.qubits[j] = n - 1 - f.tb[j];
+        ex.matrix = prog->mats.back().data();
+        prog->exported.push_back(ex);
+        if (k == 1) {
+            f.cls = L_MAT2;
+            f.t0 = bits[0];
+            f.k = 0;
+            for (int e = 0; e < 8; ++e) f.m[e] = f.mk[e];
+            f.mk.clear();
+        } else {
+            f.cls = L_MATK;
+        }
+        out->push_back(std::move(f));
+    }
+    return AQSG_OK;
+}
+
+}  // namespace aqsg
+
+using namespace aqsg;
+
+extern "C" {
+
+int aqsg_compile(int n, int dtype, const aqsg_op* ops, int count, int max_qubits, aqsg_program* out) {
+    if (!out) return set_error(AQSG_ERR_NULL, "NULL output handle");
+    *out = nullptr;
+    if (n < 1 || n > AQSG_MAX_QUBITS)
+        return set_error(AQSG_ERR_INVALID_ARGUMENT, "Invalid qubit count");
+    if (dtype != AQSG_C64 && dtype != AQSG_C128) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Unknown dtype");
+    if (max_qubits < 1 || max_qubits > AQSG_MAX_UNITARY_QUBITS)
+        return set_error(AQSG_ERR_INVALID_ARGUMENT, "Fusion width must be 1 to 5 qubits");
+    if (int rc = aqsg_check_ops(n, ops, count)) return rc;
+    std::vector<LOp> low;
+    std::vector<aqsg_op> src;
+    low.reserve(count);
+    for (int i = 0; i < count; ++i) {
+        LOp o;
+        if (int rc = lower_op(n, dtype, ops[i], &o)) return rc;
+        if (o.cls == L_NOP) continue;
+        low.push_back(std::move(o));
+        src.push_back(ops[i]);
+        src.back().matrix = nullptr;  // the caller's buffer need not outlive the program
+    }
+    auto* p = new aqsg_program_s();
+    p->n = n;
+    p->dtype = dtype;
+    p->source_ops = count;
+    // pass-through unitaries keep a private copy of their matrix
+    p->mats.reserve(2 * src.size() + 1);
+    if (int rc = fuse(n, low, src, max_qubits, p)) {
+        delete p;
+        return rc;
+    }
+    *out = p;
+    return AQSG_OK;
+}
+
+int aqsg_program_info(aqsg_program p, int* fused_ops, int* source_ops) {
+    if (!p) return set_error(AQSG_ERR_NULL, "NULL program");
+    if (fused_ops) *fused_ops = (int)p->ops.size();
+    if (source_ops) *source_ops = p->source_ops;
+    return AQSG_OK;
+}
+
+int aqsg_run_program(aqsg_state st, aqsg_program p, int mode) {
+    if (!st || !st->d) return set_error(AQSG_ERR_NULL, "NULL state");
+    if (!p) return set_error(AQSG_ERR_NULL, "NULL program");
+    if (p->n != st->n || p->dtype != st->dtype)
+        return set_error(AQSG_ERR_INVALID_ARGUMENT, "Program was compiled for another register size or dtype");
+    if (mode < 0) mode = st->ctx->exec_mode;
+    if (mode < AQSG_EXEC_AUTO || mode > AQSG_EXEC_TILED)
+        return set_error(AQSG_ERR_INVALID_ARGUMENT, "Unknown execution mode");
+    AQSG_CUDA_TRY(cudaSetDevice(st->ctx->device));
+    if (mode == AQSG_EXEC_PER_GATE) {
+        for (const LOp& o : p->ops)
+            if (int rc = launch_lop(st, o)) return rc;
+        return AQSG_OK;
+    }
+    return run_tiled(st, p->ops);
+}
+
+int aqsg_program_export(aqsg_program p, aqsg_op* out, int capacity, int* count) {
+    if (!p) return set_error(AQSG_ERR_NULL, "NULL program");
+    if (count) *count = (int)p->exported.size();
+    if (!out) return AQSG_OK;
+    if (capacity < (int)p->exported.size())
+        return set_error(AQSG_ERR_INVALID_ARGUMENT, "Output holds fewer ops than the program");
+    std::copy(p->exported.begin(), p->exported.end(), out);
+    return AQSG_OK;
+}
+
+int aqsg_program_free(aqsg_program p) {
+    if (!p) return set_error(AQSG_ERR_NULL, "NULL program");
+    delete p;
+    return AQSG_OK;
+}
+
+}  // extern "C"

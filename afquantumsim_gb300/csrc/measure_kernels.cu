@@ -678,3 +678,83 @@ int expect_z(aqsg_state_s* st, double* z, double* zz) {
 }
 
 }  // namespace aqsg
+
+// ---- comparison of two registers ------------------------------------------------
+
+namespace aqsg {
+
+template <typename TA, typename TB>
+__global__ void __launch_bounds__(256)
+k_compare(const TA* __restrict__ a, const TB* __restrict__ b, uint64_t N, double* partial) {
+    __shared__ double sh[32];
+    double mx = 0, ore = 0, oim = 0, na = 0, nb = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const TA x = __ldcs(a + i);
+        const TB y = __ldcs(b + i);
+        const double xr = x.x, xi = x.y, yr = y.x, yi = y.y;
+        const double dr = xr - yr, di = xi - yi;
+        mx = fmax(mx, sqrt(dr * dr + di * di));
+        ore += xr * yr + xi * yi;  // conj(x) * y
+        oim += xr * yi - xi * yr;
+        na += xr * xr + xi * xi;
+        nb += yr * yr + yi * yi;
+    }
+    // block max of mx through shared memory, sums through block_sum
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    __shared__ double shm[32];
+    if ((threadIdx.x & 31) == 0) shm[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0;
+        for (unsigned w = 0; w < (blockDim.x >> 5); ++w) m = fmax(m, shm[w]);
+        partial[5 * blockIdx.x] = m;
+    }
+    const double s1 = block_sum(ore, sh), s2 = block_sum(oim, sh), s3 = block_sum(na, sh),
+                 s4 = block_sum(nb, sh);
+    if (threadIdx.x == 0) {
+        partial[5 * blockIdx.x + 1] = s1;
+        partial[5 * blockIdx.x + 2] = s2;
+        partial[5 * blockIdx.x + 3] = s3;
+        partial[5 * blockIdx.x + 4] = s4;
+    }
+}
+
+}  // namespace aqsg
+
+extern "C" int aqsg_state_compare(aqsg_state a, aqsg_state b, double* max_abs_diff, double* overlap_re,
+                                  double* overlap_im, double* norm2_a, double* norm2_b) {
+    using namespace aqsg;
+    if (!a || !a->d || !b || !b->d) return set_error(AQSG_ERR_NULL, "NULL state");
+    if (a->n != b->n) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Registers differ in qubit count");
+    if (a->ctx != b->ctx) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Registers belong to different contexts");
+    aqsg_ctx_s* c = a->ctx;
+    const unsigned grid = stream_grid(a, a->amps, 256);
+    if (int rc = ensure_scratch(c->partial, sizeof(double) * 5 * grid)) return rc;
+    double* part = (double*)c->partial.ptr;
+    const bool a64 = a->dtype == AQSG_C64, b64 = b->dtype == AQSG_C64;
+    if (a64 && b64)
+        k_compare<float2, float2><<<grid, 256, 0, c->stream>>>((const float2*)a->d, (const float2*)b->d, a->amps, part);
+    else if (a64)
+        k_compare<float2, double2><<<grid, 256, 0, c->stream>>>((const float2*)a->d, (const double2*)b->d, a->amps, part);
+    else if (b64)
+        k_compare<double2, float2><<<grid, 256, 0, c->stream>>>((const double2*)a->d, (const float2*)b->d, a->amps, part);
+    else
+        k_compare<double2, double2><<<grid, 256, 0, c->stream>>>((const double2*)a->d, (const double2*)b->d, a->amps, part);
+    c->launches++;
+    AQSG_CUDA_TRY(cudaGetLastError());
+    std::vector<double> h(5 * grid);
+    AQSG_CUDA_TRY(cudaMemcpyAsync(h.data(), part, sizeof(double) * 5 * grid, cudaMemcpyDeviceToHost, c->stream));
+    AQSG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    double r[5] = {0, 0, 0, 0, 0};
+    for (unsigned i = 0; i < grid; ++i) {
+        r[0] = h[5 * i] > r[0] ? h[5 * i] : r[0];
+        for (int j = 1; j < 5; ++j) r[j] += h[5 * i + j];
+    }
+    if (max_abs_diff) *max_abs_diff = r[0];
+    if (overlap_re) *overlap_re = r[1];
+    if (overlap_im) *overlap_im = r[2];
+    if (norm2_a) *norm2_a = r[3];
+    if (norm2_b) *norm2_b = r[4];
+    return AQSG_OK;
+}

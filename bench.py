@@ -175,6 +175,103 @@ def reference_algorithm_small(n=12):
     return {"n": n, "gate_apps_per_s": len(ops) / dt, "seconds": dt}
 
 
+# ---- secondary workloads (reported under "extras") -----------------------------------
+
+def _time_ms(stream, fn, reps):
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def bench_fused_brickwork(ctx, st, stream, n, depth):
+    """Depth-`depth` brick-work circuit (Haar SU(2) as RotZ.RotY.RotZ + CZ
+    layers, seed 4) on |0...0>: one gate per pass, plain tile passes, and the
+    compiled program (<= 5-qubit fused unitaries) on tensor cores and on CUDA
+    cores; error and 1 - fidelity of the tensor-core result against the same
+    circuit run one gate per pass in complex128."""
+    import afquantumsim_gb300 as aq
+    from afquantumsim_gb300 import circuits
+    ops = aq.op_array(circuits.brickwork(n, depth, seed=4))
+    N = 1 << n
+    prog = aq.Program(n, list(ops), aq.C64, max_qubits=5)
+    fused, src = prog.info()
+    res = {"workload": f"brickwork{n}x{depth}", "gates": src, "fused_ops": fused}
+
+    def reset():
+        st.set_basis(0)
+
+    reset()
+    st.apply(ops, aq.EXEC_PER_GATE)
+    res["per_gate_ms"] = round(_time_ms(stream, lambda: st.apply(ops, aq.EXEC_PER_GATE), 1), 2)
+    st.apply(ops, aq.EXEC_TILED)
+    res["tiled_ms"] = round(_time_ms(stream, lambda: st.apply(ops, aq.EXEC_TILED), 2), 2)
+    ctx.set_tensor_cores(False)
+    prog.run(st, aq.EXEC_TILED)
+    res["fused_cuda_core_ms"] = round(_time_ms(stream, lambda: prog.run(st, aq.EXEC_TILED), 2), 2)
+    ctx.set_tensor_cores(True)
+    prog.run(st, aq.EXEC_TILED)
+    res["fused_tensor_core_ms"] = round(_time_ms(stream, lambda: prog.run(st, aq.EXEC_TILED), 3), 2)
+    res["speedup_fused_vs_tiled"] = round(res["tiled_ms"] / res["fused_tensor_core_ms"], 2)
+    res["speedup_fused_vs_per_gate"] = round(res["per_gate_ms"] / res["fused_tensor_core_ms"], 2)
+    # accuracy: fused (tensor cores, c64) vs one gate per pass in c128
+    reset()
+    prog.run(st, aq.EXEC_TILED)
+    with aq.State(ctx, n, aq.C128) as ref:
+        ref.set_basis(0)
+        ref.apply(ops, aq.EXEC_PER_GATE)
+        mx, ov, na, nb = st.compare(ref)
+    res["max_abs_err_vs_fp64"] = mx
+    res["one_minus_fidelity"] = max(0.0, 1.0 - abs(ov) ** 2 / (na * nb))
+    res["max_rel_err_scaled"] = mx * np.sqrt(N)  # error relative to a typical |a| = 2^(-n/2)
+    res["l2_bytes_note"] = "fused/tiled passes move 2 x 8 B x 2^n each"
+    return res
+
+
+def bench_plain12(ctx, stream, n=12, layers=10):
+    """The 12-qubit plain-method workload (H layer, then 10 layers of seeded
+    random RotX/RotY/RotZ + CX chain) with a 1000-shot histogram: one launch
+    in tiled mode (the register is one shared-memory tile) vs one gate per
+    pass; end to end through the C ABI; and the reference ALGORITHM (faithful
+    FP32 restatement: dense Kronecker / CSR operators) on the host."""
+    import time as _t
+
+    import afquantumsim_gb300 as aq
+    from afquantumsim_gb300 import circuits
+    from oracle import oracle
+    ops = aq.op_array(circuits.plain_layers(n, layers, seed=1))
+    res = {"workload": f"plain{n}x{layers}", "gates": len(ops)}
+    with aq.State(ctx, n, aq.C64) as s:
+        def run(mode):
+            s.set_basis(0)
+            s.apply(ops, mode)
+        run(aq.EXEC_TILED)
+        res["tiled_us"] = round(1e3 * _time_ms(stream, lambda: run(aq.EXEC_TILED), 200), 2)
+        run(aq.EXEC_PER_GATE)
+        res["per_gate_us"] = round(1e3 * _time_ms(stream, lambda: run(aq.EXEC_PER_GATE), 20), 2)
+        u = np.random.default_rng(2).random(1000)
+        t0 = _t.perf_counter()
+        reps = 50
+        for _ in range(reps):
+            run(aq.EXEC_TILED)
+            sv = s.download()
+            counts = np.bincount(s.sample(u).astype(np.int64), minlength=1 << n)
+        res["e2e_us_per_simulate_sv_and_1000_shots"] = round(1e6 * (_t.perf_counter() - t0) / reps, 1)
+    v = np.zeros(1 << n, dtype=np.complex64)
+    v[0] = 1
+    t0 = _t.perf_counter()
+    ref = oracle.ref32_apply(v, n, list(ops))
+    res["reference_algorithm_s"] = round(_t.perf_counter() - t0, 3)
+    res["reference_algorithm_threads"] = oracle.threads()
+    res["max_abs_diff_vs_reference_algorithm"] = float(np.max(np.abs(ref - sv)))
+    res["shots_total"] = int(counts.sum())
+    return res
+
+
 # ---- our arm ------------------------------------------------------------------------
 
 def run_ours(args, rank, world, local_rank):
@@ -308,6 +405,9 @@ def run_ours(args, rank, world, local_rank):
         e1.record(stream)
         e1.synchronize()
         extras["tiled_ms_per_step"] = round(e0.elapsed_time(e1) / 2, 3)
+        if args.dtype == "c64":
+            extras["fused_brickwork"] = bench_fused_brickwork(ctx, st, stream, n, depth=20)
+        extras["plain12"] = bench_plain12(ctx, stream)
 
     cpu = None
     if rank == 0:

@@ -154,6 +154,11 @@ int aqsg_shutdown(aqsg_ctx ctx);
 /* Default execution mode for aqsg_apply_ops on this context. */
 int aqsg_set_exec_mode(aqsg_ctx ctx, int mode);
 
+/* Apply fused 3..5-qubit unitaries of c64 tile passes on the tensor cores
+ * (tcgen05, split-BF16 three-term products accumulated in FP32) when enable
+ * is non-zero (the default); otherwise on the CUDA cores in FP32. */
+int aqsg_set_tensor_cores(aqsg_ctx ctx, int enable);
+
 /* Wait for all work queued on the context's stream. */
 int aqsg_synchronize(aqsg_ctx ctx);
 
@@ -198,6 +203,13 @@ int aqsg_state_download_range(aqsg_state st, uint64_t begin, uint64_t count,
 /* Copy src into dst (same n and dtype). */
 int aqsg_state_copy(aqsg_state dst, aqsg_state src);
 
+/* Compare two registers with the same qubit count (either dtype) in one
+ * FP64 pass: max_i |a_i - b_i|, the overlap <a|b> and both squared norms.
+ * Any output pointer may be NULL.  (Parity checks of large registers, e.g. a
+ * c64 run against a c128 run of the same circuit.) */
+int aqsg_state_compare(aqsg_state a, aqsg_state b, double* max_abs_diff, double* overlap_re,
+                       double* overlap_im, double* norm2_a, double* norm2_b);
+
 /* ---- simulation ----------------------------------------------------------- */
 
 /* Validate ops against an n-qubit register without running them.  Returns the
@@ -210,6 +222,35 @@ int aqsg_check_ops(int n, const aqsg_op* ops, int count);
  * gate class (quantum.cpp:533-1950) replaced by in-place kernels.
  * mode: an aqsg_exec_mode, or -1 for the context default. */
 int aqsg_apply_ops(aqsg_state st, const aqsg_op* ops, int count, int mode);
+
+/* ---- compiled programs ---------------------------------------------------- */
+
+typedef struct aqsg_program_s* aqsg_program;
+
+/* Compile ops for an n-qubit register of `dtype`: consecutive gates are fused
+ * into dense unitaries on at most `max_qubits` (1..5) qubits (diagonal-only
+ * groups stay diagonal).  The engine's form of QCircuit::compile
+ * (quantum.cpp:199-210), which folds gates into one 2^n x 2^n matrix; here
+ * the folded pieces stay small enough for tensor-core tile passes.
+ * Validation and messages as aqsg_check_ops. */
+int aqsg_compile(int n, int dtype, const aqsg_op* ops, int count, int max_qubits,
+                 aqsg_program* out);
+
+/* Number of fused ops and of source ops of a program. */
+int aqsg_program_info(aqsg_program prog, int* fused_ops, int* source_ops);
+
+/* Run a compiled program on a register with the program's n and dtype
+ * (QSimulator::simulate's compiled prefix, quantum.cpp:283).  mode: an
+ * aqsg_exec_mode or -1 for the context default. */
+int aqsg_run_program(aqsg_state st, aqsg_program prog, int mode);
+
+/* Copy the program's ops in ABI form into out[0..capacity) (fused groups
+ * become AQSG_OP_UNITARY ops whose matrix points into the program, valid
+ * until aqsg_program_free); *count receives the op count.  out may be NULL
+ * to query the count.  For inspection, serialisation and replay. */
+int aqsg_program_export(aqsg_program prog, aqsg_op* out, int capacity, int* count);
+
+int aqsg_program_free(aqsg_program prog);
 
 /* ---- measurement ---------------------------------------------------------- */
 

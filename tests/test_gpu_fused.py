@@ -1,0 +1,70 @@
+"""Fused programs (aqsg_compile) on the GPU: tile passes with fused
+unitaries on the tensor cores (tcgen05, split-BF16, FP32 accumulate) and on
+the CUDA cores, against the FP64 oracle.  c64 tolerance 1e-5 absolute."""
+import numpy as np
+import pytest
+
+import afquantumsim_gb300 as aq
+from afquantumsim_gb300 import circuits
+from oracle import oracle
+from tests import _kat
+
+pytestmark = pytest.mark.gpu
+
+
+def run_prog(ctx, v, prog, dtype, mode):
+    n = int(v.size).bit_length() - 1
+    with aq.State(ctx, n, dtype) as st:
+        st.upload(v)
+        prog.run(st, mode)
+        return st.download()
+
+
+@pytest.mark.parametrize("tc", [True, False])
+@pytest.mark.parametrize("n,k,seed", [(12, 5, 1), (12, 3, 2), (15, 5, 3), (16, 4, 4), (18, 5, 5),
+                                      (20, 3, 6), (20, 5, 7)])
+def test_fused_random_circuits(gpu_ctx, tc, n, k, seed):
+    ops = _kat.random_circuit(n, 150, seed)
+    v = _kat.random_state(n, seed)
+    want = oracle.apply_f64(v.copy(), ops)
+    prog = aq.Program(n, ops, aq.C64, max_qubits=k)
+    gpu_ctx.set_tensor_cores(tc)
+    try:
+        got = run_prog(gpu_ctx, v.astype(np.complex64), prog, aq.C64, aq.EXEC_TILED)
+    finally:
+        gpu_ctx.set_tensor_cores(True)
+    assert np.max(np.abs(got - want)) < 1e-5
+    prog128 = aq.Program(n, ops, aq.C128, max_qubits=k)
+    got128 = run_prog(gpu_ctx, v.copy(), prog128, aq.C128, aq.EXEC_TILED)
+    assert np.max(np.abs(got128 - want)) < 1e-12
+
+
+@pytest.mark.parametrize("n,depth", [(12, 8), (16, 20), (22, 10)])
+def test_fused_brickwork(gpu_ctx, n, depth):
+    ops = circuits.brickwork(n, depth, seed=4)
+    v = _kat.random_state(n, 9)
+    want = oracle.apply_f64(v.copy(), ops)
+    prog = aq.Program(n, ops, aq.C64, max_qubits=5)
+    for mode in (aq.EXEC_TILED, aq.EXEC_PER_GATE):
+        got = run_prog(gpu_ctx, v.astype(np.complex64), prog, aq.C64, mode)
+        err = np.max(np.abs(got - want))
+        fid = abs(np.vdot(want, got.astype(np.complex128))) ** 2
+        assert err < 1e-5 and 1 - fid < 1e-8, (mode, err, fid)
+
+
+def test_tensor_core_unitary_exact_structure(gpu_ctx):
+    """A fused 5-qubit permutation-like unitary through the tensor cores:
+    the split products reproduce entries 0/1 to FP32 accuracy."""
+    n = 15
+    rng = np.random.default_rng(3)
+    perm = rng.permutation(32)
+    m = np.zeros((32, 32))
+    m[perm, np.arange(32)] = 1
+    ops = [aq.Unitary([1, 4, 7, 9, 12], m)]
+    v = _kat.random_state(n, 2)
+    want = oracle.apply_f64(v.copy(), ops)
+    with aq.State(gpu_ctx, n, aq.C64) as st:
+        st.upload(v.astype(np.complex64))
+        st.apply(ops, aq.EXEC_TILED)
+        got = st.download()
+    assert np.max(np.abs(got - want)) < 1e-7
