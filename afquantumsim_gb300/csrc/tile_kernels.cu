@@ -15,6 +15,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "aqsg_internal.h"
@@ -27,9 +28,9 @@ struct TileOp {
     int32_t lt0, lt1;  // local target bits; DIAG2 with an external target: lt0 = -1
     int32_t k;
     int32_t ltb[AQSG_MAX_UNITARY_QUBITS];
-    int32_t mat;       // MATK: offset (complex elements) in the matrix pool
+    int32_t mat;       // MATK: byte offset of its matrix (or tensor-core operand) in the pool
     int32_t ext_t;     // DIAG2 external target: global bit, else -1
-    int32_t pad;
+    int32_t pad;       // MATK: 1 = apply on the tensor cores
     uint64_t cm_loc, cv_loc, cm_ext, cv_ext, am_loc, am_ext;
     double m[8];
 };
@@ -72,7 +73,7 @@ __device__ __forceinline__ T ld_coef(const double* m, int i) {
 constexpr int kTcTileBits = 12;
 constexpr int kTcThreads = 128;
 constexpr uint32_t kTcTmemCols = 64;            // 2^(12+1) / 128
-constexpr uint32_t kTcABytes = 2u << kTcTileBits;  // one split of A: 2^(m+1) bf16
+constexpr uint32_t kTcABytes = 4u << kTcTileBits;  // one split of A: 2^(m+1) bf16 = 2^(m+2) B
 constexpr uint32_t kTcBBytes = 2u * 64 * 64;       // one split of B at k = 5
 constexpr uint64_t kTcWaitNs = 200000000ull;  // 0.2 s per wait
 
@@ -688,6 +689,14 @@ static int run_tiled_t(aqsg_state_s* st, const std::vector<LOp>& ops) {
     const int tc_shm = (int)((sizeof(T) << kTcTileBits) + 1024 + 2 * kTcABytes + 2 * kTcBBytes + 256);
     bool launched_tc = false;
     if (tc_on) AQSG_CUDA_TRY(cudaFuncSetAttribute(ktc, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_shm));
+    // The tensor-core products lose a little norm in a biased way (~1e-7 per
+    // fused op); a run that uses them restores the input's FP64 norm at the
+    // end (one read pass before, one read and one scale pass after).
+    bool any_tc_pass = false;
+    for (char f : pass_tc) any_tc_pass = any_tc_pass || f;
+    double norm_before = 0;
+    if (any_tc_pass)
+        if (int rc = reduce_prob(st, 0, 0, &norm_before)) return rc;
     for (size_t pi = 0; pi < passes.size(); ++pi) {
         const Pass& p = passes[pi];
         TileGeom geo;
@@ -725,6 +734,10 @@ static int run_tiled_t(aqsg_state_s* st, const std::vector<LOp>& ops) {
             AQSG_CUDA_TRY(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
             return set_error(AQSG_ERR_TIMEOUT, "Tensor-core tile pass timed out waiting for its MMAs");
         }
+        double norm_after = 0;
+        if (int rc = reduce_prob(st, 0, 0, &norm_after)) return rc;
+        if (norm_after > 0 && norm_before > 0)
+            if (int rc = launch_scale(st, std::sqrt(norm_before / norm_after))) return rc;
     }
     return AQSG_OK;
 }
