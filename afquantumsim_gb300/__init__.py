@@ -37,7 +37,8 @@ EXPORTS = [
     "aqsg_probs", "aqsg_norm2", "aqsg_sample", "aqsg_sample_seeded",
     "aqsg_collapse_qubit", "aqsg_collapse_all", "aqsg_expect_z", "aqsg_sample_noalloc",
     "aqsg_state_compare", "aqsg_compile", "aqsg_program_info", "aqsg_run_program", "aqsg_program_export",
-    "aqsg_program_free",
+    "aqsg_program_free", "aqsg_batch_create", "aqsg_batch_update", "aqsg_batch_run",
+    "aqsg_batch_info", "aqsg_batch_free",
 ]
 
 _lib = None
@@ -493,3 +494,79 @@ class Program:
             self.free()
         except Exception:
             pass
+
+
+# ---- batched engine ------------------------------------------------------------
+
+class _Circuit(C.Structure):
+    _fields_ = [("n", C.c_int32), ("count", C.c_int32), ("ops", C.POINTER(Op))]
+
+
+def _bind_batch(lib):
+    P, I, D = C.c_void_p, C.c_int, C.POINTER(C.c_double)
+    lib.aqsg_batch_create.argtypes = [P, C.POINTER(_Circuit), I, C.POINTER(P)]
+    lib.aqsg_batch_update.argtypes = [P, C.POINTER(_Circuit)]
+    lib.aqsg_batch_run.argtypes = [P, D, D]
+    lib.aqsg_batch_info.argtypes = [P, C.POINTER(I), C.POINTER(I), C.POINTER(I)]
+    lib.aqsg_batch_free.argtypes = [P]
+    for f in ("aqsg_batch_create", "aqsg_batch_update", "aqsg_batch_run", "aqsg_batch_info",
+              "aqsg_batch_free"):
+        getattr(lib, f).restype = I
+
+
+class Batch:
+    """aqsg_batch: independent circuits [(n, ops), ...] run from |0...0> to
+    <Z_q> and <Z_q Z_q+1>, captured once as a CUDA graph."""
+
+    def __init__(self, ctx: Context, circuits):
+        self.ctx, self.lib = ctx, ctx.lib
+        _bind_batch(self.lib)
+        arr, keep = self._encode(circuits)
+        h = C.c_void_p()
+        _check(self.lib.aqsg_batch_create(ctx.h, arr, len(arr), C.byref(h)))
+        self.h = h
+        self.ns = [n for n, _ in circuits]
+
+    @staticmethod
+    def _encode(circuits):
+        arr = (_Circuit * len(circuits))()
+        keep = []
+        for i, (n, ops) in enumerate(circuits):
+            if isinstance(ops, np.ndarray):  # structured array in aqsg_op layout
+                a = np.ascontiguousarray(ops)
+                ptr = C.cast(a.ctypes.data, C.POINTER(Op))
+            else:
+                a = ops if isinstance(ops, C.Array) else op_array(list(ops))
+                ptr = C.cast(a, C.POINTER(Op))
+            keep.append(a)
+            arr[i].n, arr[i].count, arr[i].ops = n, len(a), ptr
+        arr._keep = keep
+        return arr, keep
+
+    def update(self, circuits) -> None:
+        arr, keep = self._encode(circuits)
+        _check(self.lib.aqsg_batch_update(self.h, arr))
+
+    def run(self):
+        """Returns (z, zz): lists of per-circuit numpy arrays."""
+        nz = sum(self.ns)
+        z = np.empty(nz, dtype=np.float64)
+        zz = np.empty(max(nz - len(self.ns), 1), dtype=np.float64)
+        _check(self.lib.aqsg_batch_run(self.h, z.ctypes.data_as(C.POINTER(C.c_double)),
+                                       zz.ctypes.data_as(C.POINTER(C.c_double))))
+        zs, zzs, a, b = [], [], 0, 0
+        for n in self.ns:
+            zs.append(z[a:a + n])
+            zzs.append(zz[b:b + n - 1])
+            a, b = a + n, b + n - 1
+        return zs, zzs
+
+    def info(self):
+        s, l, k = C.c_int(), C.c_int(), C.c_int()
+        _check(self.lib.aqsg_batch_info(self.h, C.byref(s), C.byref(l), C.byref(k)))
+        return {"small": s.value, "large": l.value, "kernels": k.value}
+
+    def free(self) -> None:
+        if self.h:
+            _check(self.lib.aqsg_batch_free(self.h))
+            self.h = None

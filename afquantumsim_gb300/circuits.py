@@ -90,3 +90,60 @@ def gate_count(ops) -> int:
 
 
 __all__ = ["qft", "plain_layers", "brickwork", "vqe_ansatz", "haar_su2", "euler_zyz", "CPhase", "Swap"]
+
+
+def op_dtype():
+    """numpy structured dtype with the exact layout of struct aqsg_op."""
+    import ctypes as C
+
+    from ._abi import Op
+    names, formats, offsets = [], [], []
+    fmt = {"kind": "<i4", "num_qubits": "<i4", "num_controls": "<i4", "control_values": "<u4",
+           "angle": "<f4", "qubits": ("<i4", 5), "controls": ("<i4", 16), "matrix": "<u8"}
+    for name, _ in Op._fields_:
+        names.append(name)
+        formats.append(fmt[name])
+        offsets.append(getattr(Op, name).offset)
+    return np.dtype({"names": names, "formats": formats, "offsets": offsets, "itemsize": C.sizeof(Op)})
+
+
+def vqe_ops_array(n: int, layers: int, params: np.ndarray) -> np.ndarray:
+    """vqe_ansatz(n, layers, params) as a structured array (fast for big
+    sweeps): per layer RotY then RotZ on each qubit, then the CX ring."""
+    from . import _abi
+    ring = n if n > 2 else (1 if n == 2 else 0)
+    per = 2 * n + ring
+    a = np.zeros(layers * per, dtype=op_dtype())
+    idx = np.arange(layers)[:, None] * per
+    q = np.arange(n)
+    ry = (idx + 2 * q).ravel()
+    rz = (idx + 2 * q + 1).ravel()
+    a["kind"][ry] = _abi.RY
+    a["kind"][rz] = _abi.RZ
+    a["num_qubits"][ry] = 1
+    a["num_qubits"][rz] = 1
+    a["qubits"][ry, 0] = np.tile(q, layers)
+    a["qubits"][rz, 0] = np.tile(q, layers)
+    a["angle"][ry] = params[:, :, 0].astype(np.float32).ravel()
+    a["angle"][rz] = params[:, :, 1].astype(np.float32).ravel()
+    if ring:
+        cx = (idx + 2 * n + np.arange(ring)).ravel()
+        a["kind"][cx] = _abi.CX
+        a["num_qubits"][cx] = 2
+        a["qubits"][cx, 0] = np.tile(np.arange(ring), layers)
+        a["qubits"][cx, 1] = np.tile((np.arange(ring) + 1) % n, layers)
+    return a
+
+
+def vqe_sweep(count: int = 4096, seed: int = 5, n_range=(8, 20), layer_range=(4, 12)):
+    """The batched VQE sweep: `count` hardware-efficient-ansatz circuits with
+    qubits uniform in n_range, layers uniform in layer_range and angles
+    uniform in [-pi, pi].  Returns [(n, structured op array), ...]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n = int(rng.integers(n_range[0], n_range[1] + 1))
+        L = int(rng.integers(layer_range[0], layer_range[1] + 1))
+        params = rng.uniform(-np.pi, np.pi, size=(L, n, 2))
+        out.append((n, vqe_ops_array(n, L, params)))
+    return out

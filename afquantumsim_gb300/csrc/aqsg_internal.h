@@ -99,6 +99,29 @@ inline size_t amp_bytes(int dtype) { return dtype == AQSG_C128 ? 16 : 8; }
 int launch_lop(aqsg_state_s* st, const LOp& op);
 
 // ---- tile passes (tile_kernels.cu) ---------------------------------------------
+// One pass of a tile plan: its m tile bits (ascending; the first L are the
+// row bits) and its ops table[first, first+count).
+struct TilePass {
+    int m, L;
+    int tbits[16];
+    uint32_t first, count;
+    int tc;  // uses the tensor-core kernel
+};
+// Encoded passes of an op list: op table (device TileOp records, as bytes)
+// and operand pool (matrices / tensor-core operands) to upload together,
+// table first and the pool at pool_offset().
+struct TilePlan {
+    int n = 0, dtype = AQSG_C64;
+    std::vector<unsigned char> table;
+    std::vector<unsigned char> pool;
+    std::vector<TilePass> passes;
+    bool any_tc = false;
+    size_t pool_offset() const;
+};
+int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, TilePlan* plan);
+// Launch the passes on `stream`; dev = device copy of table + pool.
+int launch_tile_plan(void* sv, const TilePlan& plan, const void* dev, cudaStream_t stream, int* d_err,
+                     uint64_t* launches);
 // Runs ops through shared-memory tile passes; returns AQSG_OK.
 int run_tiled(aqsg_state_s* st, const std::vector<LOp>& ops);
 // Largest tile (log2 amplitudes) the tile kernel holds for a dtype.

@@ -1,0 +1,508 @@
+// Batched engine: many independent c64 registers of uneven size, each run
+// from |0...0> and reduced to <Z_q> and <Z_q Z_q+1> (FP64), in one CUDA
+// graph.  It generalises the reference's VQE cost loop
+// (src/quantum_algo.cpp:412-456: simulate, then read expectation values)
+// from one circuit at a time to a whole parameter sweep.
+//
+// Registers of up to 14 qubits never touch HBM: a persistent kernel per size
+// class takes circuits from an atomic work counter, one CTA per circuit,
+// prepares |0...0> in shared memory, runs the circuit's ops with the tile
+// interpreter, and sums the expectation values on chip.  Larger registers
+// run as preplanned tile passes over one reused device register.  The whole
+// sequence is captured once; aqsg_batch_update swaps in new angles without
+// re-planning, and aqsg_batch_run replays the graph.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "tile_device.cuh"
+
+namespace aqsg {
+
+struct SmallItem {
+    int32_t n, nops;
+    uint32_t op_first;  // first TileOp of this circuit in the class table
+    uint32_t out;       // offset (doubles) of its 2n raw results
+};
+
+constexpr int kSmallMaxQubits = 14;
+constexpr int kZMaxBits = 14;
+
+__device__ __forceinline__ double warp_sum_b(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block sum; valid in thread 0.  blockDim.x is a multiple of 32.
+__device__ __forceinline__ double block_sum_b(double v, double* sh) {
+    v = warp_sum_b(v);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0;
+    if (w == 0) {
+        r = (l < (int)(blockDim.x >> 5)) ? sh[l] : 0.0;
+        r = warp_sum_b(r);
+    }
+    __syncthreads();
+    return r;
+}
+
+// Raw results per circuit, 2n doubles: S[b] = sum p over indices with bit b
+// set (b < n), X[b] = sum p over indices whose bits b and b+1 differ
+// (b < n-1), then the total T.  <Z_q> = T - 2 S[n-1-q].
+template <int EPT, int MAXT>
+__global__ void __launch_bounds__(MAXT, 1)
+k_batch_small(const SmallItem* __restrict__ items, int count, int* counter, const TileOp* __restrict__ ops,
+              const unsigned char* __restrict__ pool, double* __restrict__ out) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* s = reinterpret_cast<float2*>(smem_raw);
+    __shared__ int cur;
+    __shared__ double red[32];
+    TcShared tcs;  // no tensor-core ops in this kernel
+    uint32_t phase = 0;
+    for (;;) {
+        if (threadIdx.x == 0) cur = atomicAdd(counter, 1);
+        __syncthreads();
+        const int i = cur;
+        __syncthreads();
+        if (i >= count) break;
+        const SmallItem it = items[i];
+        const int n = it.n;
+        const uint32_t size = 1u << n;
+        for (uint32_t j = threadIdx.x; j < size; j += blockDim.x) s[j] = make_float2(j == 0 ? 1.f : 0.f, 0.f);
+        __syncthreads();
+        tile_run_ops<float, EPT, false>(s, size, 0, ops + it.op_first, it.nops, pool, tcs, phase);
+        double T = 0, S[kZMaxBits], X[kZMaxBits];
+#pragma unroll
+        for (int b = 0; b < kZMaxBits; ++b) { S[b] = 0; X[b] = 0; }
+        for (uint32_t j = threadIdx.x; j < size; j += blockDim.x) {
+            const float2 a = s[j];
+            const double p = (double)a.x * a.x + (double)a.y * a.y;
+            T += p;
+#pragma unroll
+            for (int b = 0; b < kZMaxBits; ++b) {
+                if (b < n && ((j >> b) & 1u)) S[b] += p;
+                if (b + 1 < n && (((j >> b) ^ (j >> (b + 1))) & 1u)) X[b] += p;
+            }
+        }
+        double* o = out + it.out;
+#pragma unroll
+        for (int b = 0; b < kZMaxBits; ++b) {
+            if (b < n) {
+                const double v = block_sum_b(S[b], red);
+                if (threadIdx.x == 0) o[b] = v;
+            }
+            if (b + 1 < n) {
+                const double v = block_sum_b(X[b], red);
+                if (threadIdx.x == 0) o[n + b] = v;
+            }
+        }
+        const double t = block_sum_b(T, red);
+        if (threadIdx.x == 0) o[2 * n - 1] = t;
+        __syncthreads();
+    }
+}
+
+__global__ void k_basis0(float2* sv) { sv[0] = make_float2(1.f, 0.f); }
+
+// classes of small registers: (max qubits, threads, elements per thread)
+struct SmallClass {
+    int max_n, threads;
+};
+static const SmallClass kClasses[3] = {{10, 128}, {12, 256}, {14, 512}};
+
+static int class_of(int n) {
+    for (int c = 0; c < 3; ++c)
+        if (n <= kClasses[c].max_n) return c;
+    return -1;
+}
+
+}  // namespace aqsg
+
+using namespace aqsg;
+
+struct aqsg_batch_s {
+    aqsg_ctx ctx = nullptr;
+    int count = 0;
+    std::vector<int> n;
+    std::vector<size_t> out_off;  // raw-result offset per circuit
+    size_t out_doubles = 0;
+    // small classes
+    std::vector<SmallItem> items[3];
+    std::vector<int> class_circuits[3];
+    std::vector<unsigned char> small_table[3], small_pool[3];
+    void* d_small_items[3] = {nullptr, nullptr, nullptr};
+    void* d_small_ops[3] = {nullptr, nullptr, nullptr};
+    int grid[3] = {0, 0, 0};
+    // large registers
+    std::vector<int> large;  // circuit indices
+    std::vector<TilePlan> plans;
+    std::vector<size_t> plan_off;  // offset of each plan's table+pool in d_large
+    void* d_large = nullptr;
+    // parallel branches of the graph: large circuits go round-robin to
+    // branch streams, each with its own register and reduction scratch
+    std::vector<cudaStream_t> streams;
+    std::vector<cudaEvent_t> joins;
+    cudaEvent_t fork = nullptr;
+    std::vector<void*> regs, partials;
+    // results and counters
+    double* d_out = nullptr;
+    double* h_out = nullptr;  // pinned
+    int* d_counters = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t kernels = 0;  // kernel launches in one replay
+};
+
+namespace aqsg {
+
+int launch_expz_raw(const void* sv, int n, int dtype, double* partial, double* out_raw, cudaStream_t stream);
+size_t expz_partial_doubles(int n);
+
+// Lower and encode every circuit; fills the host-side tables of b.
+static int encode_batch(aqsg_batch_s* b, const aqsg_circuit* cs, bool first_time) {
+    for (int c = 0; c < 3; ++c) {
+        b->small_table[c].clear();
+        b->small_pool[c].clear();
+        if (first_time) {
+            b->items[c].clear();
+            b->class_circuits[c].clear();
+        }
+    }
+    if (first_time) {
+        b->large.clear();
+        b->plans.clear();
+    }
+    size_t li = 0;
+    std::vector<size_t> seen(3, 0);
+    for (int i = 0; i < b->count; ++i) {
+        const aqsg_circuit& ci = cs[i];
+        if (ci.n != b->n[i]) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Batch structure changed (qubit count)");
+        if (int rc = aqsg_check_ops(ci.n, ci.ops, ci.count)) return rc;
+        std::vector<LOp> low;
+        for (int k = 0; k < ci.count; ++k) {
+            LOp o;
+            if (int rc = lower_op(ci.n, AQSG_C64, ci.ops[k], &o)) return rc;
+            if (o.cls != L_NOP) low.push_back(std::move(o));
+        }
+        TilePlan plan;
+        if (int rc = encode_tiled(ci.n, AQSG_C64, low, false, &plan)) return rc;
+        const int cls = class_of(ci.n);
+        if (cls >= 0) {
+            // one whole-register pass; append its ops to the class table with
+            // their pool offsets shifted to the class pool
+            const size_t tsz = sizeof(TileOp);
+            const uint32_t first = (uint32_t)(b->small_table[cls].size() / tsz);
+            const size_t pbase = (b->small_pool[cls].size() + 255) & ~size_t(255);
+            b->small_pool[cls].resize(pbase);
+            b->small_pool[cls].insert(b->small_pool[cls].end(), plan.pool.begin(), plan.pool.end());
+            for (size_t at = 0; at < plan.table.size(); at += tsz) {
+                TileOp t;
+                std::memcpy(&t, &plan.table[at], tsz);
+                if (t.cls == L_MATK) t.mat += (int32_t)pbase;
+                const size_t w = b->small_table[cls].size();
+                b->small_table[cls].resize(w + tsz);
+                std::memcpy(&b->small_table[cls][w], &t, tsz);
+            }
+            const int nops = (int)(plan.table.size() / tsz);
+            if (first_time) {
+                SmallItem it;
+                it.n = ci.n;
+                it.nops = nops;
+                it.op_first = first;
+                it.out = (uint32_t)b->out_off[i];
+                b->items[cls].push_back(it);
+                b->class_circuits[cls].push_back(i);
+            } else {
+                SmallItem& it = b->items[cls][seen[cls]];
+                if (it.nops != nops || it.op_first != first)
+                    return set_error(AQSG_ERR_INVALID_ARGUMENT, "Batch structure changed (ops)");
+            }
+            seen[cls]++;
+        } else {
+            if (first_time) {
+                b->large.push_back(i);
+                b->plans.push_back(std::move(plan));
+            } else {
+                TilePlan& old = b->plans[li];
+                if (old.table.size() != plan.table.size() || old.pool.size() != plan.pool.size() ||
+                    old.passes.size() != plan.passes.size())
+                    return set_error(AQSG_ERR_INVALID_ARGUMENT, "Batch structure changed (ops)");
+                old.table = std::move(plan.table);
+                old.pool = std::move(plan.pool);
+            }
+            ++li;
+        }
+    }
+    return AQSG_OK;
+}
+
+static int upload_batch(aqsg_batch_s* b, cudaStream_t s) {
+    for (int c = 0; c < 3; ++c) {
+        if (b->items[c].empty()) continue;
+        const size_t tb = b->small_table[c].size();
+        const size_t poff = (tb + 255) & ~size_t(255);
+        AQSG_CUDA_TRY(cudaMemcpyAsync(b->d_small_ops[c], b->small_table[c].data(), tb, cudaMemcpyHostToDevice, s));
+        if (!b->small_pool[c].empty())
+            AQSG_CUDA_TRY(cudaMemcpyAsync((char*)b->d_small_ops[c] + poff, b->small_pool[c].data(),
+                                          b->small_pool[c].size(), cudaMemcpyHostToDevice, s));
+    }
+    for (size_t k = 0; k < b->plans.size(); ++k) {
+        const TilePlan& p = b->plans[k];
+        char* dst = (char*)b->d_large + b->plan_off[k];
+        AQSG_CUDA_TRY(cudaMemcpyAsync(dst, p.table.data(), p.table.size(), cudaMemcpyHostToDevice, s));
+        if (!p.pool.empty())
+            AQSG_CUDA_TRY(cudaMemcpyAsync(dst + p.pool_offset(), p.pool.data(), p.pool.size(),
+                                          cudaMemcpyHostToDevice, s));
+    }
+    AQSG_CUDA_TRY(cudaStreamSynchronize(s));
+    return AQSG_OK;
+}
+
+static constexpr int kMaxBranches = 32;
+
+static int branch_of_large(const aqsg_batch_s* b, size_t k) {
+    return (int)((k + 3) % b->streams.size());
+}
+
+// The device work of one run (captured into the graph): fork to the branch
+// streams, small-register classes on branches 0..2, large registers
+// round-robin, join back.
+static int record_batch(aqsg_batch_s* b, cudaStream_t s) {
+    b->kernels = 0;
+    AQSG_CUDA_TRY(cudaMemsetAsync(b->d_counters, 0, 3 * sizeof(int), s));
+    const int nb = (int)b->streams.size();
+    AQSG_CUDA_TRY(cudaEventRecord(b->fork, s));
+    for (int k = 0; k < nb; ++k) AQSG_CUDA_TRY(cudaStreamWaitEvent(b->streams[k], b->fork, 0));
+    for (int c = 0; c < 3; ++c) {
+        if (b->items[c].empty()) continue;
+        cudaStream_t bs = b->streams[c % nb];
+        const size_t shm = (size_t)8 << kClasses[c].max_n;
+        const size_t poff = (b->small_table[c].size() + 255) & ~size_t(255);
+        const TileOp* ops = (const TileOp*)b->d_small_ops[c];
+        const unsigned char* pool = (const unsigned char*)b->d_small_ops[c] + poff;
+        const SmallItem* items = (const SmallItem*)b->d_small_items[c];
+        const int cnt = (int)b->items[c].size();
+        switch (c) {
+            case 0:
+                k_batch_small<8, 128><<<b->grid[c], 128, shm, bs>>>(items, cnt, b->d_counters + c, ops, pool, b->d_out);
+                break;
+            case 1:
+                k_batch_small<16, 256><<<b->grid[c], 256, shm, bs>>>(items, cnt, b->d_counters + c, ops, pool, b->d_out);
+                break;
+            default:
+                k_batch_small<32, 512><<<b->grid[c], 512, shm, bs>>>(items, cnt, b->d_counters + c, ops, pool, b->d_out);
+                break;
+        }
+        AQSG_CUDA_TRY(cudaGetLastError());
+        b->kernels++;
+    }
+    for (size_t k = 0; k < b->large.size(); ++k) {
+        const int i = b->large[k];
+        const int n = b->n[i];
+        const int br = branch_of_large(b, k);
+        cudaStream_t bs = b->streams[br];
+        void* reg = b->regs[br];
+        AQSG_CUDA_TRY(cudaMemsetAsync(reg, 0, (size_t)8 << n, bs));
+        k_basis0<<<1, 1, 0, bs>>>((float2*)reg);
+        AQSG_CUDA_TRY(cudaGetLastError());
+        const void* dev = (const char*)b->d_large + b->plan_off[k];
+        if (int rc = launch_tile_plan(reg, b->plans[k], dev, bs, b->ctx->d_err, &b->kernels)) return rc;
+        if (int rc = launch_expz_raw(reg, n, AQSG_C64, (double*)b->partials[br], b->d_out + b->out_off[i], bs))
+            return rc;
+        b->kernels += 3;
+    }
+    for (int k = 0; k < nb; ++k) {
+        AQSG_CUDA_TRY(cudaEventRecord(b->joins[k], b->streams[k]));
+        AQSG_CUDA_TRY(cudaStreamWaitEvent(s, b->joins[k], 0));
+    }
+    return AQSG_OK;
+}
+
+static void free_batch(aqsg_batch_s* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    for (int c = 0; c < 3; ++c) {
+        if (b->d_small_items[c]) cudaFree(b->d_small_items[c]);
+        if (b->d_small_ops[c]) cudaFree(b->d_small_ops[c]);
+    }
+    if (b->d_large) cudaFree(b->d_large);
+    for (void* p : b->regs)
+        if (p) cudaFree(p);
+    for (void* p : b->partials)
+        if (p) cudaFree(p);
+    for (cudaStream_t st : b->streams) cudaStreamDestroy(st);
+    for (cudaEvent_t ev : b->joins) cudaEventDestroy(ev);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->d_out) cudaFree(b->d_out);
+    if (b->h_out) cudaFreeHost(b->h_out);
+    if (b->d_counters) cudaFree(b->d_counters);
+    delete b;
+}
+
+}  // namespace aqsg
+
+extern "C" {
+
+int aqsg_batch_create(aqsg_ctx ctx, const aqsg_circuit* circuits, int count, aqsg_batch* out) {
+    if (!ctx || !out) return set_error(AQSG_ERR_NULL, "NULL argument");
+    *out = nullptr;
+    if (count < 1) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Empty batch");
+    if (!circuits) return set_error(AQSG_ERR_NULL, "NULL circuit list");
+    AQSG_CUDA_TRY(cudaSetDevice(ctx->device));
+    auto* b = new aqsg_batch_s();
+    b->ctx = ctx;
+    b->count = count;
+    b->n.resize(count);
+    b->out_off.resize(count);
+    for (int i = 0; i < count; ++i) {
+        const int n = circuits[i].n;
+        if (n < 1 || n > 30) {
+            delete b;
+            return set_error(AQSG_ERR_INVALID_ARGUMENT, "Batch registers take 1 to 30 qubits");
+        }
+        if (circuits[i].count > 0 && !circuits[i].ops) {
+            delete b;
+            return set_error(AQSG_ERR_NULL, "NULL op list");
+        }
+        b->n[i] = n;
+        b->out_off[i] = b->out_doubles;
+        b->out_doubles += 2 * (size_t)n;
+    }
+    int rc = encode_batch(b, circuits, true);
+    auto fail = [&](int code) {
+        free_batch(b);
+        return code;
+    };
+    if (rc) return fail(rc);
+    cudaError_t e = cudaSuccess;
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
+        if (b->items[c].empty()) continue;
+        const size_t tb = b->small_table[c].size();
+        const size_t poff = (tb + 255) & ~size_t(255);
+        e = cudaMalloc(&b->d_small_ops[c], poff + b->small_pool[c].size() + 16);
+        if (e == cudaSuccess) e = cudaMalloc(&b->d_small_items[c], sizeof(SmallItem) * b->items[c].size());
+        if (e == cudaSuccess)
+            e = cudaMemcpy(b->d_small_items[c], b->items[c].data(), sizeof(SmallItem) * b->items[c].size(),
+                           cudaMemcpyHostToDevice);
+    }
+    size_t large_bytes = 0;
+    for (const TilePlan& p : b->plans) {
+        b->plan_off.push_back(large_bytes);
+        large_bytes += (p.pool_offset() + p.pool.size() + 255) & ~size_t(255);
+    }
+    if (e == cudaSuccess && large_bytes) e = cudaMalloc(&b->d_large, large_bytes);
+    // branch streams: three for the small classes, up to kMaxBranches overall
+    int nb = 3;
+    if ((int)b->large.size() + 3 > nb) nb = (int)b->large.size() + 3;
+    if (nb > kMaxBranches) nb = kMaxBranches;
+    b->streams.assign(nb, nullptr);
+    b->joins.assign(nb, nullptr);
+    b->regs.assign(nb, nullptr);
+    b->partials.assign(nb, nullptr);
+    for (int k = 0; k < nb && e == cudaSuccess; ++k) {
+        e = cudaStreamCreateWithFlags(&b->streams[k], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->joins[k], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    std::vector<int> branch_max(nb, 0);
+    for (size_t k = 0; k < b->large.size(); ++k) {
+        const int br = branch_of_large(b, k);
+        branch_max[br] = std::max(branch_max[br], b->n[b->large[k]]);
+    }
+    for (int k = 0; k < nb && e == cudaSuccess; ++k) {
+        if (!branch_max[k]) continue;
+        e = cudaMalloc(&b->regs[k], (size_t)8 << branch_max[k]);
+        if (e == cudaSuccess) e = cudaMalloc(&b->partials[k], sizeof(double) * expz_partial_doubles(branch_max[k]));
+    }
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_out, sizeof(double) * b->out_doubles);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&b->h_out, sizeof(double) * b->out_doubles);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_counters, 4 * sizeof(int));
+    if (e != cudaSuccess) return fail(cuda_error(e, "aqsg_batch_create"));
+    // persistent grids: resident CTAs per SM x SMs, at most one CTA per circuit
+    for (int c = 0; c < 3; ++c) {
+        if (b->items[c].empty()) continue;
+        const size_t shm = (size_t)8 << kClasses[c].max_n;
+        int per_sm = 1;
+        if (c == 0) {
+            cudaFuncSetAttribute(k_batch_small<8, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_small<8, 128>, 128, shm);
+        } else if (c == 1) {
+            cudaFuncSetAttribute(k_batch_small<16, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_small<16, 256>, 256, shm);
+        } else {
+            cudaFuncSetAttribute(k_batch_small<32, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_small<32, 512>, 512, shm);
+        }
+        if (per_sm < 1) per_sm = 1;
+        const int want = per_sm * ctx->sm_count;
+        b->grid[c] = (int)b->items[c].size() < want ? (int)b->items[c].size() : want;
+    }
+    if ((rc = upload_batch(b, ctx->stream))) return fail(rc);
+    // capture the run once
+    e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) return fail(cuda_error(e, "cudaStreamBeginCapture"));
+    rc = record_batch(b, ctx->stream);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(ctx->stream, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return fail(rc);
+    }
+    if (e != cudaSuccess) return fail(cuda_error(e, "cudaStreamEndCapture"));
+    b->graph = g;
+    e = cudaGraphInstantiate(&b->exec, g, 0);
+    if (e != cudaSuccess) return fail(cuda_error(e, "cudaGraphInstantiate"));
+    *out = b;
+    return AQSG_OK;
+}
+
+int aqsg_batch_update(aqsg_batch b, const aqsg_circuit* circuits) {
+    if (!b || !circuits) return set_error(AQSG_ERR_NULL, "NULL argument");
+    AQSG_CUDA_TRY(cudaSetDevice(b->ctx->device));
+    if (int rc = encode_batch(b, circuits, false)) return rc;
+    return upload_batch(b, b->ctx->stream);
+}
+
+int aqsg_batch_run(aqsg_batch b, double* z, double* zz) {
+    if (!b) return set_error(AQSG_ERR_NULL, "NULL batch");
+    aqsg_ctx_s* c = b->ctx;
+    AQSG_CUDA_TRY(cudaSetDevice(c->device));
+    AQSG_CUDA_TRY(cudaGraphLaunch(b->exec, c->stream));
+    c->launches += b->kernels;
+    AQSG_CUDA_TRY(cudaMemcpyAsync(b->h_out, b->d_out, sizeof(double) * b->out_doubles, cudaMemcpyDeviceToHost,
+                                  c->stream));
+    AQSG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    size_t zo = 0, zzo = 0;
+    for (int i = 0; i < b->count; ++i) {
+        const int n = b->n[i];
+        const double* r = b->h_out + b->out_off[i];
+        const double tot = r[2 * n - 1];
+        for (int q = 0; q < n; ++q)
+            if (z) z[zo + q] = tot - 2.0 * r[n - 1 - q];
+        for (int q = 0; q + 1 < n; ++q)
+            if (zz) zz[zzo + q] = tot - 2.0 * r[n + (n - 2 - q)];
+        zo += n;
+        zzo += n - 1;
+    }
+    return AQSG_OK;
+}
+
+int aqsg_batch_info(aqsg_batch b, int* small_circuits, int* large_circuits, int* kernels) {
+    if (!b) return set_error(AQSG_ERR_NULL, "NULL batch");
+    if (small_circuits) *small_circuits = (int)(b->items[0].size() + b->items[1].size() + b->items[2].size());
+    if (large_circuits) *large_circuits = (int)b->large.size();
+    if (kernels) *kernels = (int)b->kernels;
+    return AQSG_OK;
+}
+
+int aqsg_batch_free(aqsg_batch b) {
+    if (!b) return set_error(AQSG_ERR_NULL, "NULL batch");
+    cudaStreamSynchronize(b->ctx->stream);
+    free_batch(b);
+    return AQSG_OK;
+}
+
+}  // extern "C"

@@ -571,6 +571,9 @@ int launch_collapse_qubit(aqsg_state_s* st, uint64_t mask, int outcome, double s
 
 constexpr int kZMaxS = 12;
 
+size_t expz_partial_doubles(int n);
+int launch_expz_raw(const void* sv, int n, int dtype, double* partial, double* out_raw, cudaStream_t stream);
+
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_expz_partial(const T* __restrict__ sv, int tb, int rb, double* partial) {
@@ -647,20 +650,12 @@ template <typename T>
 static int expect_z_t(aqsg_state_s* st, double* z, double* zz) {
     aqsg_ctx_s* c = st->ctx;
     const int n = st->n;
-    const int rb = n < 20 ? n : 20;
-    int tb = rb < 8 ? rb : 8;
-    if (rb - tb > kZMaxS) tb = rb - kZMaxS;
-    const uint64_t nblocks = st->amps >> rb;
-    const size_t pbytes = sizeof(double) * (nblocks * 2 * rb + 2 * n + 1);
-    if (int rc = ensure_scratch(c->partial, pbytes)) return rc;
+    const size_t pd = expz_partial_doubles(n);
+    if (int rc = ensure_scratch(c->partial, sizeof(double) * (pd + 2 * n + 1))) return rc;
     double* partial = (double*)c->partial.ptr;
-    double* res = partial + nblocks * 2 * rb;
-    // at least one full warp: the block reductions shuffle over all 32 lanes
-    const int threads = (1 << tb) < 32 ? 32 : (1 << tb);
-    k_expz_partial<T><<<(unsigned)nblocks, threads, 0, c->stream>>>((const T*)st->d, tb, rb, partial);
-    k_expz_final<<<1, 128, 0, c->stream>>>(partial, n, rb, nblocks, res);
+    double* res = partial + pd;
+    if (int rc = launch_expz_raw(st->d, n, st->dtype, partial, res, c->stream)) return rc;
     c->launches += 2;
-    AQSG_CUDA_TRY(cudaGetLastError());
     std::vector<double> h(2 * n);
     AQSG_CUDA_TRY(cudaMemcpyAsync(h.data(), res, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, c->stream));
     AQSG_CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -758,3 +753,31 @@ extern "C" int aqsg_state_compare(aqsg_state a, aqsg_state b, double* max_abs_di
     if (norm2_b) *norm2_b = r[4];
     return AQSG_OK;
 }
+
+// ---- raw <Z> sums without a host read (the batched engine) -----------------------
+
+namespace aqsg {
+
+size_t expz_partial_doubles(int n) {
+    const int rb = n < 20 ? n : 20;
+    return ((size_t)1 << (n - rb)) * 2 * (size_t)rb;
+}
+
+// Writes the 2n raw sums (S over index bits, X over neighbour bit pairs, then
+// the total) of register sv to out_raw, on `stream`, without synchronising.
+int launch_expz_raw(const void* sv, int n, int dtype, double* partial, double* out_raw, cudaStream_t stream) {
+    const int rb = n < 20 ? n : 20;
+    int tb = rb < 8 ? rb : 8;
+    if (rb - tb > kZMaxS) tb = rb - kZMaxS;
+    const uint64_t nblocks = (1ull << n) >> rb;
+    const int threads = (1 << tb) < 32 ? 32 : (1 << tb);
+    if (dtype == AQSG_C64)
+        k_expz_partial<float2><<<(unsigned)nblocks, threads, 0, stream>>>((const float2*)sv, tb, rb, partial);
+    else
+        k_expz_partial<double2><<<(unsigned)nblocks, threads, 0, stream>>>((const double2*)sv, tb, rb, partial);
+    k_expz_final<<<1, 128, 0, stream>>>(partial, n, rb, nblocks, out_raw);
+    AQSG_CUDA_TRY(cudaGetLastError());
+    return AQSG_OK;
+}
+
+}  // namespace aqsg

@@ -272,6 +272,73 @@ def bench_plain12(ctx, stream, n=12, layers=10):
     return res
 
 
+def bench_vqe_batch(ctx, count=4096, seed=5):
+    """The batched VQE sweep: `count` hardware-efficient-ansatz circuits
+    (qubits uniform in 8..20, layers uniform in 4..12, angles uniform in
+    [-pi, pi], seed 5), each to <Z_q> and <Z_q Z_q+1> in FP64, as one
+    CUDA-graph replay; then new angles for every circuit and another replay.
+    CPU baseline: the FP64 per-gate oracle on every 64th circuit, all host
+    threads, scaled to the sweep by amplitude-gate work."""
+    import time as _t
+
+    import afquantumsim_gb300 as aq
+    from afquantumsim_gb300 import circuits
+    from oracle import oracle
+    items = circuits.vqe_sweep(count, seed=seed)
+    gates = sum(len(ops) for _, ops in items)
+    work = sum(len(ops) * (1 << n) for n, ops in items)
+    t0 = _t.perf_counter()
+    b = aq.Batch(ctx, items)
+    create_s = _t.perf_counter() - t0
+    info = b.info()
+    b.run()
+    b.run()
+    reps = 5
+    t0 = _t.perf_counter()
+    for _ in range(reps):
+        z, zz = b.run()
+    sweep_s = (_t.perf_counter() - t0) / reps
+    rng = np.random.default_rng(seed + 1)
+    new = []
+    for n, ops in items:  # same shapes (n >= 8: 3n ops per layer), new angles
+        L = len(ops) // (3 * n)
+        new.append((n, circuits.vqe_ops_array(n, L, rng.uniform(-np.pi, np.pi, size=(L, n, 2)))))
+    t0 = _t.perf_counter()
+    b.update(new)
+    z, zz = b.run()
+    update_run_s = _t.perf_counter() - t0
+    # accuracy on a sample against the FP64 oracle
+    err = 0.0
+    sample = list(range(0, count, 64))
+    threads = len(os.sched_getaffinity(0))
+    oracle.set_threads(threads)
+    cpu_s = 0.0
+    cpu_work = 0
+    for i in sample:
+        n, ops = new[i]
+        v = np.zeros(1 << n, dtype=np.complex128)
+        v[0] = 1
+        olist = list((aq.Op * len(ops)).from_buffer_copy(ops.tobytes()))
+        t0 = _t.perf_counter()
+        v = oracle.apply_f64(v, olist)
+        cpu_s += _t.perf_counter() - t0
+        cpu_work += len(ops) * (1 << n)
+        p = np.abs(v) ** 2
+        idx = np.arange(1 << n)
+        wz = np.array([np.sum(p * (1 - 2 * ((idx >> (n - 1 - q)) & 1))) for q in range(n)])
+        err = max(err, float(np.max(np.abs(wz - z[i]))))
+    b.free()
+    cpu_sweep_est = cpu_s * work / cpu_work
+    return {"workload": f"vqe_sweep{count}", "gates": gates, "small_circuits": info["small"],
+            "large_circuits": info["large"], "kernels_per_replay": info["kernels"],
+            "create_s": round(create_s, 3), "sweep_ms": round(1e3 * sweep_s, 3),
+            "circuits_per_s": round(count / sweep_s, 1), "gate_apps_per_s": round(gates / sweep_s, 1),
+            "update_and_run_ms": round(1e3 * update_run_s, 3),
+            "max_abs_err_z_vs_fp64_sample": err,
+            "cpu_baseline": {"kind": "port", "cores": threads, "sample": f"{len(sample)} circuits (every 64th)",
+                             "sample_s": round(cpu_s, 3), "sweep_s_scaled": round(cpu_sweep_est, 2)}}
+
+
 # ---- our arm ------------------------------------------------------------------------
 
 def run_ours(args, rank, world, local_rank):
@@ -408,6 +475,7 @@ def run_ours(args, rank, world, local_rank):
         if args.dtype == "c64":
             extras["fused_brickwork"] = bench_fused_brickwork(ctx, st, stream, n, depth=20)
         extras["plain12"] = bench_plain12(ctx, stream)
+        extras["vqe_batch"] = bench_vqe_batch(ctx)
 
     cpu = None
     if rank == 0:

@@ -252,6 +252,40 @@ int aqsg_program_export(aqsg_program prog, aqsg_op* out, int capacity, int* coun
 
 int aqsg_program_free(aqsg_program prog);
 
+/* ---- batched engine (many independent registers) ------------------------ */
+
+/* One circuit of a batch: an n-qubit c64 register, run from |0...0>. */
+typedef struct aqsg_circuit {
+    int32_t n;
+    int32_t count;
+    const aqsg_op* ops;
+} aqsg_circuit;
+
+typedef struct aqsg_batch_s* aqsg_batch;
+
+/* Plan a batch of independent circuits of uneven size, each ending in
+ * <Z_q> and <Z_q Z_q+1> summed in FP64.  It generalises the reference's VQE
+ * cost loop (src/quantum_algo.cpp:412-456: one simulate and one expectation
+ * read per parameter set) to a whole sweep.  Registers of up to 14 qubits run
+ * entirely in shared memory (a persistent kernel per size class, one CTA per
+ * circuit); larger ones (up to 30) run as tile passes over one reused device
+ * register.  The whole run is captured once as a CUDA graph. */
+int aqsg_batch_create(aqsg_ctx ctx, const aqsg_circuit* circuits, int count, aqsg_batch* out);
+
+/* Swap in new parameters (angles, matrices): the same count, qubit counts,
+ * gate kinds and operands as at creation; the graph is kept. */
+int aqsg_batch_update(aqsg_batch b, const aqsg_circuit* circuits);
+
+/* Replay the graph.  z receives sum_i n_i values (<Z_q> of circuit i at
+ * offset sum_{j<i} n_j), zz receives sum_i (n_i - 1) values of <Z_q Z_q+1>;
+ * either may be NULL. */
+int aqsg_batch_run(aqsg_batch b, double* z, double* zz);
+
+/* Circuits run in shared memory / as tile passes, kernels per replay. */
+int aqsg_batch_info(aqsg_batch b, int* small_circuits, int* large_circuits, int* kernels);
+
+int aqsg_batch_free(aqsg_batch b);
+
 /* ---- measurement ---------------------------------------------------------- */
 
 /* Probability that `qubit` reads |1>, summed in FP64.
