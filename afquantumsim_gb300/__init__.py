@@ -39,6 +39,8 @@ EXPORTS = [
     "aqsg_state_compare", "aqsg_compile", "aqsg_program_info", "aqsg_run_program", "aqsg_program_export",
     "aqsg_program_free", "aqsg_batch_create", "aqsg_batch_update", "aqsg_batch_run",
     "aqsg_batch_info", "aqsg_batch_free",
+    "aqsg_server_create", "aqsg_server_submit", "aqsg_server_start", "aqsg_server_poll",
+    "aqsg_server_wait_idle", "aqsg_server_get_stats", "aqsg_server_destroy",
 ]
 
 _lib = None
@@ -570,3 +572,100 @@ class Batch:
         if self.h:
             _check(self.lib.aqsg_batch_free(self.h))
             self.h = None
+
+
+# ---- serving runtime -----------------------------------------------------------
+
+class ServerDone(C.Structure):
+    """struct aqsg_server_done."""
+    _fields_ = [("ticket", C.c_uint64), ("status", C.c_int32), ("n", C.c_int32),
+                ("lane", C.c_int32), ("fused_ops", C.c_int32), ("arrival_s", C.c_double),
+                ("admit_s", C.c_double), ("done_s", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    """struct aqsg_server_stats."""
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("slab_bytes", C.c_uint64), ("peak_bytes", C.c_uint64),
+                ("peak_running", C.c_int32), ("lanes", C.c_int32), ("launches", C.c_uint64)]
+
+
+def _bind_server(lib):
+    P, I, U64, U32, D = C.c_void_p, C.c_int, C.c_uint64, C.c_uint32, C.c_double
+    lib.aqsg_server_create.argtypes = [I, I, U64, I, I, U32, C.POINTER(P)]
+    lib.aqsg_server_submit.argtypes = [P, I, C.POINTER(Op), I, I, U32, U64, D,
+                                       C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+    lib.aqsg_server_start.argtypes = [P]
+    lib.aqsg_server_poll.argtypes = [P, C.POINTER(ServerDone), I, C.POINTER(I)]
+    lib.aqsg_server_wait_idle.argtypes = [P, D]
+    lib.aqsg_server_get_stats.argtypes = [P, C.POINTER(ServerStats)]
+    lib.aqsg_server_destroy.argtypes = [P]
+    for f in ("aqsg_server_create", "aqsg_server_submit", "aqsg_server_start", "aqsg_server_poll",
+              "aqsg_server_wait_idle", "aqsg_server_get_stats", "aqsg_server_destroy"):
+        getattr(lib, f).restype = I
+
+
+class Server:
+    """aqsg_server: a stream of independent requests (circuit from |0...0>,
+    then `shots` seeded measure-all draws) admitted by arrival time and HBM
+    onto concurrent lanes over one register slab."""
+
+    def __init__(self, device: int = 0, dtype: int = C64, hbm_budget_bytes: int = 8 << 30,
+                 lanes: int = 8, max_qubits: int = 28, max_shots: int = 1024):
+        self.lib = load_library()
+        _bind_server(self.lib)
+        h = C.c_void_p()
+        _check(self.lib.aqsg_server_create(device, dtype, hbm_budget_bytes, lanes, max_qubits,
+                                           max_shots, C.byref(h)))
+        self.h = h
+        self._outs = {}  # ticket -> (outcome array, op array kept alive until submit returns)
+
+    def submit(self, n: int, ops, shots: int = 1024, seed: int = 0, arrival_s: float = -1.0,
+               fuse_qubits: int = 0) -> int:
+        if isinstance(ops, np.ndarray):
+            a = np.ascontiguousarray(ops)
+            ptr, count = C.cast(a.ctypes.data, C.POINTER(Op)), len(a)
+        else:
+            a = ops if isinstance(ops, C.Array) else op_array(list(ops))
+            ptr, count = C.cast(a, C.POINTER(Op)), len(a)
+        out = np.zeros(max(shots, 1), dtype=np.uint64)
+        t = C.c_uint64()
+        _check(self.lib.aqsg_server_submit(self.h, n, ptr, count, fuse_qubits, shots, seed, arrival_s,
+                                           out.ctypes.data_as(C.POINTER(C.c_uint64)), C.byref(t)))
+        self._outs[t.value] = out[:shots]
+        return t.value
+
+    def start(self) -> None:
+        _check(self.lib.aqsg_server_start(self.h))
+
+    def poll(self, capacity: int = 4096):
+        """Finished requests: list of dicts (ticket, status, n, lane, fused_ops,
+        arrival_s, admit_s, done_s, outcomes)."""
+        buf = (ServerDone * capacity)()
+        k = C.c_int()
+        _check(self.lib.aqsg_server_poll(self.h, buf, capacity, C.byref(k)))
+        out = []
+        for d in buf[:k.value]:
+            rec = {f: getattr(d, f) for f, _ in ServerDone._fields_}
+            rec["outcomes"] = self._outs.pop(d.ticket)
+            out.append(rec)
+        return out
+
+    def wait_idle(self, timeout_s: float = 600.0) -> None:
+        _check(self.lib.aqsg_server_wait_idle(self.h, timeout_s))
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        _check(self.lib.aqsg_server_get_stats(self.h, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in ServerStats._fields_}
+
+    def close(self) -> None:
+        if self.h:
+            _check(self.lib.aqsg_server_destroy(self.h))
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

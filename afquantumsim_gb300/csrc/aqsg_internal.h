@@ -139,5 +139,16 @@ int sample(aqsg_state_s* st, const double* host_u, uint64_t seed, bool seeded,
 int launch_collapse_qubit(aqsg_state_s* st, uint64_t mask, int outcome,
                           double scale);
 int expect_z(aqsg_state_s* st, double* z, double* zz);
+// asynchronous variants (no host read; scratch reserved beforehand)
+int reserve_scratch(aqsg_ctx_s* c, int n, uint64_t shots);
+int launch_norm_to_device(aqsg_state_s* st, double* d_out);
+int launch_renorm_device(aqsg_state_s* st, const double* n_before, const double* n_after);
+int sample_seeded_async(aqsg_state_s* st, uint64_t seed, uint64_t count, int rule, uint64_t* pinned_out);
+// Tile passes without host synchronisation; dev_table is the device copy of
+// plan.table followed by plan.pool at plan.pool_offset().  Tensor-core runs
+// renormalise on the device through d_norms[0..1].
+int run_plan_async(aqsg_state_s* st, const TilePlan& plan, const void* dev_table, double* d_norms);
+// The fused op list of a compiled program.
+const std::vector<LOp>& program_ops(aqsg_program p);
 
 }  // namespace aqsg

@@ -32,6 +32,8 @@ namespace aqsg {
 
 using cd = std::complex<double>;
 
+const std::vector<LOp>& program_ops(aqsg_program p) { return p->ops; }
+
 static uint64_t support(const LOp& o) {
     uint64_t s = o.cmask | o.amask;
     if (o.t0 >= 0) s |= 1ull << o.t0;

@@ -781,3 +781,103 @@ int launch_expz_raw(const void* sv, int n, int dtype, double* partial, double* o
 }
 
 }  // namespace aqsg
+
+// ---- asynchronous variants (no host read) for the serving runtime -------------------
+
+namespace aqsg {
+
+// FP64 sum of |a|^2 into d_out (device), on the context stream.
+int launch_norm_to_device(aqsg_state_s* st, double* d_out) {
+    aqsg_ctx_s* c = st->ctx;
+    uint64_t units = st->amps;
+    const bool vec2 = st->dtype == AQSG_C64 && units >= 2;
+    if (vec2) units >>= 1;
+    const unsigned grid = stream_grid(st, units, kRedThreads);
+    if (c->partial.bytes < sizeof(double) * (grid + 1))
+        return set_error(AQSG_ERR_RUNTIME, "Reduction scratch not reserved");
+    double* partial = (double*)c->partial.ptr;
+    Fix<0> fx;
+    fx.pos[0] = 0;
+    fx.val = 0;
+    if (st->dtype == AQSG_C64) {
+        if (vec2)
+            k_prob_partial<float, 2, Fix<0>><<<grid, kRedThreads, 0, c->stream>>>((const float2*)st->d, fx, units, partial);
+        else
+            k_prob_partial<float, 1, Fix<0>><<<grid, kRedThreads, 0, c->stream>>>((const float2*)st->d, fx, units, partial);
+    } else {
+        k_prob_partial<double, 1, Fix<0>><<<grid, kRedThreads, 0, c->stream>>>((const double2*)st->d, fx, units, partial);
+    }
+    k_sum_partials<<<1, 256, 0, c->stream>>>(partial, (int)grid, d_out);
+    c->launches += 2;
+    AQSG_CUDA_TRY(cudaGetLastError());
+    return AQSG_OK;
+}
+
+template <typename T, typename R>
+__global__ void k_scale_dev(T* sv, uint64_t N, const double* n_before, const double* n_after) {
+    const double nb = *n_before, na = *n_after;
+    const R s = (na > 0 && nb > 0) ? (R)sqrt(nb / na) : (R)1;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        T a = sv[i];
+        a.x *= s;
+        a.y *= s;
+        sv[i] = a;
+    }
+}
+
+// Scale the register by sqrt(*n_before / *n_after), both read on the device.
+int launch_renorm_device(aqsg_state_s* st, const double* n_before, const double* n_after) {
+    const unsigned grid = stream_grid(st, st->amps, 256);
+    if (st->dtype == AQSG_C64)
+        k_scale_dev<float2, float><<<grid, 256, 0, st->ctx->stream>>>((float2*)st->d, st->amps, n_before, n_after);
+    else
+        k_scale_dev<double2, double><<<grid, 256, 0, st->ctx->stream>>>((double2*)st->d, st->amps, n_before, n_after);
+    st->ctx->launches++;
+    AQSG_CUDA_TRY(cudaGetLastError());
+    return AQSG_OK;
+}
+
+// Reserve the context scratch a register of n qubits and `shots` samples
+// need, so the asynchronous calls below never allocate.
+int reserve_scratch(aqsg_ctx_s* c, int n, uint64_t shots) {
+    const uint64_t nchunks = (1ull << n) >> (n < kChunkBits ? n : kChunkBits);
+    const size_t red = sizeof(double) * ((size_t)c->sm_count * 8 + 1);
+    size_t need = sizeof(double) * nchunks;
+    if (red > need) need = red;
+    if (int rc = ensure_scratch(c->partial, need + 64)) return rc;
+    if (int rc = ensure_scratch(c->prefix, sizeof(double) * nchunks)) return rc;
+    if (int rc = ensure_scratch(c->sample_o, sizeof(uint64_t) * (shots ? shots : 1))) return rc;
+    return AQSG_OK;
+}
+
+// Seeded sampling whose outcomes land in pinned host memory when the
+// context stream reaches that point; nothing waits.
+int sample_seeded_async(aqsg_state_s* st, uint64_t seed, uint64_t count, int rule, uint64_t* pinned_out) {
+    aqsg_ctx_s* c = st->ctx;
+    const int cb = st->n < kChunkBits ? st->n : kChunkBits;
+    const uint64_t nchunks = st->amps >> cb;
+    if (c->partial.bytes < sizeof(double) * nchunks || c->prefix.bytes < sizeof(double) * nchunks ||
+        c->sample_o.bytes < sizeof(uint64_t) * count)
+        return set_error(AQSG_ERR_RUNTIME, "Sampling scratch not reserved");
+    if (st->dtype == AQSG_C64) {
+        k_chunk_sums<float2><<<(unsigned)nchunks, 256, 0, c->stream>>>((const float2*)st->d, cb, (double*)c->partial.ptr);
+    } else {
+        k_chunk_sums<double2><<<(unsigned)nchunks, 256, 0, c->stream>>>((const double2*)st->d, cb, (double*)c->partial.ptr);
+    }
+    k_scan<<<1, 1024, 0, c->stream>>>((const double*)c->partial.ptr, (double*)c->prefix.ptr, nchunks);
+    const unsigned grid = (unsigned)((count * 32 + 255) / 256);
+    if (st->dtype == AQSG_C64)
+        k_sample<float2><<<grid, 256, 0, c->stream>>>((const float2*)st->d, cb, nchunks, (const double*)c->prefix.ptr,
+                                                       nullptr, seed, 1, count, rule, (uint64_t*)c->sample_o.ptr);
+    else
+        k_sample<double2><<<grid, 256, 0, c->stream>>>((const double2*)st->d, cb, nchunks, (const double*)c->prefix.ptr,
+                                                        nullptr, seed, 1, count, rule, (uint64_t*)c->sample_o.ptr);
+    c->launches += 3;
+    AQSG_CUDA_TRY(cudaGetLastError());
+    AQSG_CUDA_TRY(cudaMemcpyAsync(pinned_out, c->sample_o.ptr, sizeof(uint64_t) * count, cudaMemcpyDeviceToHost,
+                                  c->stream));
+    return AQSG_OK;
+}
+
+}  // namespace aqsg

@@ -223,6 +223,24 @@ static void tc_operand(const std::vector<double>& mk, int k, std::vector<unsigne
         }
 }
 
+// A matrix with one non-zero per row, each 1 (a permutation), is applied on
+// CUDA cores, where x * 1 + 0 * y is exact; the split-bf16 tensor-core
+// product keeps only 16 significant bits of each amplitude.
+static bool is_permutation(const std::vector<double>& mk, int k) {
+    const int D = 1 << k;
+    for (int r = 0; r < D; ++r) {
+        int ones = 0;
+        for (int c = 0; c < D; ++c) {
+            const double re = mk[2 * (r * D + c)], im = mk[2 * (r * D + c) + 1];
+            if (im != 0.0) return false;
+            if (re == 1.0) ++ones;
+            else if (re != 0.0) return false;
+        }
+        if (ones != 1) return false;
+    }
+    return true;
+}
+
 static void pad_to(std::vector<unsigned char>& v, size_t align) {
     v.resize((v.size() + align - 1) / align * align, 0);
 }
@@ -269,7 +287,7 @@ int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, Tile
             if (o->cls == L_MATK) {
                 pad_to(plan->pool, 256);
                 t.mat = (int32_t)plan->pool.size();
-                if (tc_pass && o->k >= 3 && t.cm_loc == 0) {
+                if (tc_pass && o->k >= 3 && t.cm_loc == 0 && !is_permutation(o->mk, o->k)) {
                     t.pad = 1;  // tensor-core op
                     tp.tc = 1;
                     tc_operand(o->mk, o->k, plan->pool);
@@ -383,6 +401,19 @@ int run_tiled(aqsg_state_s* st, const std::vector<LOp>& ops) {
         if (int rc = reduce_prob(st, 0, 0, &norm_after)) return rc;
         if (norm_after > 0 && norm_before > 0)
             if (int rc = launch_scale(st, std::sqrt(norm_before / norm_after))) return rc;
+    }
+    return AQSG_OK;
+}
+
+int run_plan_async(aqsg_state_s* st, const TilePlan& plan, const void* dev_table, double* d_norms) {
+    aqsg_ctx_s* c = st->ctx;
+    if (plan.passes.empty()) return AQSG_OK;
+    if (plan.any_tc)
+        if (int rc = launch_norm_to_device(st, d_norms)) return rc;
+    if (int rc = launch_tile_plan(st->d, plan, dev_table, c->stream, c->d_err, &c->launches)) return rc;
+    if (plan.any_tc) {
+        if (int rc = launch_norm_to_device(st, d_norms + 1)) return rc;
+        if (int rc = launch_renorm_device(st, d_norms, d_norms + 1)) return rc;
     }
     return AQSG_OK;
 }

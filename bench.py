@@ -339,11 +339,85 @@ def bench_vqe_batch(ctx, count=4096, seed=5):
                              "sample_s": round(cpu_s, 3), "sweep_s_scaled": round(cpu_sweep_est, 2)}}
 
 
+def serving_requests(count, seed=6):
+    """The serving stream's requests: brick-work circuits (Haar SU(2) as
+    RotZ.RotY.RotZ + CZ layers) with qubits uniform in 10..28 and depth
+    uniform in 5..30, each with its own sampling seed."""
+    import afquantumsim_gb300 as aq
+    from afquantumsim_gb300 import circuits
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(count):
+        n = int(rng.integers(10, 29))
+        d = int(rng.integers(5, 31))
+        reqs.append((n, aq.op_array(circuits.brickwork(n, d, seed=10_000 + i)), int(rng.integers(1 << 40))))
+    return reqs
+
+
+def bench_serving(ctx, count=160, seed=6, shots=1024, fuse=5, lanes=8, budget_gib=32, load=0.7):
+    """The serving loop: `count` requests through aqsg_server (HBM slab of
+    `budget_gib` GiB cut by register size 2^n x 8 B, `lanes` concurrent
+    lanes, fusion width `fuse`, 1024 seeded shots each).  First every request
+    arrives at t = 0 (capacity, circuits/s); then the same requests arrive as
+    a Poisson stream (seed 6) at `load` x that capacity, and latency
+    (arrival -> outcomes on the host) is reported as p50/p99.  Accuracy: the
+    fused c64 state of the three smallest requests against the same circuit
+    one gate per pass in c128 (the server's outcomes are those of the direct
+    path, which the tests check bit for bit)."""
+    import time as _t
+
+    import afquantumsim_gb300 as aq
+    t0 = _t.perf_counter()
+    reqs = serving_requests(count, seed)
+    gen_s = _t.perf_counter() - t0
+    gates = sum(len(o) for _, o, _ in reqs)
+
+    def run(arrivals):
+        srv = aq.Server(0, aq.C64, budget_gib << 30, lanes, 28, shots)
+        t1 = _t.perf_counter()
+        for (n, ops, sd), a in zip(reqs, arrivals):
+            srv.submit(n, ops, shots, sd, float(a), fuse)
+        submit_s = _t.perf_counter() - t1
+        srv.start()
+        srv.wait_idle(900)
+        done = srv.poll(count + 8)
+        stats = srv.stats()
+        srv.close()
+        assert len(done) == count and all(d["status"] == 0 for d in done)
+        lat = np.array([d["done_s"] - d["arrival_s"] for d in done])
+        span = max(d["done_s"] for d in done) - min(d["arrival_s"] for d in done)
+        return {"circuits_per_s": round(count / span, 2), "gate_apps_per_s": round(gates / span, 1),
+                "makespan_s": round(span, 3), "p50_latency_ms": round(1e3 * float(np.percentile(lat, 50)), 2),
+                "p99_latency_ms": round(1e3 * float(np.percentile(lat, 99)), 2),
+                "peak_running": stats["peak_running"], "peak_slab_gib": round(stats["peak_bytes"] / 2**30, 2),
+                "host_submit_s": round(submit_s, 2), "kernel_launches": stats["launches"]}
+
+    sat = run(np.zeros(count))
+    rate = load * sat["circuits_per_s"]
+    arrivals = np.cumsum(np.random.default_rng(seed).exponential(1.0 / rate, size=count))
+    poisson = run(arrivals)
+    poisson["arrival_rate_per_s"] = round(rate, 2)
+    err = 0.0
+    for n, ops, _ in sorted(reqs, key=lambda r: r[0])[:3]:
+        prog = aq.Program(n, list(ops), aq.C64, max_qubits=fuse)
+        with aq.State(ctx, n, aq.C64) as a, aq.State(ctx, n, aq.C128) as b:
+            a.set_basis(0)
+            prog.run(a, aq.EXEC_TILED)
+            b.set_basis(0)
+            b.apply(ops, aq.EXEC_PER_GATE)
+            err = max(err, a.compare(b)[0])
+        prog.free()
+    return {"workload": f"serving{count}_brickwork_n10-28_d5-30", "shots": shots, "fuse_qubits": fuse,
+            "lanes": lanes, "hbm_budget_gib": budget_gib, "gates": gates, "requests_gen_s": round(gen_s, 2),
+            "saturated": sat, "poisson": poisson, "max_abs_err_vs_fp64_3_smallest": err}
+
+
 # ---- our arm ------------------------------------------------------------------------
 
 def run_ours(args, rank, world, local_rank):
     import torch
     import afquantumsim_gb300 as aq
+    from afquantumsim_gb300 import replicas
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
@@ -359,7 +433,7 @@ def run_ours(args, rank, world, local_rank):
 
     # seeded input, normalised, staged in pinned host memory (not timed)
     g = torch.Generator(device=dev)
-    g.manual_seed(3 + rank)
+    g.manual_seed(replicas.rank_seed(3, rank))
     x = torch.randn(N, dtype=dt_t, device=dev, generator=g)
     x /= torch.linalg.vector_norm(x)
     host_in = torch.empty(N, dtype=dt_t, pin_memory=True)
@@ -399,14 +473,12 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.synchronize()
     launches = ctx.launch_count() - launches0
     ms = ev0.elapsed_time(ev1)
+    ms, total_gates = replicas.reduce_timing(ms, gates * args.steps, dev if world > 1 else None)
     if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
         torch.distributed.barrier()
     ms_per_step = ms / args.steps
-    value = world * gates * args.steps / (ms / 1e3)
-    hbm_gbs = world * total_bytes * args.steps / (ms / 1e3) / 1e9
+    value = total_gates / (ms / 1e3)
+    hbm_gbs = total_gates / gates * total_bytes / (ms / 1e3) / 1e9
 
     # dominant kernel in isolation: the controlled-phase pass (N/4 amplitudes)
     cp_ops = aq.op_array([o for o in qft_ops(n) if o.kind == aq.kinds.CPHASE])
@@ -476,6 +548,8 @@ def run_ours(args, rank, world, local_rank):
             extras["fused_brickwork"] = bench_fused_brickwork(ctx, st, stream, n, depth=20)
         extras["plain12"] = bench_plain12(ctx, stream)
         extras["vqe_batch"] = bench_vqe_batch(ctx)
+        if args.dtype == "c64":
+            extras["serving"] = bench_serving(ctx)
 
     cpu = None
     if rank == 0:

@@ -286,6 +286,80 @@ int aqsg_batch_info(aqsg_batch b, int* small_circuits, int* large_circuits, int*
 
 int aqsg_batch_free(aqsg_batch b);
 
+/* ---- serving runtime (a stream of independent requests) ------------------ */
+
+/* A request is one circuit run from |0...0> followed by `shots` seeded
+ * measure-all draws: QSimulator::simulate (quantum.cpp:277) then repeated
+ * peek_measure_all (quantum.cpp:343-358, sample rule AQSG_SAMPLE_REFERENCE,
+ * uniforms from aqsg_sample_seeded's generator); profile_measure_all
+ * (quantum.cpp:467) is the histogram of such draws.  The reference handles one circuit per
+ * QSimulator call; the server keeps a fixed HBM slab and runs many requests
+ * at once:
+ *  - admission: a request is eligible once its arrival time has passed; it
+ *    is admitted when a lane is idle and a 2^n-amplitude block of the slab
+ *    (buddy allocator, power-of-two blocks) is free.  Eligible requests are
+ *    tried in arrival order and a smaller later one may pass a larger one
+ *    that does not fit, unless that one has been passed over 64 times;
+ *  - lanes: each lane owns a CUDA stream and reserved scratch, so a running
+ *    request never allocates and never blocks the host;
+ *  - the register stays in HBM from preparation to sampling; only the op
+ *    tables go up and the outcomes come down. */
+typedef struct aqsg_server_s* aqsg_server;
+
+typedef struct aqsg_server_done {
+    uint64_t ticket;
+    int32_t status;   /* aqsg_status of the request */
+    int32_t n;
+    int32_t lane;
+    int32_t fused_ops; /* ops after fusion (or the lowered op count) */
+    double arrival_s;  /* seconds since aqsg_server_start */
+    double admit_s;
+    double done_s;     /* when the worker saw the outcomes on the host */
+} aqsg_server_done;
+
+typedef struct aqsg_server_stats {
+    uint64_t submitted, completed, failed;
+    uint64_t slab_bytes;       /* HBM held for registers */
+    uint64_t peak_bytes;       /* most slab bytes in use at once */
+    int32_t peak_running;      /* most requests in flight at once */
+    int32_t lanes;
+    uint64_t launches;         /* kernels launched by all lanes */
+} aqsg_server_stats;
+
+/* Create a server on `device` for registers of dtype and at most max_qubits
+ * qubits, holding hbm_budget_bytes of registers (rounded down to a multiple
+ * of the largest register), with `lanes` concurrent requests and at most
+ * max_shots shots per request. */
+int aqsg_server_create(int device, int dtype, uint64_t hbm_budget_bytes, int lanes, int max_qubits,
+                       uint32_t max_shots, aqsg_server* out);
+
+/* Queue a request.  The ops are validated (aqsg_check_ops), lowered, fused
+ * into unitaries of up to fuse_qubits qubits (0 = no fusion) and planned
+ * here, on the caller's thread.  arrival_s is the earliest admission time in
+ * seconds after aqsg_server_start (negative = now).  `outcomes` (shots
+ * values) must stay valid until the request shows up in aqsg_server_poll.
+ * The ops and their matrices may be freed when this returns. */
+int aqsg_server_submit(aqsg_server srv, int n, const aqsg_op* ops, int count, int fuse_qubits,
+                       uint32_t shots, uint64_t seed, double arrival_s, uint64_t* outcomes,
+                       uint64_t* ticket);
+
+/* Start the clock and the worker thread. */
+int aqsg_server_start(aqsg_server srv);
+
+/* Move up to `capacity` finished requests into done[]; *count receives how
+ * many. */
+int aqsg_server_poll(aqsg_server srv, aqsg_server_done* done, int capacity, int* count);
+
+/* Wait until every submitted request has finished (AQSG_ERR_TIMEOUT after
+ * timeout_s seconds). */
+int aqsg_server_wait_idle(aqsg_server srv, double timeout_s);
+
+int aqsg_server_get_stats(aqsg_server srv, aqsg_server_stats* out);
+
+/* Stop the worker and free the slab: requests in flight finish, queued ones
+ * are dropped (they never show up in aqsg_server_poll). */
+int aqsg_server_destroy(aqsg_server srv);
+
 /* ---- measurement ---------------------------------------------------------- */
 
 /* Probability that `qubit` reads |1>, summed in FP64.
