@@ -41,6 +41,7 @@ EXPORTS = [
     "aqsg_batch_info", "aqsg_batch_free",
     "aqsg_server_create", "aqsg_server_submit", "aqsg_server_start", "aqsg_server_poll",
     "aqsg_server_wait_idle", "aqsg_server_get_stats", "aqsg_server_destroy",
+    "aqsg_expect_pauli",
 ]
 
 _lib = None
@@ -112,6 +113,7 @@ def load_library(path: os.PathLike | str | None = None) -> C.CDLL:
         "aqsg_collapse_qubit": ([P, I, D, C.POINTER(I), C.POINTER(D)], I),
         "aqsg_collapse_all": ([P, D, C.POINTER(U64)], I),
         "aqsg_expect_z": ([P, C.POINTER(D), C.POINTER(D)], I),
+        "aqsg_expect_pauli": ([P, C.c_char_p, I, C.POINTER(D)], I),
         "aqsg_sample_noalloc": ([P, C.POINTER(D), U64, I, C.POINTER(U64)], I),
         "aqsg_state_compare": ([P, P] + [C.POINTER(D)] * 5, I),
     }
@@ -422,6 +424,18 @@ class State:
         _check(self.lib.aqsg_expect_z(self.h, z.ctypes.data_as(C.POINTER(C.c_double)),
                                       zz.ctypes.data_as(C.POINTER(C.c_double))))
         return z, zz[: self.n - 1]
+
+    def expect_pauli(self, strings) -> np.ndarray:
+        """<psi|P|psi> (complex128) for each Pauli string (n letters from
+        i/x/y/z, letter j on qubit j)."""
+        strings = list(strings)
+        for s in strings:
+            if len(s) != self.n:
+                raise InvalidArgument(-2, f"Pauli string {s!r} does not have {self.n} letters")
+        out = np.empty(2 * max(len(strings), 1), dtype=np.float64)
+        _check(self.lib.aqsg_expect_pauli(self.h, "".join(strings).encode(), len(strings),
+                                          out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out[0::2][: len(strings)] + 1j * out[1::2][: len(strings)]
 
 
 def check_ops(n: int, ops) -> None:

@@ -64,6 +64,12 @@ void clear_circuit_cache();
 void seed(uint64_t s);
 // The engine context, opened on first use.
 aqsg_ctx engine();
+// Width (qubits) of the dense unitaries QCircuit::compile() folds gate
+// windows into when a circuit is simulated: 1..5, or 0 to apply the compiled
+// gates one by one.  Default 5.  (Extension: the reference folds the whole
+// circuit into one 2^n x 2^n matrix, quantum.cpp:199-210.)
+void set_fusion_qubits(int k);
+int fusion_qubits();
 
 // Throws the reference's exception class for an engine status.
 void throw_status(int rc);
@@ -164,6 +170,11 @@ class QCircuit {
     uint32_t qubits_ = 0;
     std::size_t cached_index_ = 0;
     std::vector<aqsg_op> program_;
+    // program_ fused into <= fused_k_-qubit unitaries (aqsg_compile), built on
+    // the first simulate after a change
+    mutable std::shared_ptr<aqsg_program_s> fused_;
+    mutable std::size_t fused_len_ = 0;
+    mutable int fused_k_ = 0;
     mutable std::vector<std::complex<float>> matrix_;
     mutable bool matrix_valid_ = false;
 };
@@ -209,6 +220,12 @@ class QSimulator {
     std::vector<std::complex<float>> statevector() const;
     // The engine register.
     aqsg_state handle() const noexcept { return sv_; }
+    // <psi|P|psi> for Pauli strings of qubit_count() letters from i/x/y/z,
+    // letter j on qubit j (the strings decompose_hamiltonian returns), summed
+    // in FP64 on the device.  (Extension.)
+    std::vector<std::complex<double>> pauli_expectations(const std::vector<std::string>& paulis) const;
+    // sum_s c_s <psi|P_s|psi> for a decomposed Hamiltonian.  (Extension.)
+    std::complex<double> expectation(const std::vector<std::pair<std::string, cfloat>>& hamiltonian) const;
 
    private:
     std::vector<QState> states_;

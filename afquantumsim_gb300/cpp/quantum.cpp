@@ -19,6 +19,7 @@ std::mutex g_mu;
 aqsg_ctx g_ctx = nullptr;
 int g_device = 0;
 std::mt19937 g_rng{std::random_device{}()};
+int g_fusion = 5;
 std::uniform_real_distribution<float> g_lin{0.0f, 1.0f};
 std::unordered_map<std::string, std::shared_ptr<QCircuit>> g_cache;
 
@@ -84,6 +85,18 @@ aqsg_ctx engine() {
 }
 
 void clear_circuit_cache() { g_cache.clear(); }
+
+void set_fusion_qubits(int k) {
+    if (k < 0 || k > AQSG_MAX_UNITARY_QUBITS)
+        throw std::invalid_argument{"Fusion width must be 0 to 5 qubits"};
+    std::lock_guard<std::mutex> lock(g_mu);
+    g_fusion = k;
+}
+
+int fusion_qubits() {
+    std::lock_guard<std::mutex> lock(g_mu);
+    return g_fusion;
+}
 
 void seed(uint64_t s) {
     std::lock_guard<std::mutex> lock(g_mu);
@@ -174,6 +187,7 @@ void QCircuit::clear() {
 void QCircuit::clear_cache() {
     cached_index_ = 0;
     program_.clear();
+    fused_.reset();
     matrix_valid_ = false;
 }
 
@@ -285,14 +299,27 @@ void QSimulator::generate_statevector() {
     check_call(aqsg_state_set_product(sv_, amps.data()));
 }
 
-// quantum.cpp:277-291: compiled prefix, then the remaining gates in order
+// quantum.cpp:277-291: compiled prefix, then the remaining gates in order.
+// The compiled prefix runs as fused unitaries of fusion_qubits() qubits.
 void QSimulator::simulate(const QCircuit& circuit) {
     if (circuit.qubit_count() != qubits_)
         throw std::invalid_argument{"Number of qubit states and circuit input qubit states do not match"};
-    std::vector<aqsg_op> ops = circuit.program();
+    const auto& prog = circuit.program();
     auto rest = circuit.lower(circuit.cached_index(), circuit.gate_list().size());
-    ops.insert(ops.end(), rest.begin(), rest.end());
-    if (!ops.empty()) check_call(aqsg_apply_ops(sv_, ops.data(), (int)ops.size(), -1));
+    const int k = fusion_qubits();
+    if (k > 0 && !prog.empty()) {
+        if (!circuit.fused_ || circuit.fused_len_ != prog.size() || circuit.fused_k_ != k) {
+            aqsg_program p = nullptr;
+            check_call(aqsg_compile((int)qubits_, AQSG_C64, prog.data(), (int)prog.size(), k, &p));
+            circuit.fused_.reset(p, [](aqsg_program q) { aqsg_program_free(q); });
+            circuit.fused_len_ = prog.size();
+            circuit.fused_k_ = k;
+        }
+        check_call(aqsg_run_program(sv_, circuit.fused_.get(), -1));
+    } else if (!prog.empty()) {
+        check_call(aqsg_apply_ops(sv_, prog.data(), (int)prog.size(), -1));
+    }
+    if (!rest.empty()) check_call(aqsg_apply_ops(sv_, rest.data(), (int)rest.size(), -1));
 }
 
 bool QSimulator::peek_measure(uint32_t qubit) const {
@@ -344,6 +371,32 @@ std::vector<float> QSimulator::probabilities() const {
     std::vector<float> out(state_count());
     check_call(aqsg_probs(sv_, out.data(), 0));
     return out;
+}
+
+std::vector<std::complex<double>> QSimulator::pauli_expectations(const std::vector<std::string>& paulis) const {
+    std::string all;
+    all.reserve(paulis.size() * qubits_);
+    for (const auto& p : paulis) {
+        if (p.size() != qubits_)
+            throw std::invalid_argument{"Pauli string length does not match the qubit count"};
+        all += p;
+    }
+    std::vector<double> raw(2 * paulis.size());
+    if (!paulis.empty()) check_call(aqsg_expect_pauli(sv_, all.data(), (int)paulis.size(), raw.data()));
+    std::vector<std::complex<double>> out(paulis.size());
+    for (std::size_t i = 0; i < out.size(); ++i) out[i] = {raw[2 * i], raw[2 * i + 1]};
+    return out;
+}
+
+std::complex<double> QSimulator::expectation(const std::vector<std::pair<std::string, cfloat>>& hamiltonian) const {
+    std::vector<std::string> strings;
+    strings.reserve(hamiltonian.size());
+    for (const auto& term : hamiltonian) strings.push_back(term.first);
+    const auto vals = pauli_expectations(strings);
+    std::complex<double> e = 0;
+    for (std::size_t i = 0; i < vals.size(); ++i)
+        e += std::complex<double>(hamiltonian[i].second.real, hamiltonian[i].second.imag) * vals[i];
+    return e;
 }
 
 std::vector<std::complex<float>> QSimulator::statevector() const {

@@ -3,9 +3,12 @@
 // Reductions are FP64 and deterministic (fixed two-level trees, no atomics).
 // They replace the ArrayFire reductions of the reference's measurement
 // members (src/quantum.cpp:308-531), which sum in FP32.
+#include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "aqsg_internal.h"
 #include "common.cuh"
@@ -881,3 +884,155 @@ int sample_seeded_async(aqsg_state_s* st, uint64_t seed, uint64_t count, int rul
 }
 
 }  // namespace aqsg
+
+// ---- Pauli-string expectation values -----------------------------------------------
+//
+// P = P_0 (x) ... (x) P_{n-1} with P_j in {I, X, Y, Z} on qubit j (index bit
+// n-1-j).  With Y = i X Z, P = i^{#Y} X^x Z^z where x marks the X/Y qubits and
+// z the Y/Z qubits, so P|k> = i^{#Y} (-1)^{|k & z|} |k ^ x> and
+//   <psi|P|psi> = i^{#Y} sum_k (-1)^{|k & z|} conj(psi[k ^ x]) psi[k].
+// The sums run in FP64, kPauliChunk strings per pass over the register.
+
+namespace aqsg {
+
+constexpr int kPauliChunk = 8;
+constexpr int kPauliThreads = 256;
+
+struct PauliChunk {
+    uint64_t x[kPauliChunk];
+    uint64_t z[kPauliChunk];
+    int count;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kPauliThreads)
+k_pauli_partial(const T* __restrict__ sv, uint64_t N, PauliChunk pc, double* partial) {
+    __shared__ double sh[32];
+    double re[kPauliChunk], im[kPauliChunk];
+#pragma unroll
+    for (int s = 0; s < kPauliChunk; ++s) re[s] = im[s] = 0.0;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < N;
+         k += (uint64_t)gridDim.x * blockDim.x) {
+        const T a = sv[k];
+        const double ar = a.x, ai = a.y;
+#pragma unroll
+        for (int s = 0; s < kPauliChunk; ++s) {
+            if (s < pc.count) {
+                const T b = sv[k ^ pc.x[s]];
+                const double br = b.x, bi = b.y;
+                double pr = br * ar + bi * ai, pi = br * ai - bi * ar;
+                if (__popcll(k & pc.z[s]) & 1) {
+                    pr = -pr;
+                    pi = -pi;
+                }
+                re[s] += pr;
+                im[s] += pi;
+            }
+        }
+    }
+    for (int s = 0; s < kPauliChunk; ++s) {
+        if (s >= pc.count) break;
+        const double r = block_sum(re[s], sh);
+        const double q = block_sum(im[s], sh);
+        if (threadIdx.x == 0) {
+            partial[(uint64_t)blockIdx.x * 2 * kPauliChunk + 2 * s] = r;
+            partial[(uint64_t)blockIdx.x * 2 * kPauliChunk + 2 * s + 1] = q;
+        }
+    }
+}
+
+// out[c] = sum over blocks of partial[b * cols + c]; one warp per column.
+__global__ void k_pauli_final(const double* partial, int blocks, int cols, double* out) {
+    const int c = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (c >= cols) return;
+    double acc = 0;
+    for (int b = l; b < blocks; b += 32) acc += partial[(uint64_t)b * 2 * kPauliChunk + c];
+    acc = warp_sum(acc);
+    if (l == 0) out[c] = acc;
+}
+
+static int pauli_masks(int n, const char* s, uint64_t* x, uint64_t* z, int* ny) {
+    *x = *z = 0;
+    *ny = 0;
+    for (int j = 0; j < n; ++j) {
+        const uint64_t bit = 1ull << (n - 1 - j);
+        switch (s[j]) {
+            case 'i': case 'I': break;
+            case 'x': case 'X': *x |= bit; break;
+            case 'y': case 'Y': *x |= bit; *z |= bit; ++*ny; break;
+            case 'z': case 'Z': *z |= bit; break;
+            default:
+                return set_error(AQSG_ERR_INVALID_ARGUMENT,
+                                 std::string("Pauli strings take the letters i, x, y, z; got '") + s[j] + "'");
+        }
+    }
+    return AQSG_OK;
+}
+
+template <typename T>
+static int expect_pauli_t(aqsg_state_s* st, const char* paulis, int count, double* out) {
+    aqsg_ctx_s* c = st->ctx;
+    const int n = st->n;
+    struct Item {
+        uint64_t x, z;
+        int ny, idx;
+    };
+    std::vector<Item> items(count);
+    for (int s = 0; s < count; ++s) {
+        items[s].idx = s;
+        if (int rc = pauli_masks(n, paulis + (size_t)s * n, &items[s].x, &items[s].z, &items[s].ny)) return rc;
+    }
+    // strings with the same x read the same partner amplitudes: keep them together
+    std::stable_sort(items.begin(), items.end(), [](const Item& a, const Item& b) { return a.x < b.x; });
+    const unsigned grid = stream_grid(st, st->amps, kPauliThreads);
+    const size_t chunk_doubles = (size_t)grid * 2 * kPauliChunk;
+    const int chunks = (count + kPauliChunk - 1) / kPauliChunk;
+    if (int rc = ensure_scratch(c->partial, sizeof(double) * (chunk_doubles + 2 * kPauliChunk * (size_t)chunks)))
+        return rc;
+    double* partial = (double*)c->partial.ptr;
+    double* results = partial + chunk_doubles;
+    for (int ch = 0; ch < chunks; ++ch) {
+        PauliChunk pc;
+        std::memset(&pc, 0, sizeof(pc));
+        pc.count = std::min(kPauliChunk, count - ch * kPauliChunk);
+        for (int s = 0; s < pc.count; ++s) {
+            pc.x[s] = items[ch * kPauliChunk + s].x;
+            pc.z[s] = items[ch * kPauliChunk + s].z;
+        }
+        k_pauli_partial<T><<<grid, kPauliThreads, 0, c->stream>>>((const T*)st->d, st->amps, pc, partial);
+        k_pauli_final<<<1, 32 * 2 * kPauliChunk, 0, c->stream>>>(partial, (int)grid, 2 * pc.count,
+                                                                  results + (size_t)ch * 2 * kPauliChunk);
+        c->launches += 2;
+        AQSG_CUDA_TRY(cudaGetLastError());
+    }
+    std::vector<double> host((size_t)chunks * 2 * kPauliChunk);
+    AQSG_CUDA_TRY(cudaMemcpyAsync(host.data(), results, sizeof(double) * host.size(), cudaMemcpyDeviceToHost,
+                                  c->stream));
+    AQSG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    for (int j = 0; j < count; ++j) {
+        const Item& it = items[j];
+        double r = host[2 * (size_t)j], q = host[2 * (size_t)j + 1];
+        // multiply by i^{ny}
+        for (int t = 0; t < (it.ny & 3); ++t) {
+            const double nr = -q;
+            q = r;
+            r = nr;
+        }
+        out[2 * (size_t)it.idx] = r;
+        out[2 * (size_t)it.idx + 1] = q;
+    }
+    return AQSG_OK;
+}
+
+}  // namespace aqsg
+
+extern "C" int aqsg_expect_pauli(aqsg_state st, const char* paulis, int count, double* out) {
+    using namespace aqsg;
+    if (!st || !st->d) return set_error(AQSG_ERR_NULL, "NULL state");
+    if (count < 0) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Negative string count");
+    if (count == 0) return AQSG_OK;
+    if (!paulis || !out) return set_error(AQSG_ERR_NULL, "NULL argument");
+    AQSG_CUDA_TRY(cudaSetDevice(st->ctx->device));
+    return st->dtype == AQSG_C64 ? expect_pauli_t<float2>(st, paulis, count, out)
+                                 : expect_pauli_t<double2>(st, paulis, count, out);
+}

@@ -52,6 +52,11 @@ def parse_args():
     ap.add_argument("--cpu-sample-ops", type=int, default=8,
                     help="QFT gates in the CPU-baseline sample")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--only", choices=["fused_brickwork", "plain12", "vqe_batch", "serving"],
+                    help="run one secondary workload alone (at --n qubits where it takes a size) "
+                         "and print its JSON; for profiling")
+    ap.add_argument("--depth", type=int, default=20, help="brick-work depth for --only fused_brickwork")
+    ap.add_argument("--count", type=int, default=0, help="circuits for --only vqe_batch / serving")
     return ap.parse_args()
 
 
@@ -642,10 +647,31 @@ def run_reference(args):
     }
 
 
+def run_only(args):
+    import torch
+    import afquantumsim_gb300 as aq
+    ctx = aq.Context(0)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=torch.device("cuda", 0))
+    if args.only == "fused_brickwork":
+        with aq.State(ctx, args.n, aq.C64) as st:
+            res = bench_fused_brickwork(ctx, st, stream, args.n, args.depth)
+    elif args.only == "plain12":
+        res = bench_plain12(ctx, stream)
+    elif args.only == "vqe_batch":
+        res = bench_vqe_batch(ctx, count=args.count or 4096)
+    else:
+        res = bench_serving(ctx, count=args.count or 160)
+    ctx.close()
+    return res
+
+
 def main():
     args = parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if args.only:
+        print(json.dumps(run_only(args)), flush=True)
+        return 0
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         if rank != 0:

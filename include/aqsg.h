@@ -429,6 +429,16 @@ int aqsg_collapse_all(aqsg_state st, double u, uint64_t* outcome);
  * 1 - 2 * qubit_probability_true(q) (quantum.cpp:372-391). */
 int aqsg_expect_z(aqsg_state st, double* z, double* zz);
 
+/* <psi|P|psi> for `count` Pauli strings, summed in FP64: out[2s], out[2s+1]
+ * = real and imaginary part for string s.  `paulis` holds the strings back
+ * to back, n characters each from {i, x, y, z} (either case), character j
+ * acting on qubit j: the strings decompose_hamiltonian returns
+ * (quantum_algo.cpp:131-190).  A Hamiltonian's energy is sum_s c_s out[s];
+ * this replaces the reference's bra-ket product of the state with the
+ * evolved state (quantum_algo.cpp:441-450).  Strings with the same X/Y
+ * pattern share their reads; each pass over the register serves 8 strings. */
+int aqsg_expect_pauli(aqsg_state st, const char* paulis, int count, double* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -212,7 +212,35 @@ static void builder_tests() {
     }
 }
 
+// decompose_hamiltonian / compose_hamiltonian (quantum_algo.cpp:131-231)
+static void hamiltonian_tests() {
+    using cf = std::complex<float>;
+    // Z (x) I on two qubits: letter 0 = qubit 0 = the first Kronecker factor
+    std::vector<cf> zi(16, 0.f);
+    for (int k = 0; k < 4; ++k) zi[k * 4 + k] = (k & 2) ? -1.f : 1.f;
+    auto d = decompose_hamiltonian(zi, 2);
+    CHECK(d.size() == 1 && d[0].first == "zi" && d[0].second == cfloat(1.f, 0.f));
+    // a Hermitian 3-qubit matrix: compose(decompose(H)) == H, strings in code order
+    std::vector<cf> H(64);
+    for (int r = 0; r < 8; ++r)
+        for (int c = 0; c <= r; ++c) {
+            const cf v((float)((r * 7 + c * 3) % 5) - 2.f, r == c ? 0.f : (float)((r + 2 * c) % 3) - 1.f);
+            H[r * 8 + c] = v;
+            H[c * 8 + r] = std::conj(v);
+        }
+    auto desc = decompose_hamiltonian(H, 3);
+    CHECK(!desc.empty());
+    auto back = compose_hamiltonian(desc);
+    double mx = 0;
+    for (int i = 0; i < 64; ++i) mx = std::max(mx, (double)std::abs(back[i] - H[i]));
+    CHECK(mx < 1e-5);
+    for (const auto& t : desc) CHECK(std::abs(t.second.imag) < 1e-6);  // Hermitian: real coefficients
+    CHECK_THROWS((compose_hamiltonian({{"xi", cfloat(1.f, 0.f)}, {"x", cfloat(1.f, 0.f)}})), std::invalid_argument);
+    CHECK_THROWS((decompose_hamiltonian(H, 2)), std::invalid_argument);
+}
+
 int main() {
+    hamiltonian_tests();
     qstate_tests();
     qstate_op_tests();
     representation_tests();

@@ -465,6 +465,31 @@ static void extras() {
     s4.set_basis(QSimulator::Basis::X);
     CHECK(fequal(s4.state_probability(6), 0.125f, 1e-5f));
     CHECK(s4.get_basis() == QSimulator::Basis::X);
+    // compiled circuits run fused (default width 5) or gate by gate (width 0)
+    for (int k : {0, 2, 5}) {
+        set_fusion_qubits(k);
+        QCircuit f = fourier_transform(10);
+        f.compile();
+        QSimulator s5(10, QState::plus());
+        s5.simulate(f);
+        auto z = s5.statevector();
+        float d = 0;
+        for (size_t i = 0; i < x.size(); ++i) d = std::max(d, std::abs(x[i] - z[i]));
+        CHECK(d < 1e-5f);
+    }
+    set_fusion_qubits(5);
+    CHECK_THROWS(set_fusion_qubits(6), std::invalid_argument);
+    // Pauli expectations on a Bell pair; a Hamiltonian's energy
+    QSimulator bell(2);
+    QCircuit bc(2);
+    bc << H(0) << CNot(0, 1);
+    bell.simulate(bc);
+    auto e = bell.pauli_expectations({"zz", "xx", "yy", "zi", "ii"});
+    CHECK(std::abs(e[0] - 1.0) < 1e-6 && std::abs(e[1] - 1.0) < 1e-6 && std::abs(e[2] + 1.0) < 1e-6);
+    CHECK(std::abs(e[3]) < 1e-6 && std::abs(e[4] - 1.0) < 1e-6);
+    auto energy = bell.expectation({{"zz", cfloat(0.5f, 0.f)}, {"xx", cfloat(-2.f, 0.f)}});
+    CHECK(std::abs(energy - std::complex<double>(-1.5, 0.0)) < 1e-6);
+    CHECK_THROWS(bell.pauli_expectations({"zzz"}), std::invalid_argument);
 }
 
 int main(int argc, char** argv) {

@@ -53,19 +53,37 @@ def test_fused_brickwork(gpu_ctx, n, depth):
         assert err < 1e-5 and 1 - fid < 1e-7, (mode, err, fid)
 
 
-def test_tensor_core_unitary_exact_structure(gpu_ctx):
-    """A fused 5-qubit permutation-like unitary through the tensor cores:
-    the split products reproduce entries 0/1 to FP32 accuracy."""
+def test_fused_permutation_unitary_bit_exact(gpu_ctx):
+    """A 5-qubit permutation unitary in a tensor-core-capable tile pass: it
+    runs on the CUDA cores (x * 1 + 0 * y), so it only moves amplitudes."""
     n = 15
     rng = np.random.default_rng(3)
     perm = rng.permutation(32)
     m = np.zeros((32, 32))
     m[perm, np.arange(32)] = 1
     ops = [aq.Unitary([1, 4, 7, 9, 12], m)]
-    v = _kat.random_state(n, 2)
-    want = oracle.apply_f64(v.copy(), ops)
+    v = _kat.random_state(n, 2).astype(np.complex64)
+    want = oracle.apply_f64(v.astype(np.complex128), ops)
     with aq.State(gpu_ctx, n, aq.C64) as st:
-        st.upload(v.astype(np.complex64))
+        st.upload(v)
         st.apply(ops, aq.EXEC_TILED)
         got = st.download()
-    assert np.max(np.abs(got - want)) < 1e-7
+    assert np.array_equal(got.astype(np.complex128), want)
+
+
+@pytest.mark.parametrize("n,k", [(12, 5), (16, 5), (19, 4)])
+def test_fused_permutation_circuit_bit_exact(gpu_ctx, n, k):
+    """Permutation-only circuits (X, CX, CCNot, Swap, CSwap, Or) stay
+    bit-exact when fused: the fused unitaries are permutation matrices."""
+    ops = _kat.random_circuit(n, 200, 40 + n, kinds=["X", "CX", "CCNot", "Swap", "CSwap", "Or"])
+    v = _kat.random_state(n, 5).astype(np.complex64)
+    with aq.State(gpu_ctx, n, aq.C64) as st:
+        st.upload(v)
+        st.apply(ops, aq.EXEC_PER_GATE)
+        want = st.download()
+        prog = aq.Program(n, ops, aq.C64, max_qubits=k)
+        st.upload(v)
+        prog.run(st, aq.EXEC_TILED)
+        got = st.download()
+        prog.free()
+    assert np.array_equal(got, want)
