@@ -105,7 +105,10 @@ struct TilePass {
     int m, L;
     int tbits[16];
     uint32_t first, count;
-    int tc;  // uses the tensor-core kernel
+    int tc;              // uses the tensor-core kernel
+    int matk;            // has dense k-qubit ops run on CUDA cores
+    uint32_t tc_blob;    // pool offset of the pass's tensor-core operands (1 KiB aligned)
+    uint32_t tc_bytes;   // their size: loaded into shared memory once per CTA
 };
 // Encoded passes of an op list: op table (device TileOp records, as bytes)
 // and operand pool (matrices / tensor-core operands) to upload together,
@@ -116,6 +119,7 @@ struct TilePlan {
     std::vector<unsigned char> pool;
     std::vector<TilePass> passes;
     bool any_tc = false;
+    bool any_stream = false;  // a pass runs bounded waits that may set the error flag
     size_t pool_offset() const;
 };
 int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, TilePlan* plan);

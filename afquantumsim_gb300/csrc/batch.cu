@@ -60,8 +60,6 @@ k_batch_small(const SmallItem* __restrict__ items, int count, int* counter, cons
     float2* s = reinterpret_cast<float2*>(smem_raw);
     __shared__ int cur;
     __shared__ double red[32];
-    TcShared tcs;  // no tensor-core ops in this kernel
-    uint32_t phase = 0;
     for (;;) {
         if (threadIdx.x == 0) cur = atomicAdd(counter, 1);
         __syncthreads();
@@ -73,7 +71,8 @@ k_batch_small(const SmallItem* __restrict__ items, int count, int* counter, cons
         const uint32_t size = 1u << n;
         for (uint32_t j = threadIdx.x; j < size; j += blockDim.x) s[j] = make_float2(j == 0 ? 1.f : 0.f, 0.f);
         __syncthreads();
-        tile_run_ops<float, EPT, false>(s, size, 0, ops + it.op_first, it.nops, pool, tcs, phase);
+        tile_run_ops<float, EPT, false, FlatLay>(s, size, blockDim.x, 0, ops + it.op_first, it.nops, pool, nullptr,
+                                                 nullptr);
         double T = 0, S[kZMaxBits], X[kZMaxBits];
 #pragma unroll
         for (int b = 0; b < kZMaxBits; ++b) { S[b] = 0; X[b] = 0; }

@@ -24,7 +24,9 @@ struct TileOp {
 
 struct TileGeom {
     int n, m, L;
-    int tbits[16];  // global bit of each local bit, ascending; tbits[i] = i for i < L
+    int tbits[16];      // global bit of each local bit, ascending; tbits[i] = i for i < L
+    uint32_t tc_blob;   // tensor-core passes: pool offset and size of the operand blob
+    uint32_t tc_bytes;
 };
 
 __device__ __forceinline__ uint32_t ins0(uint32_t p, int b) {
@@ -39,26 +41,28 @@ __device__ __forceinline__ T ld_coef(const double* m, int i) {
     return t;
 }
 
-// ---- tensor-core path (tcgen05) for fused 3..5-qubit unitaries -----------------
-//
-// On a 4096-amplitude c64 tile, a fused unitary U (D x D, D = 2^k) on k tile
-// bits is Y = U X with X the tile viewed as D rows (the target bits) by
-// C = 4096 / D columns (the other bits).  In real form
-//   [Yr; Yi] = [[Ur, -Ui], [Ui, Ur]] [Xr; Xi]
-// and with the data as the M side, D_tmem[c][n] = sum_kk A[c][kk] B[n][kk]
-// where A[c][kk] = Xrf[kk][c] (M = 128 columns per block, K = 2D) and
-// B[n][kk] = Urf[n][kk] (N = 2D).  Both operands are split into BF16 hi + lo
-// parts; D = Ahi Bhi + Ahi Blo + Alo Bhi accumulates in FP32 in tensor memory
-// (the dropped Alo Blo term is ~2^-18 relative).  Operands sit in shared
-// memory in the no-swizzle K-major canonical layout: 8 x 16-byte core
-// matrices, K-direction stride 128 B, M/N-direction stride (K/8) * 128 B.
+// Position of tile element j in shared memory: the identity, or rows of 2^L
+// elements followed by PAD elements of padding.  The streaming passes keep
+// 256-byte rows at a 288-byte stride, so elements of different rows that
+// share their low index bits fall into different shared-memory banks.
+template <int L, int PAD>
+struct TileLay {
+    static __device__ __forceinline__ uint32_t at(uint32_t j) { return PAD ? j + (j >> L) * (uint32_t)PAD : j; }
+};
+using FlatLay = TileLay<0, 0>;
 
-constexpr int kTcTileBits = 12;
-constexpr int kTcThreads = 128;
-constexpr uint32_t kTcTmemCols = 64;            // 2^(12+1) / 128
-constexpr uint32_t kTcABytes = 4u << kTcTileBits;  // one split of A: 2^(m+1) bf16 = 2^(m+2) B
-constexpr uint32_t kTcBBytes = 2u * 64 * 64;       // one split of B at k = 5
-constexpr uint64_t kTcWaitNs = 200000000ull;  // 0.2 s per wait
+// Barrier among the threads that run a tile's ops: the whole CTA, or (in a
+// warp-specialised kernel) the first 512 threads on named barrier 1.
+struct CtaSync {
+    static __device__ __forceinline__ void sync() { __syncthreads(); }
+};
+struct ComputeSync512 {
+    static __device__ __forceinline__ void sync() { asm volatile("bar.sync 1, 512;" ::: "memory"); }
+};
+
+// ---- asynchronous copies and barriers (sm_90+ bulk copies, mbarriers) -----------
+
+constexpr uint64_t kWaitNs = 200000000ull;  // 0.2 s per bounded wait
 
 __device__ __forceinline__ uint64_t globaltimer_ns() {
     uint64_t t;
@@ -69,6 +73,90 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ uint32_t mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+    return ok;
+}
+
+// Wait for the phase of `bar` with the given parity; gives up after kWaitNs
+// of wall time, or early once the device error flag is set.  Returns whether
+// the phase completed.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, const int* err) {
+    const uint64_t t0 = globaltimer_ns();
+    for (uint32_t it = 0;; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 63u) == 63u && (globaltimer_ns() - t0 > kWaitNs || *(volatile const int*)err != 0))
+            return false;
+    }
+}
+
+// global -> shared bulk copy completing on `bar` (bytes: multiple of 16,
+// both addresses 16-byte aligned)
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
+// shared -> global bulk copy in the issuing thread's current bulk group
+__device__ __forceinline__ void bulk_store(void* dst, const void* src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                 ::"l"(dst), "r"(smem_u32(src)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// this thread's bulk stores have finished reading shared memory
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// this thread's bulk stores are complete
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+// order this thread's shared-memory writes before later async-proxy accesses
+__device__ __forceinline__ void fence_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// ---- tensor-core path (tcgen05) for fused 3..5-qubit unitaries -----------------
+//
+// On a 4096-amplitude c64 tile, a fused unitary U (D x D, D = 2^k) on k tile
+// bits is Y = U X with X the tile viewed as D rows (the target bits) by
+// C = 4096 / D columns (the other bits).  In real form, with the complex
+// components interleaved (index 2r = real part of row r, 2r + 1 = imaginary
+// part),
+//   Y[2r]   = sum_c Ur[r][c] X[2c] - Ui[r][c] X[2c+1]
+//   Y[2r+1] = sum_c Ui[r][c] X[2c] + Ur[r][c] X[2c+1].
+// With the data as the M side, D_tmem[col][n] = sum_kk A[col][kk] B[n][kk]
+// where A[col][kk] = X[kk] of data column col (M = 128 columns per block,
+// K = 2D) and B is the real form above (N = 2D).  Both operands are split
+// into BF16 hi + lo parts; D = Ahi Bhi + Ahi Blo + Alo Bhi accumulates in
+// FP32 in tensor memory (the dropped Alo Blo term is ~2^-18 relative).
+// Operands sit in shared memory in the no-swizzle K-major canonical layout:
+// 8 x 16-byte core matrices, K-direction stride 128 B, M/N-direction stride
+// (K/8) * 128 B.  The interleaved K order lets one bf16x2 conversion turn one
+// amplitude into one 4-byte operand word.
+
+constexpr int kTcTileBits = 12;
+constexpr int kTcThreads = 512;                    // 16 warps: 4 per TMEM lane quarter
+constexpr uint32_t kTcTmemCols = 64;               // 2^(12+1) / 128
+constexpr uint32_t kTcABytes = 4u << kTcTileBits;  // one split of A: 16 KiB
+// A pass's tensor-core operands (per op: B hi and lo splits, then the index
+// tables) are loaded into shared memory once per CTA; at most this many bytes.
+constexpr uint32_t kTcBlobMax = 100u * 1024u;
 
 __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
     uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
@@ -97,18 +185,8 @@ __device__ __forceinline__ void tc_commit(uint64_t* bar) {
                  ::"r"(smem_u32(bar)) : "memory");
 }
 
-__device__ __forceinline__ uint32_t mbar_try_wait(uint64_t* bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
-    return ok;
-}
-
-__device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
-    uint32_t r[16];
+// 32 lanes x 16 columns of 32-bit words; the caller waits (tc_ld_wait)
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t* r) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
         "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
@@ -116,17 +194,8 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
           "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
           "=r"(r[14]), "=r"(r[15])
         : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
-
-__device__ __forceinline__ uint16_t bf16_bits(float x) {
-    return __bfloat16_as_ushort(__float2bfloat16_rn(x));
-}
-__device__ __forceinline__ float bf16_val(uint16_t h) {
-    return __uint_as_float((uint32_t)h << 16);
-}
+__device__ __forceinline__ void tc_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // Byte offset of element (row, kk) in a no-swizzle K-major operand with
 // K elements per row.
@@ -134,89 +203,66 @@ __host__ __device__ __forceinline__ uint32_t kmajor_off(uint32_t row, uint32_t k
     return ((row >> 3) * (K >> 3) + (kk >> 3)) * 128u + (row & 7u) * 16u + (kk & 7u) * 2u;
 }
 
-struct TcShared {
-    unsigned char* a;   // A hi, then A lo (kTcABytes each)
-    unsigned char* b;   // B hi, then B lo (kTcBBytes each)
-    uint64_t* bar;
-    uint32_t* tmem;     // allocated tensor-memory address
-    uint32_t* offr;     // per matrix row: local offset of its target-bit pattern
-    int* err;           // device error flag
+struct TcSmem {
+    unsigned char* a;      // A hi, then A lo (kTcABytes each)
+    const unsigned char* blob;  // the pass's operands; an op's B hi at blob + op.mat
+    uint64_t* mma_bar;     // MMAs done
+    uint32_t tmem;         // tensor-memory base address (kTcTmemCols columns)
+    int* err;              // device error flag
+};
+
+struct TcPhase {
+    uint32_t mma = 0;
 };
 
 // One fused unitary on the tile through the tensor cores.  All kTcThreads
-// threads of the CTA call this; returns the next mbarrier phase.
-static __device__ uint32_t tc_apply(float2* s, const TileOp& op, const unsigned char* __restrict__ pool,
-                             const TcShared& t, uint32_t phase) {
+// threads call it.  A bounded wait that gives up sets the error flag (the
+// caller checks it once per tile).
+//
+// The op's blob entry holds B hi, B lo (2 N K bytes each), then colbase[c]
+// (tile index of data column c; 512 x u16) and offr[r] (tile-index bits of
+// matrix row r; 32 x u16).
+template <class LAY, class SYNC>
+__device__ __forceinline__ void tc_apply(float2* s, const TileOp& op, const TcSmem& t, TcPhase& ph) {
     const int k = op.k, D = 1 << k;
     const uint32_t K = 2u * D, N = 2u * D;
-    const uint32_t cols = 1u << (kTcTileBits - k);  // columns of X
-    const uint32_t blocks = cols / 128u;
-    const uint32_t bsplit = 2u * N * K;              // bytes of one B split
-    const int tid = threadIdx.x;
+    const uint32_t blocks = 1u << (kTcTileBits - k - 7);
+    const uint32_t bsplit = 2u * N * K;
+    const uint32_t tid = threadIdx.x;
+    const unsigned char* bsm = t.blob + op.mat;
+    const uint16_t* colbase = reinterpret_cast<const uint16_t*>(bsm + 2u * bsplit);
+    const uint16_t* offr = colbase + 512;
 
-    // B operand (host-prepared hi and lo splits) and the row offset table
-    const uint4* src = reinterpret_cast<const uint4*>(pool + op.mat);
-    uint4* dstb = reinterpret_cast<uint4*>(t.b);
-    for (uint32_t i = tid; i < 2u * bsplit / 16u; i += kTcThreads) {
-        const uint32_t half = i / (bsplit / 16u), w = i % (bsplit / 16u);
-        dstb[half * (kTcBBytes / 16u) + w] = __ldg(src + i);
-    }
-    if (tid < D) {
-        uint32_t off = 0;
-        for (int i = 0; i < k; ++i)
-            if ((tid >> (k - 1 - i)) & 1) off |= 1u << op.ltb[i];
-        t.offr[tid] = off;
-    }
-    uint32_t tmask = 0;
-    for (int i = 0; i < k; ++i) tmask |= 1u << op.ltb[i];
-    __syncthreads();
-
-    // A operand: column c of X -> row c % 128 of block c / 128
-    for (uint32_t c = tid; c < cols; c += kTcThreads) {
-        uint32_t basec = 0, cc = c;  // spread c over the non-target tile bits
-        for (int b = 0; b < kTcTileBits; ++b) {
-            if ((tmask >> b) & 1u) continue;
-            basec |= (cc & 1u) << b;
-            cc >>= 1;
-        }
-        unsigned char* ahi = t.a + (c >> 7) * (128u * K * 2u);
-        unsigned char* alo = ahi + kTcABytes;
+    // A operand: lanes cover 8 data columns x 4 matrix rows, so the 4-byte
+    // operand stores hit 32 different banks
+    const int kd = k - 2;
+#pragma unroll 2
+    for (uint32_t u = tid; u < (1u << kTcTileBits); u += kTcThreads) {
+        const uint32_t lane = u & 31u, rest = u >> 5;
+        const uint32_t c = ((rest >> kd) << 3) | (lane >> 2);
+        const uint32_t r = ((rest & ((1u << kd) - 1u)) << 2) | (lane & 3u);
+        const float2 x = s[LAY::at((uint32_t)colbase[c] | (uint32_t)offr[r])];
+        const __nv_bfloat162 hi = __float22bfloat162_rn(x);
+        const float2 hf = __bfloat1622float2(hi);
+        const __nv_bfloat162 lo = __float22bfloat162_rn(make_float2(x.x - hf.x, x.y - hf.y));
         const uint32_t row = c & 127u;
-        for (uint32_t q = 0; q < K / 8u; ++q) {  // 8 consecutive kk per 16-byte chunk
-            uint32_t hw[4], lw[4];
-#pragma unroll
-            for (int e = 0; e < 8; e += 2) {
-                float x2[2];
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const uint32_t kk = q * 8u + e + h;
-                    const uint32_t r = kk < (uint32_t)D ? kk : kk - D;
-                    const float2 a = s[basec | t.offr[r]];
-                    x2[h] = kk < (uint32_t)D ? a.x : a.y;
-                }
-                const uint16_t h0 = bf16_bits(x2[0]), h1 = bf16_bits(x2[1]);
-                const uint16_t l0 = bf16_bits(x2[0] - bf16_val(h0)), l1 = bf16_bits(x2[1] - bf16_val(h1));
-                hw[e / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
-                lw[e / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
-            }
-            const uint32_t off = kmajor_off(row, q * 8u, K);
-            *reinterpret_cast<uint4*>(ahi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-            *reinterpret_cast<uint4*>(alo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
-        }
+        const uint32_t off = (c >> 7) * (256u * K) + (((row >> 3) * (K >> 3) + (r >> 2)) << 7) +
+                             ((row & 7u) << 4) + ((r & 3u) << 2);
+        *reinterpret_cast<__nv_bfloat162*>(t.a + off) = hi;
+        *reinterpret_cast<__nv_bfloat162*>(t.a + kTcABytes + off) = lo;
     }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
+    fence_async_smem();
+    SYNC::sync();
 
-    const uint32_t tmem = *t.tmem;
     if (tid == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t idesc = tc_idesc(128, N);
         const uint32_t sbo = (K / 8u) * 128u;
         const uint32_t a_hi = smem_u32(t.a), a_lo = a_hi + kTcABytes;
-        const uint32_t b_hi = smem_u32(t.b), b_lo = b_hi + kTcBBytes;
+        const uint32_t b_hi = smem_u32(bsm), b_lo = b_hi + bsplit;
         for (uint32_t blk = 0; blk < blocks; ++blk) {
-            const uint32_t dcol = tmem + blk * N;
-            const uint32_t aoff = blk * (128u * K * 2u);
+            const uint32_t dcol = t.tmem + blk * N;
+            const uint32_t aoff = blk * (256u * K);
             for (uint32_t st = 0; st < K / 16u; ++st) {
                 const uint32_t ko = st * 256u;  // two core matrices along K
                 tc_mma(dcol, tc_desc(a_hi + aoff + ko, 128u, sbo), tc_desc(b_hi + ko, 128u, sbo), idesc,
@@ -225,101 +271,146 @@ static __device__ uint32_t tc_apply(float2* s, const TileOp& op, const unsigned 
                 tc_mma(dcol, tc_desc(a_lo + aoff + ko, 128u, sbo), tc_desc(b_hi + ko, 128u, sbo), idesc, 1u);
             }
         }
-        tc_commit(t.bar);
+        tc_commit(t.mma_bar);
     }
-    // bounded wait for the tensor-core work: at most kTcWaitNs of wall time,
-    // and none once another CTA has given up
-    uint32_t done = 0;
-    const uint64_t t0 = globaltimer_ns();
-    for (long it = 0; !done; ++it) {
-        done = mbar_try_wait(t.bar, phase);
-        if (!done && (it & 63) == 63 &&
-            (globaltimer_ns() - t0 > kTcWaitNs || *(volatile int*)t.err != 0))
-            break;
-    }
-    if (!done && tid == 0) atomicExch(t.err, 1);
+    if (!mbar_wait_bounded(t.mma_bar, ph.mma, t.err)) atomicExch(t.err, 1);
+    ph.mma ^= 1u;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
-    // D back to the tile: warp w reads TMEM lanes 32w..32w+31 = columns
-    const uint32_t warp = tid >> 5, lane_base = warp * 32u;
-    for (uint32_t blk = 0; blk < blocks; ++blk) {
-        const uint32_t c = blk * 128u + lane_base + (tid & 31u);
-        uint32_t basec = 0, cc = c;
-        for (int b = 0; b < kTcTileBits; ++b) {
-            if ((tmask >> b) & 1u) continue;
-            basec |= (cc & 1u) << b;
-            cc >>= 1;
-        }
-        float v[64];
-        for (uint32_t chunk = 0; chunk < N / 16u; ++chunk)
-            tc_ld16(tmem + (lane_base << 16) + blk * N + chunk * 16u, v + chunk * 16u);
-        for (int r = 0; r < D; ++r) s[basec | t.offr[r]] = make_float2(v[r], v[D + r]);
-    }
+    // D straight to the tile: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its
+    // data columns) and the 16 columns 16 (w / 4) .. + 15 (8 output rows)
+    const uint32_t w = tid >> 5, lane = tid & 31u, g = w & 3u, h = w >> 2;
+    uint32_t v[16];
+    tc_ld16(t.tmem + ((g * 32u) << 16) + h * 16u, v);
+    tc_ld_wait();
+    const uint32_t tcol = h * 16u;
+    const uint32_t c = ((tcol >> (k + 1)) << 7) + g * 32u + lane;
+    const uint32_t r0 = (tcol & (N - 1u)) >> 1;
+    const uint32_t cb = colbase[c];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+        s[LAY::at(cb | (uint32_t)offr[r0 + i])] = make_float2(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1]));
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    return phase ^ 1u;
+    SYNC::sync();
+}
+
+// k-qubit dense unitary on CUDA cores: each thread updates one group of 2^K
+// amplitudes, with the group in registers.  Not inlined, so the registers
+// the group needs do not weigh on the passes that never use it.
+template <typename T, int K, class LAY>
+__device__ __noinline__ void matk_apply(T* s, uint32_t size, uint32_t nthr, const TileOp& op,
+                                        const T* __restrict__ mat, uint32_t cm, uint32_t cv) {
+    constexpr int D = 1 << K;
+    int srt[K];
+#pragma unroll
+    for (int i = 0; i < K; ++i) srt[i] = op.ltb[i];
+#pragma unroll
+    for (int i = 1; i < K; ++i)
+#pragma unroll
+        for (int q = i; q > 0; --q)
+            if (srt[q - 1] > srt[q]) {
+                const int x = srt[q];
+                srt[q] = srt[q - 1];
+                srt[q - 1] = x;
+            }
+    uint32_t tb[K];  // tile bit of matrix-row bit K-1-i
+#pragma unroll
+    for (int i = 0; i < K; ++i) tb[i] = 1u << op.ltb[i];
+    auto off_of = [&](int r) {
+        uint32_t off = 0;
+#pragma unroll
+        for (int i = 0; i < K; ++i)
+            if ((r >> (K - 1 - i)) & 1) off |= tb[i];
+        return off;
+    };
+    for (uint32_t p = threadIdx.x; p < (size >> K); p += nthr) {
+        uint32_t j = p;
+#pragma unroll
+        for (int i = 0; i < K; ++i) j = ins0(j, srt[i]);
+        if ((j & cm) != cv) continue;
+        T v[D];
+#pragma unroll
+        for (int r = 0; r < D; ++r) v[r] = s[LAY::at(j | off_of(r))];
+#pragma unroll 1
+        for (int r = 0; r < D; ++r) {
+            T acc;
+            acc.x = 0;
+            acc.y = 0;
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                const T mm = mat[r * D + c];
+                acc.x += mm.x * v[c].x - mm.y * v[c].y;
+                acc.y += mm.x * v[c].y + mm.y * v[c].x;
+            }
+            uint32_t off = 0;
+            for (int i = 0; i < K; ++i)
+                if ((r >> (K - 1 - i)) & 1) off |= tb[i];
+            s[LAY::at(j | off)] = acc;
+        }
+    }
 }
 
 // Apply a pass's ops to the 2^m-amplitude tile s in shared memory (all
-// threads of the CTA call this).  base = the tile's global base index (its
-// bits outside the tile); TC ops use tcs and advance tc_phase.
-template <typename R, int EPT, bool TC>
-__device__ __forceinline__ void tile_run_ops(typename Cx<R>::T* s, uint32_t size, uint64_t base,
+// nthr threads that SYNC covers call this; EPT x nthr >= 2^m).  base = the
+// tile's global base index (its bits outside the tile).  With TC, ops the
+// host marked go through tc_apply (tcs, ph).  Without MATK the kernel has no
+// dense k-qubit path (passes the host knows to be free of them).  A run of
+// consecutive diagonal
+// ops runs from registers: each thread keeps the same EPT elements for the
+// whole run, so the run costs one shared-memory round trip and one barrier.
+template <typename R, int EPT, bool TC, class LAY, class SYNC = CtaSync, bool MATK = true>
+__device__ __forceinline__ void tile_run_ops(typename Cx<R>::T* s, uint32_t size, uint32_t nthr, uint64_t base,
                                              const TileOp* __restrict__ ops, int nops,
-                                             const unsigned char* __restrict__ pool, const TcShared& tcs,
-                                             uint32_t& tc_phase) {
+                                             const unsigned char* __restrict__ pool, const TcSmem* tcs,
+                                             TcPhase* ph) {
     using T = typename Cx<R>::T;
-    const int nthr = blockDim.x;
-    T reg[EPT];
-    bool in_regs = false;
-    for (int oi = 0; oi < nops; ++oi) {
+    for (int oi = 0; oi < nops;) {
         const TileOp& op = ops[oi];
         const int cls = op.cls;
-        if ((base & op.cm_ext) != op.cv_ext) continue;
-        const bool diag = cls == L_DIAG1 || cls == L_DIAG2;
-        if (diag) {
-            if (!in_regs) {
+        if (cls == L_DIAG1 || cls == L_DIAG2) {
+            int oe = oi + 1;
+            while (oe < nops && (ops[oe].cls == L_DIAG1 || ops[oe].cls == L_DIAG2)) ++oe;
+            T reg[EPT];
+#pragma unroll
+            for (int e = 0; e < EPT; ++e) {
+                const uint32_t j = threadIdx.x + e * nthr;
+                if (j < size) reg[e] = s[LAY::at(j)];
+            }
+            for (int q = oi; q < oe; ++q) {
+                const TileOp& d = ops[q];
+                if ((base & d.cm_ext) != d.cv_ext) continue;
+                T ph0 = ld_coef<T>(d.m, 0);
+                const T ph1 = ld_coef<T>(d.m, 1);
+                const int lt = d.lt0;
+                if (d.cls == L_DIAG2 && lt < 0)  // target outside the tile: one phase
+                    ph0 = ((base >> d.ext_t) & 1ull) ? ph1 : ph0;
+                const bool two = d.cls == L_DIAG2 && lt >= 0;
+                const uint32_t cm = (uint32_t)d.cm_loc, cv = (uint32_t)d.cv_loc;
 #pragma unroll
                 for (int e = 0; e < EPT; ++e) {
                     const uint32_t j = threadIdx.x + e * nthr;
-                    if (j < size) reg[e] = s[j];
+                    if (j < size && (j & cm) == cv) reg[e] = cmul((two && ((j >> lt) & 1u)) ? ph1 : ph0, reg[e]);
                 }
-                in_regs = true;
             }
-            T ph0 = ld_coef<T>(op.m, 0), ph1 = ld_coef<T>(op.m, 1);
-            int lt = op.lt0;
-            if (cls == L_DIAG2 && lt < 0) {  // target outside the tile: one phase
-                ph0 = ((base >> op.ext_t) & 1ull) ? ph1 : ph0;
-            }
-            const uint32_t cm = (uint32_t)op.cm_loc, cv = (uint32_t)op.cv_loc;
 #pragma unroll
             for (int e = 0; e < EPT; ++e) {
                 const uint32_t j = threadIdx.x + e * nthr;
-                if (j < size && (j & cm) == cv) {
-                    T ph = ph0;
-                    if (cls == L_DIAG2 && lt >= 0 && ((j >> lt) & 1u)) ph = ph1;
-                    reg[e] = cmul(ph, reg[e]);
-                }
+                if (j < size) s[LAY::at(j)] = reg[e];
             }
+            SYNC::sync();
+            oi = oe;
             continue;
         }
-        if (in_regs) {
-#pragma unroll
-            for (int e = 0; e < EPT; ++e) {
-                const uint32_t j = threadIdx.x + e * nthr;
-                if (j < size) s[j] = reg[e];
-            }
-            in_regs = false;
-            __syncthreads();
-        }
+        ++oi;
+        if ((base & op.cm_ext) != op.cv_ext) continue;
         if constexpr (TC) {
             if (cls == L_MATK && op.pad) {  // tensor-core op (host marks it)
-                tc_phase = tc_apply(reinterpret_cast<float2*>(s), op, pool, tcs, tc_phase);
+                tc_apply<LAY, SYNC>(reinterpret_cast<float2*>(s), op, *tcs, *ph);
                 continue;
             }
         }
         const uint32_t cm = (uint32_t)op.cm_loc, cv = (uint32_t)op.cv_loc;
-        if (cls == L_MAT2 || cls == L_PERM_X || cls == L_PERM_OR || cls == L_DIAG2) {
+        if (cls == L_MAT2 || cls == L_PERM_X || cls == L_PERM_OR) {
             const int lt = op.lt0;
             const uint32_t tb = 1u << lt;
             const T m00 = ld_coef<T>(op.m, 0), m01 = ld_coef<T>(op.m, 1);
@@ -329,13 +420,14 @@ __device__ __forceinline__ void tile_run_ops(typename Cx<R>::T* s, uint32_t size
             for (uint32_t p = threadIdx.x; p < (size >> 1); p += nthr) {
                 const uint32_t j0 = ins0(p, lt);
                 if ((j0 & cm) != cv) continue;
-                const T a = s[j0], b = s[j0 | tb];
+                const uint32_t a0 = LAY::at(j0), a1 = LAY::at(j0 | tb);
+                const T a = s[a0], b = s[a1];
                 if (cls == L_MAT2) {
-                    s[j0] = cmul2(m00, a, m01, b);
-                    s[j0 | tb] = cmul2(m10, a, m11, b);
+                    s[a0] = cmul2(m00, a, m01, b);
+                    s[a1] = cmul2(m10, a, m11, b);
                 } else if (cls == L_PERM_X || or_all || (j0 & am)) {
-                    s[j0] = b;
-                    s[j0 | tb] = a;
+                    s[a0] = b;
+                    s[a1] = a;
                 }
             }
         } else if (cls == L_PERM_SWAP) {
@@ -344,58 +436,22 @@ __device__ __forceinline__ void tile_run_ops(typename Cx<R>::T* s, uint32_t size
             for (uint32_t p = threadIdx.x; p < (size >> 2); p += nthr) {
                 const uint32_t j = ins0(ins0(p, lo), hi) | mb;  // a = 0, b = 1
                 if ((j & cm) != cv) continue;
-                const uint32_t jj = j ^ (ma | mb);
-                const T x = s[j];
-                s[j] = s[jj];
-                s[jj] = x;
+                const uint32_t a0 = LAY::at(j), a1 = LAY::at(j ^ (ma | mb));
+                const T x = s[a0];
+                s[a0] = s[a1];
+                s[a1] = x;
             }
-        } else if (cls == L_MATK) {
-            const int k = op.k, D = 1 << k;
-            int srt[AQSG_MAX_UNITARY_QUBITS];
-            for (int i = 0; i < k; ++i) srt[i] = op.ltb[i];
-            for (int i = 1; i < k; ++i)
-                for (int q = i; q > 0 && srt[q - 1] > srt[q]; --q) {
-                    const int t = srt[q]; srt[q] = srt[q - 1]; srt[q - 1] = t;
-                }
+        } else if (MATK && cls == L_MATK) {
             const T* mat = reinterpret_cast<const T*>(pool + op.mat);
-            for (uint32_t p = threadIdx.x; p < (size >> k); p += nthr) {
-                uint32_t j = p;
-                for (int i = 0; i < k; ++i) j = ins0(j, srt[i]);
-                if ((j & cm) != cv) continue;
-                T v[32];
-                for (int r = 0; r < D; ++r) {
-                    uint32_t off = 0;
-                    for (int i = 0; i < k; ++i)
-                        if ((r >> (k - 1 - i)) & 1) off |= 1u << op.ltb[i];
-                    v[r] = s[j | off];
-                }
-                for (int r = 0; r < D; ++r) {
-                    T acc;
-                    acc.x = 0;
-                    acc.y = 0;
-                    for (int c = 0; c < D; ++c) {
-                        const T mm = mat[r * D + c];
-                        acc.x += mm.x * v[c].x - mm.y * v[c].y;
-                        acc.y += mm.x * v[c].y + mm.y * v[c].x;
-                    }
-                    uint32_t off = 0;
-                    for (int i = 0; i < k; ++i)
-                        if ((r >> (k - 1 - i)) & 1) off |= 1u << op.ltb[i];
-                    s[j | off] = acc;
-                }
+            switch (op.k) {
+                case 2: matk_apply<T, 2, LAY>(s, size, nthr, op, mat, cm, cv); break;
+                case 3: matk_apply<T, 3, LAY>(s, size, nthr, op, mat, cm, cv); break;
+                case 4: matk_apply<T, 4, LAY>(s, size, nthr, op, mat, cm, cv); break;
+                default: matk_apply<T, 5, LAY>(s, size, nthr, op, mat, cm, cv); break;
             }
         }
-        __syncthreads();
+        SYNC::sync();
     }
-    if (in_regs) {
-#pragma unroll
-        for (int e = 0; e < EPT; ++e) {
-            const uint32_t j = threadIdx.x + e * nthr;
-            if (j < size) s[j] = reg[e];
-        }
-    }
-    __syncthreads();
-
 }
 
 }  // namespace aqsg

@@ -15,6 +15,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 
 #include "tile_device.cuh"
 
@@ -24,14 +26,41 @@ int tile_max_bits(int dtype) { return dtype == AQSG_C64 ? 14 : 13; }
 static int stream_tile_bits(int dtype) { return dtype == AQSG_C64 ? 12 : 11; }
 static int row_bits(int dtype) { return dtype == AQSG_C64 ? 5 : 4; }
 
-// EPT: elements per thread in register runs; MAXT/MINB: launch bounds (the
-// whole-register variant runs up to 512 threads in one CTA, the streaming
-// variant 256 threads with several CTAs per SM).  TC: fused unitaries with
-// k >= 3 go through tc_apply (c64, 4096-amplitude tiles, 128 threads).
-template <typename R, int EPT, int MAXT, int MINB, bool TC>
-__global__ void __launch_bounds__(MAXT, MINB)
-k_tile(typename Cx<R>::T* __restrict__ sv, const TileGeom g, const TileOp* __restrict__ ops,
-       int nops, const unsigned char* __restrict__ pool, int* err) {
+// Whole-register passes (n <= 14 c64 / 13 c128): one CTA holds the register.
+// EPT: elements per thread in register runs.
+template <typename R, int EPT>
+__global__ void __launch_bounds__(512, 1)
+k_tile(typename Cx<R>::T* __restrict__ sv, const TileGeom g, const TileOp* __restrict__ ops, int nops,
+       const unsigned char* __restrict__ pool) {
+    using T = typename Cx<R>::T;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    const uint32_t size = 1u << g.m;
+    T* s = reinterpret_cast<T*>(smem_raw);
+    if constexpr (sizeof(R) == 4) {
+        for (uint32_t i = threadIdx.x; i < (size >> 1); i += blockDim.x)
+            reinterpret_cast<float4*>(s)[i] = __ldcs(reinterpret_cast<const float4*>(sv) + i);
+    } else {
+        for (uint32_t j = threadIdx.x; j < size; j += blockDim.x) s[j] = __ldcs(sv + j);
+    }
+    __syncthreads();
+    tile_run_ops<R, EPT, false, FlatLay>(s, size, blockDim.x, 0, ops, nops, pool, nullptr, nullptr);
+    if constexpr (sizeof(R) == 4) {
+        for (uint32_t i = threadIdx.x; i < (size >> 1); i += blockDim.x)
+            __stcs(reinterpret_cast<float4*>(sv) + i, reinterpret_cast<const float4*>(s)[i]);
+    } else {
+        for (uint32_t j = threadIdx.x; j < size; j += blockDim.x) __stcs(sv + j, s[j]);
+    }
+}
+
+// Plain streaming passes (no tensor-core ops): one CTA per tile of 2^m
+// amplitudes (rows of 2^L contiguous amplitudes = 256 B at the row offsets of
+// the pass's high tile bits); several CTAs per SM overlap one another's
+// loads, compute and stores.  MATK: the pass has dense k-qubit ops on CUDA
+// cores (their register groups allow two CTAs per SM instead of three).
+template <typename R, int EPT, bool MATK>
+__global__ void __launch_bounds__(256, MATK ? 2 : 3)
+k_tile_stream(typename Cx<R>::T* __restrict__ sv, const TileGeom g, const TileOp* __restrict__ ops, int nops,
+              const unsigned char* __restrict__ pool) {
     using T = typename Cx<R>::T;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     const int m = g.m, L = g.L;
@@ -39,83 +68,223 @@ k_tile(typename Cx<R>::T* __restrict__ sv, const TileGeom g, const TileOp* __res
     T* s = reinterpret_cast<T*>(smem_raw);
     uint64_t* rowoff = reinterpret_cast<uint64_t*>(smem_raw + sizeof(T) * size);
     const uint32_t rows = 1u << (m - L), rowlen = 1u << L;
-    const int nthr = blockDim.x;
-
-    TcShared tcs;
-    uint32_t tc_phase = 0;
-    if constexpr (TC) {
-        // after the tile (32 KiB) and its row table (<= 1 KiB), 1 KiB aligned
-        unsigned char* p = smem_raw + sizeof(T) * size + 1024;
-        tcs.a = p;
-        tcs.b = p + 2 * kTcABytes;
-        tcs.bar = reinterpret_cast<uint64_t*>(tcs.b + 2 * kTcBBytes);
-        tcs.tmem = reinterpret_cast<uint32_t*>(tcs.bar + 1);
-        tcs.offr = tcs.tmem + 1;
-        tcs.err = err;
-        if (threadIdx.x < 32) {
-            asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                         ::"r"(smem_u32(tcs.tmem)), "r"(kTcTmemCols));
-            asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-        }
-        if (threadIdx.x == 0) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(tcs.bar)), "r"(1));
-            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    }
-
-    // base index of this tile: the block index spread over the non-tile bits
-    uint64_t base = blockIdx.x;
+    uint64_t base = blockIdx.x;  // the block index spread over the non-tile bits
     for (int i = 0; i < m; ++i) {
         const int b = g.tbits[i];
         const uint64_t lo = base & ((1ull << b) - 1ull);
         base = ((base - lo) << 1) | lo;
     }
-    for (uint32_t r = threadIdx.x; r < rows; r += nthr) {
+    for (uint32_t r = threadIdx.x; r < rows; r += blockDim.x) {
         uint64_t off = 0;
         for (int k = 0; k < m - L; ++k)
             if ((r >> k) & 1u) off |= 1ull << g.tbits[L + k];
         rowoff[r] = off;
     }
     __syncthreads();
-
-    // load (128-bit accesses along rows)
     if constexpr (sizeof(R) == 4) {
-        const uint32_t half = size >> 1;
-        for (uint32_t i = threadIdx.x; i < half; i += nthr) {
+        for (uint32_t i = threadIdx.x; i < (size >> 1); i += blockDim.x) {
             const uint32_t j = i << 1;
             const uint64_t gi = base + rowoff[j >> L] + (j & (rowlen - 1));
-            const float4 f = __ldcs(reinterpret_cast<const float4*>(sv) + (gi >> 1));
-            reinterpret_cast<float4*>(s)[i] = f;
+            reinterpret_cast<float4*>(s)[i] = __ldcs(reinterpret_cast<const float4*>(sv) + (gi >> 1));
         }
     } else {
-        for (uint32_t j = threadIdx.x; j < size; j += nthr)
+        for (uint32_t j = threadIdx.x; j < size; j += blockDim.x)
             s[j] = __ldcs(sv + base + rowoff[j >> L] + (j & (rowlen - 1)));
     }
     __syncthreads();
-
-    tile_run_ops<R, EPT, TC>(s, size, base, ops, nops, pool, tcs, tc_phase);
-
-    // store
+    tile_run_ops<R, EPT, false, FlatLay, CtaSync, MATK>(s, size, blockDim.x, base, ops, nops, pool, nullptr, nullptr);
     if constexpr (sizeof(R) == 4) {
-        const uint32_t half = size >> 1;
-        for (uint32_t i = threadIdx.x; i < half; i += nthr) {
+        for (uint32_t i = threadIdx.x; i < (size >> 1); i += blockDim.x) {
             const uint32_t j = i << 1;
             const uint64_t gi = base + rowoff[j >> L] + (j & (rowlen - 1));
             __stcs(reinterpret_cast<float4*>(sv) + (gi >> 1), reinterpret_cast<const float4*>(s)[i]);
         }
     } else {
-        for (uint32_t j = threadIdx.x; j < size; j += nthr)
+        for (uint32_t j = threadIdx.x; j < size; j += blockDim.x)
             __stcs(sv + base + rowoff[j >> L] + (j & (rowlen - 1)), s[j]);
     }
-    if constexpr (TC) {
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-        if (threadIdx.x < 32) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
-                         ::"r"(*tcs.tmem), "r"(kTcTmemCols));
+}
+
+// Streaming passes: a persistent CTA walks the tiles blockIdx.x,
+// blockIdx.x + gridDim.x, ...  A tile is kRows rows of 256 contiguous bytes
+// (the L low index bits); warp 0 moves them with bulk copies into kBufs
+// shared-memory buffers, so the next tiles load and the previous one stores
+// while this one computes.  Every wait is bounded (error flag, early exit).
+constexpr uint32_t kRowBytes = 256;
+constexpr uint32_t kRows = 128;                     // rows of a 2^12-amplitude c64 tile
+constexpr int kTcCta = kTcThreads + 32;             // 16 compute warps + 1 producer warp
+constexpr int kTcMaxOps = 96;                       // op tables up to this size go to shared memory
+static_assert(sizeof(TileOp) % 16 == 0, "op tables are bulk-copied: 16-byte multiples");
+
+// Shared memory of the tensor-core streaming kernel.  Rows are padded by 32
+// bytes (a 288-byte stride) so the operand gathers of rows that share their
+// low index bits spread over the banks.
+struct TcStreamSmem {
+    static constexpr int kBufs = 2;
+    static constexpr uint32_t kRowStride = 288u;
+    static constexpr uint32_t kBufBytes = kRows * kRowStride;          // 36 KiB
+    static constexpr uint32_t kRowOff = kBufs * kBufBytes;              // kRows x u64
+    static constexpr uint32_t kBars = kRowOff + kRows * 8u;             // full[2] done[2] mma blob
+    static constexpr uint32_t kTmemSlot = kBars + 8u * 8u;
+    static constexpr uint32_t kOps = (kTmemSlot + 16u + 127u) & ~127u;  // kTcMaxOps TileOps
+    static constexpr uint32_t kA = (kOps + kTcMaxOps * (uint32_t)sizeof(TileOp) + 1023u) & ~1023u;
+    static constexpr uint32_t kBlob = kA + 2u * kTcABytes;
+    static constexpr uint32_t kBytes = kBlob + kTcBlobMax;
+};
+
+// any(v) over the 512 compute threads (named barrier 1)
+__device__ __forceinline__ bool compute_any(bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, 1, 512, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r) : "r"((uint32_t)v) : "memory");
+    return r != 0;
+}
+
+// Tensor-core streaming passes (c64, 4096-amplitude tiles).  A persistent
+// CTA per SM walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ...; a tile
+// is 128 rows of 256 contiguous bytes (the 5 low index bits) at the row
+// offsets of the pass's 7 high tile bits.  Warp 16 is the producer: it
+// bulk-copies tiles into two shared-memory buffers (full[b] completes when a
+// tile has arrived) and copies them back once the 16 compute warps have
+// released them (done[b]); so the next tile loads and the previous one stores
+// while the compute warps run the pass's ops on the current one.  The pass's
+// operand blob and op table are loaded once per CTA.  Every wait is bounded:
+// one that gives up sets the error flag and the CTA winds down.
+__global__ void __launch_bounds__(kTcCta, 1)
+k_stream_tc(float2* __restrict__ sv, const TileGeom g, const TileOp* __restrict__ ops, int nops,
+            const unsigned char* __restrict__ pool, int* err, uint32_t ntiles) {
+    using SM = TcStreamSmem;
+    constexpr int NB = SM::kBufs;
+    constexpr int L = 5, M = 12;
+    constexpr uint32_t kRowStride = SM::kRowStride, kBufBytes = SM::kBufBytes;
+    using LAY = TileLay<L, (int)((kRowStride - kRowBytes) / sizeof(float2))>;
+    constexpr int EPT = (1 << M) / kTcThreads;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    uint64_t* rowoff = reinterpret_cast<uint64_t*>(smem_raw + SM::kRowOff);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + SM::kBars);
+    uint64_t* done = full + NB;
+    uint64_t* mma_bar = full + 2 * NB;
+    uint64_t* blob_bar = mma_bar + 1;
+    TileOp* sops = reinterpret_cast<TileOp*>(smem_raw + SM::kOps);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+    const bool ops_in_smem = nops <= kTcMaxOps;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"(smem_u32(smem_raw + SM::kTmemSlot)), "r"(kTcTmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        for (int b = 0; b < NB; ++b) {
+            mbar_init(full + b, 1);
+            mbar_init(done + b, kTcThreads / 32);
         }
+        mbar_init(mma_bar, 1);
+        mbar_init(blob_bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (uint32_t r = tid; r < kRows; r += kTcCta) {
+        uint64_t off = 0;
+        for (int q = 0; q < M - L; ++q)
+            if ((r >> q) & 1u) off |= 1ull << g.tbits[L + q];
+        rowoff[r] = off;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+    auto tile_base = [&](uint32_t t) {  // t spread over the non-tile bits
+        uint64_t base = t;
+        for (int i = 0; i < M; ++i) {
+            const int b = g.tbits[i];
+            const uint64_t lo = base & ((1ull << b) - 1ull);
+            base = ((base - lo) << 1) | lo;
+        }
+        return base;
+    };
+    const uint32_t count = blockIdx.x < ntiles ? (ntiles - 1u - blockIdx.x) / gridDim.x + 1u : 0u;
+
+    if (warp == kTcThreads / 32) {
+        // ---- producer warp ----
+        if (lane == 0) {
+            const uint32_t opb = ops_in_smem ? (uint32_t)nops * (uint32_t)sizeof(TileOp) : 0u;
+            mbar_expect_tx(blob_bar, g.tc_bytes + opb);
+            for (uint32_t o = 0; o < g.tc_bytes; o += 32768u) {
+                const uint32_t len = g.tc_bytes - o < 32768u ? g.tc_bytes - o : 32768u;
+                bulk_load(smem_raw + SM::kBlob + o, pool + g.tc_blob + o, len, blob_bar);
+            }
+            if (opb) bulk_load(sops, ops, opb, blob_bar);
+        }
+        auto issue_load = [&](uint32_t i) {
+            const uint32_t buf = i % NB;
+            const uint64_t base = tile_base(blockIdx.x + i * gridDim.x);
+            if (lane == 0) mbar_expect_tx(full + buf, kRows * kRowBytes);
+            __syncwarp();
+            unsigned char* dst = smem_raw + buf * kBufBytes;
+            for (uint32_t r = lane; r < kRows; r += 32u)
+                bulk_load(dst + r * kRowStride, sv + base + rowoff[r], kRowBytes, full + buf);
+        };
+        for (uint32_t q = 0; q < count && q < (uint32_t)NB; ++q) issue_load(q);
+        for (uint32_t i = 0; i < count; ++i) {
+            const uint32_t buf = i % NB;
+            if (!mbar_wait_bounded(done + buf, (i / NB) & 1u, err)) {
+                if (lane == 0) atomicExch(err, 1);
+                break;
+            }
+            const uint64_t base = tile_base(blockIdx.x + i * gridDim.x);
+            const unsigned char* src = smem_raw + buf * kBufBytes;
+            for (uint32_t r = lane; r < kRows; r += 32u)
+                bulk_store(sv + base + rowoff[r], src + r * kRowStride, kRowBytes);
+            bulk_commit();
+            if (i + NB < count) {
+                bulk_wait_read();  // the tile has left the buffer
+                __syncwarp();
+                issue_load(i + NB);
+            }
+        }
+        bulk_wait_all();
+    } else {
+        // ---- compute warps ----
+        TcSmem tcs;
+        TcPhase tph;
+        tcs.a = smem_raw + SM::kA;
+        tcs.blob = smem_raw + SM::kBlob;
+        tcs.mma_bar = mma_bar;
+        tcs.tmem = *reinterpret_cast<volatile uint32_t*>(smem_raw + SM::kTmemSlot);
+        tcs.err = err;
+        const TileOp* optab = ops_in_smem ? sops : ops;
+        bool ok = !compute_any(!mbar_wait_bounded(blob_bar, 0, err));
+        for (uint32_t i = 0; ok && i < count; ++i) {
+            const uint32_t buf = i % NB;
+            if (compute_any(!mbar_wait_bounded(full + buf, (i / NB) & 1u, err))) break;
+            float2* s = reinterpret_cast<float2*>(smem_raw + buf * kBufBytes);
+            const uint64_t base = tile_base(blockIdx.x + i * gridDim.x);
+            tile_run_ops<float, EPT, true, LAY, ComputeSync512>(s, 1u << M, kTcThreads, base, optab, nops, pool,
+                                                               &tcs, &tph);
+            fence_async_smem();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(done + buf);
+            if (compute_any(*(volatile int*)err != 0)) break;
+        }
+        if (!ok || *(volatile int*)err != 0) {
+            if (tid == 0) {
+                atomicExch(err, 1);
+                // the MMAs this CTA issued finish before the tensor memory goes
+                mbar_wait_bounded(mma_bar, tph.mma, err);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(
+                         *reinterpret_cast<volatile uint32_t*>(smem_raw + SM::kTmemSlot)),
+                     "r"(kTcTmemCols));
     }
 }
 
@@ -201,8 +370,11 @@ static float host_bf16_val(uint16_t h) {
     return f;
 }
 
-// B operand of tc_apply for a fused unitary: Urf = [[Ur, -Ui], [Ui, Ur]]
-// (N = K = 2D) split into bf16 hi and lo, no-swizzle K-major layout.
+// B operand of tc_apply for a fused unitary, in the interleaved real form
+// (n = 2r + output part, kk = 2c + input part; part 0 = real, 1 = imaginary):
+//   B[2r][2c] = Ur, B[2r][2c+1] = -Ui, B[2r+1][2c] = Ui, B[2r+1][2c+1] = Ur
+// (N = K = 2D), split into bf16 hi and lo, no-swizzle K-major layout, the lo
+// split right after the hi split.
 static void tc_operand(const std::vector<double>& mk, int k, std::vector<unsigned char>& out) {
     const uint32_t D = 1u << k, K = 2 * D, N = 2 * D;
     const size_t split = 2ull * N * K;
@@ -210,17 +382,21 @@ static void tc_operand(const std::vector<double>& mk, int k, std::vector<unsigne
     out.resize(at + 2 * split, 0);
     for (uint32_t n = 0; n < N; ++n)
         for (uint32_t kk = 0; kk < K; ++kk) {
-            const uint32_t r = n % D, c = kk % D;
+            const uint32_t r = n >> 1, c = kk >> 1;
             const double re = mk[2 * (r * D + c)], im = mk[2 * (r * D + c) + 1];
             double v;
-            if (n < D) v = kk < D ? re : -im;
-            else v = kk < D ? im : re;
+            if ((n & 1u) == 0) v = (kk & 1u) == 0 ? re : -im;
+            else v = (kk & 1u) == 0 ? im : re;
             const uint16_t hi = host_bf16((float)v);
             const uint16_t lo = host_bf16((float)(v - (double)host_bf16_val(hi)));
             const uint32_t off = kmajor_off(n, kk, K);
             std::memcpy(&out[at + off], &hi, 2);
             std::memcpy(&out[at + split + off], &lo, 2);
         }
+}
+
+static void pad_to(std::vector<unsigned char>& v, size_t align) {
+    v.resize((v.size() + align - 1) / align * align, 0);
 }
 
 // A matrix with one non-zero per row, each 1 (a permutation), is applied on
@@ -241,8 +417,44 @@ static bool is_permutation(const std::vector<double>& mk, int k) {
     return true;
 }
 
-static void pad_to(std::vector<unsigned char>& v, size_t align) {
-    v.resize((v.size() + align - 1) / align * align, 0);
+
+// Bytes one tensor-core op takes in its pass's blob: B hi and lo splits
+// (2 x 2N x K each), the data-column table (u16 per column, padded to 1 KiB)
+// and the matrix-row table (32 x u16).
+static size_t tc_op_bytes(int k) {
+    const size_t D = size_t(1) << k;
+    return 2 * (2 * (2 * D) * (2 * D)) + 1024 + 64;
+}
+
+// Index tables of a tensor-core op, appended to the blob after its B splits:
+// colbase[c] = tile index of data column c (c spread over the non-target
+// tile bits, ascending), offr[r] = tile-index bits of matrix row r (qubit
+// ltb[0] is the row's most significant bit).
+static void tc_tables(const TileOp& t, std::vector<unsigned char>& blob) {
+    const int k = t.k;
+    uint32_t tmask = 0;
+    for (int i = 0; i < k; ++i) tmask |= 1u << t.ltb[i];
+    const uint32_t nmask = ((1u << kTcTileBits) - 1u) & ~tmask;
+    const uint32_t cols = 1u << (kTcTileBits - k);
+    const size_t at = blob.size();
+    blob.resize(at + 1024 + 64, 0);
+    for (uint32_t c = 0; c < cols; ++c) {
+        uint32_t x = c, j = 0;
+        for (int b = 0; b < kTcTileBits; ++b)
+            if ((nmask >> b) & 1u) {
+                j |= (x & 1u) << b;
+                x >>= 1;
+            }
+        const uint16_t v = (uint16_t)j;
+        std::memcpy(&blob[at + 2 * c], &v, 2);
+    }
+    for (uint32_t r = 0; r < (1u << k); ++r) {
+        uint32_t off = 0;
+        for (int i = 0; i < k; ++i)
+            if ((r >> (k - 1 - i)) & 1u) off |= 1u << t.ltb[i];
+        const uint16_t v = (uint16_t)off;
+        std::memcpy(&blob[at + 1024 + 2 * r], &v, 2);
+    }
 }
 
 // Encode the passes of `ops` into a table of TileOps and an operand pool.
@@ -251,6 +463,7 @@ int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, Tile
     plan->pool.clear();
     plan->passes.clear();
     plan->any_tc = false;
+    plan->any_stream = false;
     plan->n = n;
     plan->dtype = dtype;
     std::vector<Pass> passes = aqsg::plan(n, dtype, ops);
@@ -267,6 +480,7 @@ int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, Tile
         std::vector<int> local(64, -1);
         for (size_t i = 0; i < p.bits.size(); ++i) local[p.bits[i]] = (int)i;
         const bool tc_pass = tc_on && dtype == AQSG_C64 && tp.m == kTcTileBits;
+        std::vector<unsigned char> blob;  // this pass's tensor-core operands
         for (const LOp* o : p.ops) {
             TileOp t;
             std::memset(&t, 0, sizeof(t));
@@ -285,13 +499,18 @@ int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, Tile
             t.am_ext = o->amask & ~S;
             for (int e = 0; e < 8; ++e) t.m[e] = o->m[e];
             if (o->cls == L_MATK) {
-                pad_to(plan->pool, 256);
-                t.mat = (int32_t)plan->pool.size();
-                if (tc_pass && o->k >= 3 && t.cm_loc == 0 && !is_permutation(o->mk, o->k)) {
-                    t.pad = 1;  // tensor-core op
+                const size_t need = tc_op_bytes(o->k);
+                if (tc_pass && o->k >= 3 && t.cm_loc == 0 && !is_permutation(o->mk, o->k) &&
+                    blob.size() + need <= kTcBlobMax) {
+                    t.pad = 1;  // tensor-core op; mat = offset in the pass's blob
                     tp.tc = 1;
-                    tc_operand(o->mk, o->k, plan->pool);
+                    t.mat = (int32_t)blob.size();
+                    tc_operand(o->mk, o->k, blob);
+                    tc_tables(t, blob);
                 } else {
+                    pad_to(plan->pool, 256);
+                    t.mat = (int32_t)plan->pool.size();
+                    tp.matk = 1;
                     const int D = 1 << o->k;
                     const size_t esz = dtype == AQSG_C64 ? 8 : 16;
                     for (int e = 0; e < D * D; ++e) {
@@ -311,13 +530,49 @@ int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, Tile
             std::memcpy(&plan->table[at], &t, tsize);
         }
         tp.count = (uint32_t)(plan->table.size() / tsize) - tp.first;
+        if (tp.tc) {
+            pad_to(plan->pool, 1024);
+            tp.tc_blob = (uint32_t)plan->pool.size();
+            tp.tc_bytes = (uint32_t)blob.size();
+            plan->pool.insert(plan->pool.end(), blob.begin(), blob.end());
+        }
         plan->any_tc = plan->any_tc || tp.tc;
+        plan->any_stream = plan->any_stream || tp.tc;
         plan->passes.push_back(tp);
     }
     return AQSG_OK;
 }
 
 size_t TilePlan::pool_offset() const { return (table.size() + 255) & ~size_t(255); }
+
+// Resident CTAs per SM of a kernel at a dynamic shared-memory size, and
+// the SM count, per device (queried once).
+struct StreamShape {
+    int sms = 0, per_sm = 0;
+};
+
+template <typename K>
+static int stream_shape(K kernel, int threads, int shm, StreamShape* out) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, StreamShape> cache;
+    int dev = 0;
+    AQSG_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> g(mu);
+    auto key = std::make_pair(dev, (const void*)kernel);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+        *out = it->second;
+        return AQSG_OK;
+    }
+    StreamShape sh;
+    AQSG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+    AQSG_CUDA_TRY(cudaDeviceGetAttribute(&sh.sms, cudaDevAttrMultiProcessorCount, dev));
+    AQSG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sh.per_sm, kernel, threads, shm));
+    if (sh.per_sm < 1) return set_error(AQSG_ERR_RUNTIME, "Streaming tile kernel does not fit on an SM");
+    cache[key] = sh;
+    *out = sh;
+    return AQSG_OK;
+}
 
 template <typename R>
 static int launch_plan_t(void* sv, const TilePlan& plan, const void* dev, cudaStream_t stream, int* d_err,
@@ -327,16 +582,14 @@ static int launch_plan_t(void* sv, const TilePlan& plan, const void* dev, cudaSt
     const TileOp* dops = (const TileOp*)dev;
     const unsigned char* dpool = (const unsigned char*)dev + plan.pool_offset();
     constexpr int EPT_WHOLE = sizeof(R) == 4 ? 32 : 16;  // 2^14 / 512, 2^13 / 512
-    constexpr int EPT_STREAM = sizeof(R) == 4 ? 16 : 8;  // 2^12 / 256, 2^11 / 256
-    auto kwhole = k_tile<R, EPT_WHOLE, 512, 1, false>;
-    auto kstream = k_tile<R, EPT_STREAM, 256, 3, false>;
-    auto ktc = k_tile<float, 32, kTcThreads, 1, true>;
-    const int max_shm = (int)(sizeof(T) << tile_max_bits(plan.dtype)) + 512 * 8;
-    AQSG_CUDA_TRY(cudaFuncSetAttribute(kwhole, cudaFuncAttributeMaxDynamicSharedMemorySize, max_shm));
-    // tile + row table (1 KiB) + A hi/lo + B hi/lo + barrier, tmem slot, row offsets
-    const int tc_shm = (int)((8u << kTcTileBits) + 1024 + 2 * kTcABytes + 2 * kTcBBytes + 256);
-    if (plan.any_tc)
-        AQSG_CUDA_TRY(cudaFuncSetAttribute(ktc, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_shm));
+    constexpr int M_STREAM = sizeof(R) == 4 ? 12 : 11;
+    auto kwhole = k_tile<R, EPT_WHOLE>;
+    auto kplain = k_tile_stream<R, (1 << M_STREAM) / 256, false>;
+    auto kplain_k = k_tile_stream<R, (1 << M_STREAM) / 256, true>;
+    const int whole_shm = (int)(sizeof(T) << tile_max_bits(plan.dtype));
+    AQSG_CUDA_TRY(cudaFuncSetAttribute(kwhole, cudaFuncAttributeMaxDynamicSharedMemorySize, whole_shm));
+    StreamShape tshape;
+    bool have_t = false;
     for (const TilePass& p : plan.passes) {
         TileGeom geo;
         std::memset(&geo, 0, sizeof(geo));
@@ -344,18 +597,30 @@ static int launch_plan_t(void* sv, const TilePlan& plan, const void* dev, cudaSt
         geo.m = p.m;
         geo.L = p.L;
         for (int i = 0; i < p.m; ++i) geo.tbits[i] = p.tbits[i];
+        geo.tc_blob = p.tc_blob;
+        geo.tc_bytes = p.tc_bytes;
         const uint32_t size = 1u << geo.m;
-        const size_t rows = size_t(1) << (geo.m - geo.L);
-        const size_t shm = sizeof(T) * size + rows * sizeof(uint64_t);
-        const unsigned grid = (unsigned)(1ull << (n - geo.m));
-        if (p.tc) {
-            ktc<<<grid, kTcThreads, tc_shm, stream>>>((float2*)sv, geo, dops + p.first, (int)p.count, dpool, d_err);
+        if (p.tc) {  // c64, 12 tile bits (streaming, or the whole 12-qubit register)
+            if (geo.m != kTcTileBits || sizeof(R) != 4)
+                return set_error(AQSG_ERR_RUNTIME, "Tensor-core pass with an unexpected tile shape");
+            if (!have_t) {
+                if (int rc = stream_shape(k_stream_tc, kTcCta, (int)TcStreamSmem::kBytes, &tshape)) return rc;
+                have_t = true;
+            }
+            if (p.tc_bytes > kTcBlobMax) return set_error(AQSG_ERR_RUNTIME, "Tensor-core operands exceed the blob");
+            const uint32_t tiles = 1u << (n - geo.m);
+            const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)(tshape.sms * tshape.per_sm));
+            k_stream_tc<<<grid, kTcCta, TcStreamSmem::kBytes, stream>>>((float2*)sv, geo, dops + p.first,
+                                                                        (int)p.count, dpool, d_err, tiles);
         } else if (geo.m == n) {
             int threads = (int)(size / EPT_WHOLE);
             threads = threads < 32 ? 32 : (threads > 512 ? 512 : threads);
-            kwhole<<<grid, threads, shm, stream>>>((T*)sv, geo, dops + p.first, (int)p.count, dpool, nullptr);
+            kwhole<<<1, threads, sizeof(T) * size, stream>>>((T*)sv, geo, dops + p.first, (int)p.count, dpool);
         } else {
-            kstream<<<grid, 256, shm, stream>>>((T*)sv, geo, dops + p.first, (int)p.count, dpool, nullptr);
+            if (geo.m != M_STREAM) return set_error(AQSG_ERR_RUNTIME, "Streaming pass with an unexpected tile size");
+            const size_t shm = sizeof(T) * size + (size_t(1) << (geo.m - geo.L)) * sizeof(uint64_t);
+            (p.matk ? kplain_k : kplain)<<<(unsigned)(1ull << (n - geo.m)), 256, shm, stream>>>(
+                (T*)sv, geo, dops + p.first, (int)p.count, dpool);
         }
         if (launches) ++*launches;
         AQSG_CUDA_TRY(cudaGetLastError());
@@ -388,15 +653,17 @@ int run_tiled(aqsg_state_s* st, const std::vector<LOp>& ops) {
     if (plan.any_tc)
         if (int rc = reduce_prob(st, 0, 0, &norm_before)) return rc;
     if (int rc = launch_tile_plan(st->d, plan, c->ops.ptr, c->stream, c->d_err, &c->launches)) return rc;
-    if (plan.any_tc) {  // a tensor-core wait that gave up leaves a flag
+    if (plan.any_stream) {  // a bounded wait that gave up leaves a flag
         AQSG_CUDA_TRY(cudaMemcpyAsync(c->host_result, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
         AQSG_CUDA_TRY(cudaStreamSynchronize(c->stream));
         int flag = 0;
         std::memcpy(&flag, c->host_result, sizeof(int));
         if (flag) {
             AQSG_CUDA_TRY(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
-            return set_error(AQSG_ERR_TIMEOUT, "Tensor-core tile pass timed out waiting for its MMAs");
+            return set_error(AQSG_ERR_TIMEOUT, "Tile pass timed out waiting for its copies or MMAs");
         }
+    }
+    if (plan.any_tc) {
         double norm_after = 0;
         if (int rc = reduce_prob(st, 0, 0, &norm_after)) return rc;
         if (norm_after > 0 && norm_before > 0)
