@@ -41,7 +41,7 @@ EXPORTS = [
     "aqsg_batch_info", "aqsg_batch_free",
     "aqsg_server_create", "aqsg_server_submit", "aqsg_server_start", "aqsg_server_poll",
     "aqsg_server_wait_idle", "aqsg_server_get_stats", "aqsg_server_destroy",
-    "aqsg_expect_pauli",
+    "aqsg_expect_pauli", "aqsg_autotune", "aqsg_batch_tuning",
 ]
 
 _lib = None
@@ -525,8 +525,9 @@ def _bind_batch(lib):
     lib.aqsg_batch_run.argtypes = [P, D, D]
     lib.aqsg_batch_info.argtypes = [P, C.POINTER(I), C.POINTER(I), C.POINTER(I)]
     lib.aqsg_batch_free.argtypes = [P]
+    lib.aqsg_batch_tuning.argtypes = [P, C.POINTER(I), C.POINTER(I)]
     for f in ("aqsg_batch_create", "aqsg_batch_update", "aqsg_batch_run", "aqsg_batch_info",
-              "aqsg_batch_free"):
+              "aqsg_batch_free", "aqsg_batch_tuning"):
         getattr(lib, f).restype = I
 
 
@@ -580,7 +581,10 @@ class Batch:
     def info(self):
         s, l, k = C.c_int(), C.c_int(), C.c_int()
         _check(self.lib.aqsg_batch_info(self.h, C.byref(s), C.byref(l), C.byref(k)))
-        return {"small": s.value, "large": l.value, "kernels": k.value}
+        f, t = (C.c_int * max(l.value, 1))(), (C.c_int * max(l.value, 1))()
+        _check(self.lib.aqsg_batch_tuning(self.h, f, t))
+        return {"small": s.value, "large": l.value, "kernels": k.value,
+                "fuse_qubits": list(f[:l.value]), "tensor_cores": list(t[:l.value])}
 
     def free(self) -> None:
         if self.h:
@@ -683,3 +687,32 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+# ---- autotuner -----------------------------------------------------------------
+
+class TuneEntry(C.Structure):
+    """struct aqsg_tune_entry."""
+    _fields_ = [("exec_mode", C.c_int32), ("fuse_qubits", C.c_int32), ("tensor_cores", C.c_int32),
+                ("ops", C.c_int32), ("ms", C.c_double)]
+
+
+def autotune(ctx: Context, n: int, ops, dtype: int = C64, reps: int = 2, all_timings: bool = True):
+    """aqsg_autotune: returns (best, [every timing]) as dicts."""
+    lib = ctx.lib
+    lib.aqsg_autotune.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(Op), C.c_int, C.c_int,
+                                  C.POINTER(TuneEntry), C.POINTER(TuneEntry), C.c_int, C.POINTER(C.c_int)]
+    lib.aqsg_autotune.restype = C.c_int
+    if isinstance(ops, np.ndarray):
+        a = np.ascontiguousarray(ops)
+        ptr, count = C.cast(a.ctypes.data, C.POINTER(Op)), len(a)
+    else:
+        a = ops if isinstance(ops, C.Array) else op_array(list(ops))
+        ptr, count = C.cast(a, C.POINTER(Op)), len(a)
+    best = TuneEntry()
+    buf = (TuneEntry * 16)()
+    k = C.c_int()
+    _check(lib.aqsg_autotune(ctx.h, n, dtype, ptr, count, reps, C.byref(best), buf if all_timings else None,
+                             16, C.byref(k)))
+    conv = lambda e: {f: getattr(e, f) for f, _ in TuneEntry._fields_}
+    return conv(best), [conv(e) for e in buf[:k.value]]

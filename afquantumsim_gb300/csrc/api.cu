@@ -323,6 +323,7 @@ int aqsg_shutdown(aqsg_ctx ctx) {
     if (ctx->host_result) cudaFreeHost(ctx->host_result);
     if (ctx->d_err) cudaFree(ctx->d_err);
     cudaStreamDestroy(ctx->stream);
+    autotune_forget(ctx);
     delete ctx;
     return AQSG_OK;
 }

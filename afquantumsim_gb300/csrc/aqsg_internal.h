@@ -122,7 +122,9 @@ struct TilePlan {
     bool any_stream = false;  // a pass runs bounded waits that may set the error flag
     size_t pool_offset() const;
 };
-int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, TilePlan* plan);
+// exact_perm: fused permutation matrices stay off the tensor cores (bit-exact
+// moves); false makes the choice depend on the op structure only.
+int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, TilePlan* plan, bool exact_perm = true);
 // Launch the passes on `stream`; dev = device copy of table + pool.
 int launch_tile_plan(void* sv, const TilePlan& plan, const void* dev, cudaStream_t stream, int* d_err,
                      uint64_t* launches);
@@ -152,6 +154,11 @@ int sample_seeded_async(aqsg_state_s* st, uint64_t seed, uint64_t count, int rul
 // plan.table followed by plan.pool at plan.pool_offset().  Tensor-core runs
 // renormalise on the device through d_norms[0..1].
 int run_plan_async(aqsg_state_s* st, const TilePlan& plan, const void* dev_table, double* d_norms);
+// aqsg_autotune, optionally without the one-gate-per-pass candidate.
+int autotune_impl(aqsg_ctx ctx, int n, int dtype, const aqsg_op* ops, int count, int reps, bool tiled_only,
+                  aqsg_tune_entry* best, aqsg_tune_entry* all, int capacity, int* count_out);
+// Drop the autotuner's cached choices of a context (it is shutting down).
+void autotune_forget(aqsg_ctx ctx);
 // The fused op list of a compiled program.
 const std::vector<LOp>& program_ops(aqsg_program p);
 

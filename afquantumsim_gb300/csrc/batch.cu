@@ -137,6 +137,8 @@ struct aqsg_batch_s {
     int grid[3] = {0, 0, 0};
     // large registers
     std::vector<int> large;  // circuit indices
+    std::vector<int> fuse;   // per large circuit: tuned fusion width (0 = none)
+    std::vector<int> tc;     // per large circuit: fused unitaries on the tensor cores
     std::vector<TilePlan> plans;
     std::vector<size_t> plan_off;  // offset of each plan's table+pool in d_large
     void* d_large = nullptr;
@@ -173,6 +175,8 @@ static int encode_batch(aqsg_batch_s* b, const aqsg_circuit* cs, bool first_time
     if (first_time) {
         b->large.clear();
         b->plans.clear();
+        b->fuse.clear();
+        b->tc.clear();
     }
     size_t li = 0;
     std::vector<size_t> seen(3, 0);
@@ -180,15 +184,40 @@ static int encode_batch(aqsg_batch_s* b, const aqsg_circuit* cs, bool first_time
         const aqsg_circuit& ci = cs[i];
         if (ci.n != b->n[i]) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Batch structure changed (qubit count)");
         if (int rc = aqsg_check_ops(ci.n, ci.ops, ci.count)) return rc;
+        const int cls = class_of(ci.n);
+        int fuse = 0, tc = 0;
+        if (cls < 0) {
+            // large register: run as the autotuner finds fastest for its
+            // structure (cached per structure, so equal structures tune once
+            // and a circuit runs the same way alone and in any batch)
+            if (first_time) {
+                aqsg_tune_entry best;
+                if (int rc = autotune_impl(b->ctx, ci.n, AQSG_C64, ci.ops, ci.count, 1, true, &best, nullptr, 0,
+                                           nullptr))
+                    return rc;
+                b->fuse.push_back(best.fuse_qubits);
+                b->tc.push_back(best.tensor_cores);
+            }
+            fuse = b->fuse[li];
+            tc = b->tc[li];
+        }
         std::vector<LOp> low;
-        for (int k = 0; k < ci.count; ++k) {
-            LOp o;
-            if (int rc = lower_op(ci.n, AQSG_C64, ci.ops[k], &o)) return rc;
-            if (o.cls != L_NOP) low.push_back(std::move(o));
+        if (fuse > 0) {
+            aqsg_program p = nullptr;
+            if (int rc = aqsg_compile(ci.n, AQSG_C64, ci.ops, ci.count, fuse, &p)) return rc;
+            low = program_ops(p);
+            aqsg_program_free(p);
+        } else {
+            for (int k = 0; k < ci.count; ++k) {
+                LOp o;
+                if (int rc = lower_op(ci.n, AQSG_C64, ci.ops[k], &o)) return rc;
+                if (o.cls != L_NOP) low.push_back(std::move(o));
+            }
         }
         TilePlan plan;
-        if (int rc = encode_tiled(ci.n, AQSG_C64, low, false, &plan)) return rc;
-        const int cls = class_of(ci.n);
+        // the tensor-core choice may not depend on parameter values, so that
+        // an update keeps the captured graph's shape
+        if (int rc = encode_tiled(ci.n, AQSG_C64, low, tc != 0, &plan, false)) return rc;
         if (cls >= 0) {
             // one whole-register pass; append its ops to the class table with
             // their pool offsets shifted to the class pool
@@ -479,10 +508,11 @@ int aqsg_batch_run(aqsg_batch b, double* z, double* zz) {
         const int n = b->n[i];
         const double* r = b->h_out + b->out_off[i];
         const double tot = r[2 * n - 1];
+        const double inv = tot > 0 ? 1.0 / tot : 0.0;  // the register's norm, in FP64
         for (int q = 0; q < n; ++q)
-            if (z) z[zo + q] = tot - 2.0 * r[n - 1 - q];
+            if (z) z[zo + q] = (tot - 2.0 * r[n - 1 - q]) * inv;
         for (int q = 0; q + 1 < n; ++q)
-            if (zz) zz[zzo + q] = tot - 2.0 * r[n + (n - 2 - q)];
+            if (zz) zz[zzo + q] = (tot - 2.0 * r[n + (n - 2 - q)]) * inv;
         zo += n;
         zzo += n - 1;
     }
@@ -494,6 +524,15 @@ int aqsg_batch_info(aqsg_batch b, int* small_circuits, int* large_circuits, int*
     if (small_circuits) *small_circuits = (int)(b->items[0].size() + b->items[1].size() + b->items[2].size());
     if (large_circuits) *large_circuits = (int)b->large.size();
     if (kernels) *kernels = (int)b->kernels;
+    return AQSG_OK;
+}
+
+int aqsg_batch_tuning(aqsg_batch b, int* fuse_qubits, int* tensor_cores) {
+    if (!b) return set_error(AQSG_ERR_NULL, "NULL batch");
+    for (size_t k = 0; k < b->large.size(); ++k) {
+        if (fuse_qubits) fuse_qubits[k] = b->fuse[k];
+        if (tensor_cores) tensor_cores[k] = b->tc[k];
+    }
     return AQSG_OK;
 }
 

@@ -9,7 +9,8 @@
 // Greedy in-order grouping.  A group may absorb the next gate when (1) no
 // later group touches any of the gate's qubits — then moving the gate up to
 // the group only crosses gates it commutes with — and (2) the union of the
-// qubits stays within K.  Each group's unitary is built on the host in FP64
+// qubits stays within K.  Afterwards each group may merge whole into the
+// previous or next group it shares a qubit with, under the same two rules.  Each group's unitary is built on the host in FP64
 // by applying its gates to the 2^k basis vectors.
 #include <algorithm>
 #include <complex>
@@ -153,11 +154,51 @@ static int fuse(int n, const std::vector<LOp>& in, const std::vector<aqsg_op>& s
         for (int b = 0; b < 64; ++b)
             if ((s >> b) & 1ull) last[b] = g;
     }
+    // Merge groups into the previous (else the next) group that shares a
+    // qubit with them when the union stays within K qubits.  The groups in
+    // between share no qubit with the merged one, so they commute with it.
+    // Lone one- and two-qubit groups would otherwise each cost a pass over
+    // the tile; diagonal-only groups are cheap and stay.
+    auto all_diag_of = [&](const Group& g) {
+        for (int oi : g.ops)
+            if (!in[oi].diagonal()) return false;
+        return true;
+    };
+    std::vector<char> gone(groups.size(), 0);
+    for (size_t g = 0; g < groups.size(); ++g) {
+        Group& cur = groups[g];
+        if (all_diag_of(cur) || __builtin_popcountll(cur.bits) > K) continue;
+        int prev = -1, next = -1;
+        for (int q = (int)g - 1; q >= 0; --q)
+            if (!gone[q] && (groups[q].bits & cur.bits)) {
+                prev = q;
+                break;
+            }
+        if (prev >= 0 && __builtin_popcountll(groups[prev].bits | cur.bits) <= K) {
+            groups[prev].bits |= cur.bits;
+            groups[prev].ops.insert(groups[prev].ops.end(), cur.ops.begin(), cur.ops.end());
+            gone[g] = 1;
+            continue;
+        }
+        for (size_t q = g + 1; q < groups.size(); ++q)
+            if (!gone[q] && (groups[q].bits & cur.bits)) {
+                next = (int)q;
+                break;
+            }
+        if (next >= 0 && __builtin_popcountll(groups[next].bits | cur.bits) <= K &&
+            !all_diag_of(groups[next])) {
+            groups[next].bits |= cur.bits;
+            groups[next].ops.insert(groups[next].ops.begin(), cur.ops.begin(), cur.ops.end());
+            gone[g] = 1;
+        }
+    }
     out->clear();
     prog->exported.clear();
     prog->mats.clear();
     prog->mats.reserve(groups.size());
-    for (const Group& gr : groups) {
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+        if (gone[gi]) continue;
+        const Group& gr = groups[gi];
         bool all_diag = true;
         for (int oi : gr.ops) all_diag = all_diag && in[oi].diagonal();
         const int k = __builtin_popcountll(gr.bits);

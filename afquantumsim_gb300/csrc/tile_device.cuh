@@ -368,16 +368,16 @@ __device__ __forceinline__ void tile_run_ops(typename Cx<R>::T* s, uint32_t size
         const TileOp& op = ops[oi];
         const int cls = op.cls;
         if (cls == L_DIAG1 || cls == L_DIAG2) {
-            int oe = oi + 1;
-            while (oe < nops && (ops[oe].cls == L_DIAG1 || ops[oe].cls == L_DIAG2)) ++oe;
             T reg[EPT];
 #pragma unroll
             for (int e = 0; e < EPT; ++e) {
                 const uint32_t j = threadIdx.x + e * nthr;
                 if (j < size) reg[e] = s[LAY::at(j)];
             }
-            for (int q = oi; q < oe; ++q) {
+            int q = oi;
+            for (; q < nops; ++q) {
                 const TileOp& d = ops[q];
+                if (d.cls != L_DIAG1 && d.cls != L_DIAG2) break;
                 if ((base & d.cm_ext) != d.cv_ext) continue;
                 T ph0 = ld_coef<T>(d.m, 0);
                 const T ph1 = ld_coef<T>(d.m, 1);
@@ -398,7 +398,7 @@ __device__ __forceinline__ void tile_run_ops(typename Cx<R>::T* s, uint32_t size
                 if (j < size) s[LAY::at(j)] = reg[e];
             }
             SYNC::sync();
-            oi = oe;
+            oi = q;
             continue;
         }
         ++oi;

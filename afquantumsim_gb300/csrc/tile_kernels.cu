@@ -27,8 +27,9 @@ static int stream_tile_bits(int dtype) { return dtype == AQSG_C64 ? 12 : 11; }
 static int row_bits(int dtype) { return dtype == AQSG_C64 ? 5 : 4; }
 
 // Whole-register passes (n <= 14 c64 / 13 c128): one CTA holds the register.
-// EPT: elements per thread in register runs.
-template <typename R, int EPT>
+// EPT: elements per thread in register runs; MATK: the pass has dense
+// k-qubit ops on CUDA cores.
+template <typename R, int EPT, bool MATK>
 __global__ void __launch_bounds__(512, 1)
 k_tile(typename Cx<R>::T* __restrict__ sv, const TileGeom g, const TileOp* __restrict__ ops, int nops,
        const unsigned char* __restrict__ pool) {
@@ -43,7 +44,7 @@ k_tile(typename Cx<R>::T* __restrict__ sv, const TileGeom g, const TileOp* __res
         for (uint32_t j = threadIdx.x; j < size; j += blockDim.x) s[j] = __ldcs(sv + j);
     }
     __syncthreads();
-    tile_run_ops<R, EPT, false, FlatLay>(s, size, blockDim.x, 0, ops, nops, pool, nullptr, nullptr);
+    tile_run_ops<R, EPT, false, FlatLay, CtaSync, MATK>(s, size, blockDim.x, 0, ops, nops, pool, nullptr, nullptr);
     if constexpr (sizeof(R) == 4) {
         for (uint32_t i = threadIdx.x; i < (size >> 1); i += blockDim.x)
             __stcs(reinterpret_cast<float4*>(sv) + i, reinterpret_cast<const float4*>(s)[i]);
@@ -315,29 +316,58 @@ static std::vector<int> bits_of(uint64_t mask) {
     return v;
 }
 
-// Greedy in-order grouping: a pass takes ops while the union of their target
-// bits (plus the L row bits) fits in m tile bits.
+static uint64_t support_of(const LOp& o) {
+    uint64_t s = o.cmask | o.amask;
+    if (o.t0 >= 0) s |= 1ull << o.t0;
+    if (o.t1 >= 0) s |= 1ull << o.t1;
+    for (int j = 0; j < o.k; ++j) s |= 1ull << o.tb[j];
+    return s;
+}
+
+// Passes with lookahead.  A pass scans the remaining ops in order and takes
+// each op whose target bits still fit in m tile bits (with the L row bits)
+// and that commutes with every op it has passed over: it shares no qubit
+// with them, or it and they are all diagonal.  Taking it moves it before the
+// ops passed over, which is then exact.  The scan gives up kWindow ops after
+// the first one it passed over.
 static std::vector<Pass> plan(int n, int dtype, const std::vector<LOp>& ops) {
     std::vector<Pass> passes;
     const bool whole = n <= tile_max_bits(dtype);
     const int m = whole ? n : stream_tile_bits(dtype);
     const int L = whole ? n : row_bits(dtype);
     const uint64_t rowmask = (L >= 64) ? ~0ull : ((1ull << L) - 1ull);
-    uint64_t S = rowmask;
-    Pass cur;
-    for (const LOp& o : ops) {
-        const uint64_t t = targets_of(o);
-        if ((S | t) != S && __builtin_popcountll(S | t) > m) {
-            passes.push_back(std::move(cur));
-            cur = Pass();
-            S = rowmask | t;
-        } else {
-            S |= t;
+    constexpr size_t kWindow = 1024;
+    std::vector<const LOp*> rest;
+    rest.reserve(ops.size());
+    for (const LOp& o : ops) rest.push_back(&o);
+    std::vector<const LOp*> left;
+    while (!rest.empty()) {
+        Pass cur;
+        uint64_t S = rowmask, blk_any = 0, blk_nondiag = 0;
+        size_t skipped = 0;
+        left.clear();
+        for (size_t i = 0; i < rest.size(); ++i) {
+            const LOp* o = rest[i];
+            if (skipped > kWindow) {
+                left.insert(left.end(), rest.begin() + (long)i, rest.end());
+                break;
+            }
+            const uint64_t sup = support_of(*o), t = targets_of(*o);
+            const bool conflict = (sup & (o->diagonal() ? blk_nondiag : blk_any)) != 0;
+            if (!conflict && __builtin_popcountll(S | t) <= m) {
+                S |= t;
+                cur.ops.push_back(o);
+            } else {
+                left.push_back(o);
+                blk_any |= sup;
+                if (!o->diagonal()) blk_nondiag |= sup;
+                ++skipped;
+            }
         }
-        cur.ops.push_back(&o);
         cur.bits = bits_of(S);
+        passes.push_back(std::move(cur));
+        rest.swap(left);
     }
-    if (!cur.ops.empty()) passes.push_back(std::move(cur));
     // pad each pass's bit set to exactly m bits with the lowest unused bits,
     // so every tile of a pass has the same shape
     for (Pass& p : passes) {
@@ -458,7 +488,7 @@ static void tc_tables(const TileOp& t, std::vector<unsigned char>& blob) {
 }
 
 // Encode the passes of `ops` into a table of TileOps and an operand pool.
-int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, TilePlan* plan) {
+int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, TilePlan* plan, bool exact_perm) {
     plan->table.clear();
     plan->pool.clear();
     plan->passes.clear();
@@ -500,7 +530,7 @@ int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, Tile
             for (int e = 0; e < 8; ++e) t.m[e] = o->m[e];
             if (o->cls == L_MATK) {
                 const size_t need = tc_op_bytes(o->k);
-                if (tc_pass && o->k >= 3 && t.cm_loc == 0 && !is_permutation(o->mk, o->k) &&
+                if (tc_pass && o->k >= 3 && t.cm_loc == 0 && !(exact_perm && is_permutation(o->mk, o->k)) &&
                     blob.size() + need <= kTcBlobMax) {
                     t.pad = 1;  // tensor-core op; mat = offset in the pass's blob
                     tp.tc = 1;
@@ -583,11 +613,13 @@ static int launch_plan_t(void* sv, const TilePlan& plan, const void* dev, cudaSt
     const unsigned char* dpool = (const unsigned char*)dev + plan.pool_offset();
     constexpr int EPT_WHOLE = sizeof(R) == 4 ? 32 : 16;  // 2^14 / 512, 2^13 / 512
     constexpr int M_STREAM = sizeof(R) == 4 ? 12 : 11;
-    auto kwhole = k_tile<R, EPT_WHOLE>;
+    auto kwhole = k_tile<R, EPT_WHOLE, false>;
+    auto kwhole_k = k_tile<R, EPT_WHOLE, true>;
     auto kplain = k_tile_stream<R, (1 << M_STREAM) / 256, false>;
     auto kplain_k = k_tile_stream<R, (1 << M_STREAM) / 256, true>;
     const int whole_shm = (int)(sizeof(T) << tile_max_bits(plan.dtype));
     AQSG_CUDA_TRY(cudaFuncSetAttribute(kwhole, cudaFuncAttributeMaxDynamicSharedMemorySize, whole_shm));
+    AQSG_CUDA_TRY(cudaFuncSetAttribute(kwhole_k, cudaFuncAttributeMaxDynamicSharedMemorySize, whole_shm));
     StreamShape tshape;
     bool have_t = false;
     for (const TilePass& p : plan.passes) {
@@ -615,7 +647,8 @@ static int launch_plan_t(void* sv, const TilePlan& plan, const void* dev, cudaSt
         } else if (geo.m == n) {
             int threads = (int)(size / EPT_WHOLE);
             threads = threads < 32 ? 32 : (threads > 512 ? 512 : threads);
-            kwhole<<<1, threads, sizeof(T) * size, stream>>>((T*)sv, geo, dops + p.first, (int)p.count, dpool);
+            (p.matk ? kwhole_k : kwhole)<<<1, threads, sizeof(T) * size, stream>>>((T*)sv, geo, dops + p.first,
+                                                                               (int)p.count, dpool);
         } else {
             if (geo.m != M_STREAM) return set_error(AQSG_ERR_RUNTIME, "Streaming pass with an unexpected tile size");
             const size_t shm = sizeof(T) * size + (size_t(1) << (geo.m - geo.L)) * sizeof(uint64_t);

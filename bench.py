@@ -222,6 +222,12 @@ def bench_fused_brickwork(ctx, st, stream, n, depth):
     prog.run(st, aq.EXEC_TILED)
     res["fused_tensor_core_ms"] = round(_time_ms(stream, lambda: prog.run(st, aq.EXEC_TILED), 3), 2)
     res["speedup_fused_vs_tiled"] = round(res["tiled_ms"] / res["fused_tensor_core_ms"], 2)
+    # what the autotuner picks for this circuit (all choices timed once)
+    best, every = aq.autotune(ctx, n, ops, aq.C64, reps=1)
+    res["autotune_best"] = {k: best[k] for k in ("exec_mode", "fuse_qubits", "tensor_cores", "ms")}
+    res["autotune_all_ms"] = {f"{'per_gate' if e['exec_mode'] == aq.EXEC_PER_GATE else 'tiled'}"
+                              f"_fuse{e['fuse_qubits']}{'_tc' if e['tensor_cores'] else ''}": round(e["ms"], 2)
+                              for e in every}
     res["speedup_fused_vs_per_gate"] = round(res["per_gate_ms"] / res["fused_tensor_core_ms"], 2)
     # accuracy: fused (tensor cores, c64) vs one gate per pass in c128
     reset()
@@ -334,8 +340,11 @@ def bench_vqe_batch(ctx, count=4096, seed=5):
         err = max(err, float(np.max(np.abs(wz - z[i]))))
     b.free()
     cpu_sweep_est = cpu_s * work / cpu_work
+    from collections import Counter
+    tuned = Counter(f"fuse{f}{'_tc' if t else ''}" for f, t in zip(info["fuse_qubits"], info["tensor_cores"]))
     return {"workload": f"vqe_sweep{count}", "gates": gates, "small_circuits": info["small"],
             "large_circuits": info["large"], "kernels_per_replay": info["kernels"],
+            "large_circuit_tuning": dict(tuned),
             "create_s": round(create_s, 3), "sweep_ms": round(1e3 * sweep_s, 3),
             "circuits_per_s": round(count / sweep_s, 1), "gate_apps_per_s": round(gates / sweep_s, 1),
             "update_and_run_ms": round(1e3 * update_run_s, 3),

@@ -252,6 +252,28 @@ int aqsg_program_export(aqsg_program prog, aqsg_op* out, int capacity, int* coun
 
 int aqsg_program_free(aqsg_program prog);
 
+/* ---- autotuner ------------------------------------------------------------- */
+
+/* One way of running a circuit and its measured time. */
+typedef struct aqsg_tune_entry {
+    int32_t exec_mode;     /* AQSG_EXEC_PER_GATE or AQSG_EXEC_TILED            */
+    int32_t fuse_qubits;   /* 0 = the gates as they are, else aqsg_compile width */
+    int32_t tensor_cores;  /* fused unitaries on the tensor cores (c64)         */
+    int32_t ops;           /* ops after fusion                                  */
+    double ms;             /* device time of one run                           */
+} aqsg_tune_entry;
+
+/* Time the circuit (on a scratch n-qubit register of dtype, from |0...0>)
+ * one gate per pass, in tile passes, and compiled with fusion widths 2..5
+ * with and without the tensor cores; reps timed runs each after one warm-up.
+ * *best receives the fastest.  The choice is cached per context by the
+ * circuit's structure (kinds and operands, not angles or matrix entries):
+ * with all == NULL a cached choice returns at once.  all (capacity entries,
+ * may be NULL) receives every timing, *count_out their number.  The
+ * reference has no counterpart: it runs every circuit one way. */
+int aqsg_autotune(aqsg_ctx ctx, int n, int dtype, const aqsg_op* ops, int count, int reps,
+                  aqsg_tune_entry* best, aqsg_tune_entry* all, int capacity, int* count_out);
+
 /* ---- batched engine (many independent registers) ------------------------ */
 
 /* One circuit of a batch: an n-qubit c64 register, run from |0...0>. */
@@ -264,12 +286,16 @@ typedef struct aqsg_circuit {
 typedef struct aqsg_batch_s* aqsg_batch;
 
 /* Plan a batch of independent circuits of uneven size, each ending in
- * <Z_q> and <Z_q Z_q+1> summed in FP64.  It generalises the reference's VQE
- * cost loop (src/quantum_algo.cpp:412-456: one simulate and one expectation
- * read per parameter set) to a whole sweep.  Registers of up to 14 qubits run
+ * <Z_q> and <Z_q Z_q+1> summed in FP64 (divided by the register's FP64
+ * norm).  It generalises the reference's VQE cost loop
+ * (src/quantum_algo.cpp:412-456: one simulate and one expectation read per
+ * parameter set) to a whole sweep.  Registers of up to 14 qubits run
  * entirely in shared memory (a persistent kernel per size class, one CTA per
  * circuit); larger ones (up to 30) run as tile passes over one reused device
- * register.  The whole run is captured once as a CUDA graph. */
+ * register, each compiled with the fusion width (and tensor-core use) that
+ * the autotuner picks for its structure (tile passes only; cached per
+ * structure, so a circuit runs the same way alone and in any batch).  The
+ * whole run is captured once as a CUDA graph. */
 int aqsg_batch_create(aqsg_ctx ctx, const aqsg_circuit* circuits, int count, aqsg_batch* out);
 
 /* Swap in new parameters (angles, matrices): the same count, qubit counts,
@@ -283,6 +309,11 @@ int aqsg_batch_run(aqsg_batch b, double* z, double* zz);
 
 /* Circuits run in shared memory / as tile passes, kernels per replay. */
 int aqsg_batch_info(aqsg_batch b, int* small_circuits, int* large_circuits, int* kernels);
+
+/* Fusion width (0 = none) and tensor-core use the autotuner chose for each
+ * large register, in circuit order (arrays of large_circuits entries, see
+ * aqsg_batch_info; either may be NULL). */
+int aqsg_batch_tuning(aqsg_batch b, int* fuse_qubits, int* tensor_cores);
 
 int aqsg_batch_free(aqsg_batch b);
 
