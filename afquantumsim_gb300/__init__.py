@@ -41,7 +41,7 @@ EXPORTS = [
     "aqsg_batch_info", "aqsg_batch_free",
     "aqsg_server_create", "aqsg_server_submit", "aqsg_server_start", "aqsg_server_poll",
     "aqsg_server_wait_idle", "aqsg_server_get_stats", "aqsg_server_destroy",
-    "aqsg_expect_pauli", "aqsg_autotune", "aqsg_batch_tuning",
+    "aqsg_expect_pauli", "aqsg_autotune", "aqsg_batch_tuning", "aqsg_selftest_bounded_wait",
 ]
 
 _lib = None
@@ -114,6 +114,7 @@ def load_library(path: os.PathLike | str | None = None) -> C.CDLL:
         "aqsg_collapse_all": ([P, D, C.POINTER(U64)], I),
         "aqsg_expect_z": ([P, C.POINTER(D), C.POINTER(D)], I),
         "aqsg_expect_pauli": ([P, C.c_char_p, I, C.POINTER(D)], I),
+        "aqsg_selftest_bounded_wait": ([P, C.c_uint32, C.POINTER(I)], I),
         "aqsg_sample_noalloc": ([P, C.POINTER(D), U64, I, C.POINTER(U64)], I),
         "aqsg_state_compare": ([P, P] + [C.POINTER(D)] * 5, I),
     }

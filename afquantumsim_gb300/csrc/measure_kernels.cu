@@ -1036,3 +1036,52 @@ extern "C" int aqsg_expect_pauli(aqsg_state st, const char* paulis, int count, d
     return st->dtype == AQSG_C64 ? expect_pauli_t<float2>(st, paulis, count, out)
                                  : expect_pauli_t<double2>(st, paulis, count, out);
 }
+
+// ---- bounded-wait check ------------------------------------------------------------
+//
+// One thread waits on an mbarrier that nothing arrives at, with the same
+// bounded-wait loop the tile kernels use (here with a caller-chosen limit),
+// and reports whether it gave up.  Used to test that a wait that runs out
+// ends with an error status the host reads while the context stays usable.
+
+namespace aqsg {
+
+__global__ void k_wait_selftest(uint64_t limit_ns, int* timed_out) {
+    __shared__ uint64_t bar;
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(&bar);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(1) : "memory");
+    uint64_t t0;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    uint32_t ok = 0;
+    for (uint32_t it = 0;; ++it) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok) : "r"(a), "r"(0u) : "memory");
+        if (ok) break;
+        uint64_t t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        if (t - t0 > limit_ns) break;
+    }
+    *timed_out = ok ? 0 : 1;
+}
+
+}  // namespace aqsg
+
+extern "C" int aqsg_selftest_bounded_wait(aqsg_ctx ctx, uint32_t limit_us, int* timed_out) {
+    using namespace aqsg;
+    if (!ctx || !timed_out) return set_error(AQSG_ERR_NULL, "NULL argument");
+    if (limit_us < 1 || limit_us > 100000) return set_error(AQSG_ERR_OUT_OF_RANGE, "Limit must be 1 us to 0.1 s");
+    AQSG_CUDA_TRY(cudaSetDevice(ctx->device));
+    if (int rc = ensure_scratch(ctx->partial, 64)) return rc;
+    int* d_flag = reinterpret_cast<int*>(ctx->partial.ptr);
+    k_wait_selftest<<<1, 1, 0, ctx->stream>>>((uint64_t)limit_us * 1000ull, d_flag);
+    ctx->launches++;
+    AQSG_CUDA_TRY(cudaGetLastError());
+    int h = -1;
+    AQSG_CUDA_TRY(cudaMemcpyAsync(&h, d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    AQSG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    *timed_out = h;
+    return h == 1 ? set_error(AQSG_ERR_TIMEOUT, "Bounded wait ran out (as intended)") : AQSG_OK;
+}

@@ -391,6 +391,16 @@ int aqsg_server_get_stats(aqsg_server srv, aqsg_server_stats* out);
  * are dropped (they never show up in aqsg_server_poll). */
 int aqsg_server_destroy(aqsg_server srv);
 
+/* ---- failure handling -------------------------------------------------------- */
+
+/* Run one thread waiting on a barrier that nothing releases, with the
+ * bounded-wait loop the tile kernels use and a limit of limit_us
+ * microseconds (1 .. 100000).  *timed_out = 1 when the wait ran out, and the
+ * call then returns AQSG_ERR_TIMEOUT; the context stays usable.  Exists to
+ * test the engine's failure path without a GPU fault; no reference
+ * counterpart. */
+int aqsg_selftest_bounded_wait(aqsg_ctx ctx, uint32_t limit_us, int* timed_out);
+
 /* ---- measurement ---------------------------------------------------------- */
 
 /* Probability that `qubit` reads |1>, summed in FP64.
