@@ -517,7 +517,8 @@ def run_ours(args, rank, world, local_rank):
     roofline = {"bound": "hbm", "kernel": "k_diag1 (CPhase pass)",
                 "achieved": round(cp_achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(cp_achieved / peak, 4), "peak_source": peak_kind,
-                "traffic": TRAFFIC_PER_LAUNCH.get((n, args.dtype)),
+                "traffic": traffic_per_launch(n, args.dtype),
+                "traffic_note": "ncu mean over the CPhase launches of a 26-qubit QFT, scaled by 2^(n-26)",
                 "algorithmic_bytes_per_launch": per_kind["CPhase"],
                 "ms_per_launch": round(cp_ms, 4)}
     kernels = {
@@ -606,9 +607,17 @@ def run_ours(args, rank, world, local_rank):
     }
 
 
-# DRAM bytes (read + write) of one controlled-phase launch from an ncu capture,
-# keyed by (qubits, dtype); see profiles/.
-TRAFFIC_PER_LAUNCH: dict = {}
+# Mean DRAM bytes (read + write) per controlled-phase launch over the 325
+# CPhase launches of one 26-qubit complex64 QFT, from an ncu capture of
+# dram__bytes_read.sum + dram__bytes_write.sum (profiles/k_diag1_qft26_c64_traffic.md).
+# Traffic grows with the register (2^n), so other sizes scale it.
+CPHASE_TRAFFIC_C64_26Q = 277.4e6
+
+
+def traffic_per_launch(n, dtype):
+    if dtype != "c64":
+        return None
+    return round(CPHASE_TRAFFIC_C64_26Q * 2.0 ** (n - 26))
 
 
 def run_reference(args):
