@@ -156,7 +156,7 @@ constexpr uint32_t kTcTmemCols = 64;               // 2^(12+1) / 128
 constexpr uint32_t kTcABytes = 4u << kTcTileBits;  // one split of A: 16 KiB
 // A pass's tensor-core operands (per op: B hi and lo splits, then the index
 // tables) are loaded into shared memory once per CTA; at most this many bytes.
-constexpr uint32_t kTcBlobMax = 100u * 1024u;
+constexpr uint32_t kTcBlobMax = 76u * 1024u;
 
 __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
     uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
@@ -233,14 +233,15 @@ __device__ __forceinline__ void tc_apply(float2* s, const TileOp& op, const TcSm
     const uint16_t* colbase = reinterpret_cast<const uint16_t*>(bsm + 2u * bsplit);
     const uint16_t* offr = colbase + 512;
 
-    // A operand: lanes cover 8 data columns x 4 matrix rows, so the 4-byte
-    // operand stores hit 32 different banks
-    const int kd = k - 2;
+    // A operand: each warp's lanes cover 2^cb data columns x 2^(5-cb) matrix
+    // rows (cb = op.lt1, chosen on the host to spread both the tile reads and
+    // the operand stores over the banks)
+    const int cb = op.lt1, rb = 5 - cb, kd = k - rb;
 #pragma unroll 2
     for (uint32_t u = tid; u < (1u << kTcTileBits); u += kTcThreads) {
         const uint32_t lane = u & 31u, rest = u >> 5;
-        const uint32_t c = ((rest >> kd) << 3) | (lane >> 2);
-        const uint32_t r = ((rest & ((1u << kd) - 1u)) << 2) | (lane & 3u);
+        const uint32_t c = ((rest >> kd) << cb) | (lane >> rb);
+        const uint32_t r = ((rest & ((1u << kd) - 1u)) << rb) | (lane & ((1u << rb) - 1u));
         const float2 x = s[LAY::at((uint32_t)colbase[c] | (uint32_t)offr[r])];
         const __nv_bfloat162 hi = __float22bfloat162_rn(x);
         const float2 hf = __bfloat1622float2(hi);
@@ -286,10 +287,10 @@ __device__ __forceinline__ void tc_apply(float2* s, const TileOp& op, const TcSm
     const uint32_t tcol = h * 16u;
     const uint32_t c = ((tcol >> (k + 1)) << 7) + g * 32u + lane;
     const uint32_t r0 = (tcol & (N - 1u)) >> 1;
-    const uint32_t cb = colbase[c];
+    const uint32_t cbase = colbase[c];
 #pragma unroll
     for (int i = 0; i < 8; ++i)
-        s[LAY::at(cb | (uint32_t)offr[r0 + i])] = make_float2(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1]));
+        s[LAY::at(cbase | (uint32_t)offr[r0 + i])] = make_float2(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1]));
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     SYNC::sync();
 }

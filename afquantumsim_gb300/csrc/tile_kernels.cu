@@ -115,22 +115,25 @@ constexpr uint32_t kRowBytes = 256;
 constexpr uint32_t kRows = 128;                     // rows of a 2^12-amplitude c64 tile
 constexpr int kTcCta = kTcThreads + 32;             // 16 compute warps + 1 producer warp
 constexpr int kTcMaxOps = 96;                       // op tables up to this size go to shared memory
+constexpr uint32_t kTcRowStride = 272u;             // padded tile row in the tensor-core kernel
 static_assert(sizeof(TileOp) % 16 == 0, "op tables are bulk-copied: 16-byte multiples");
 
-// Shared memory of the tensor-core streaming kernel.  Rows are padded by 32
-// bytes (a 288-byte stride) so the operand gathers of rows that share their
+// Shared memory of the tensor-core streaming kernel: three tile buffers (one
+// computing, the next loaded, the previous storing).  Rows are padded by 16
+// bytes (a 272-byte stride) so the operand gathers of rows that share their
 // low index bits spread over the banks.
 struct TcStreamSmem {
-    static constexpr int kBufs = 2;
-    static constexpr uint32_t kRowStride = 288u;
-    static constexpr uint32_t kBufBytes = kRows * kRowStride;          // 36 KiB
+    static constexpr int kBufs = 3;
+    static constexpr uint32_t kRowStride = kTcRowStride;
+    static constexpr uint32_t kBufBytes = kRows * kRowStride;          // 34 KiB
     static constexpr uint32_t kRowOff = kBufs * kBufBytes;              // kRows x u64
-    static constexpr uint32_t kBars = kRowOff + kRows * 8u;             // full[2] done[2] mma blob
-    static constexpr uint32_t kTmemSlot = kBars + 8u * 8u;
+    static constexpr uint32_t kBars = kRowOff + kRows * 8u;             // full[3] done[3] mma blob
+    static constexpr uint32_t kTmemSlot = kBars + 16u * 8u;
     static constexpr uint32_t kOps = (kTmemSlot + 16u + 127u) & ~127u;  // kTcMaxOps TileOps
     static constexpr uint32_t kA = (kOps + kTcMaxOps * (uint32_t)sizeof(TileOp) + 1023u) & ~1023u;
     static constexpr uint32_t kBlob = kA + 2u * kTcABytes;
     static constexpr uint32_t kBytes = kBlob + kTcBlobMax;
+    static_assert(kBytes <= 232448u, "more shared memory than a CTA may have");
 };
 
 // any(v) over the 512 compute threads (named barrier 1)
@@ -269,7 +272,7 @@ k_stream_tc(float2* __restrict__ sv, const TileGeom g, const TileOp* __restrict_
             fence_async_smem();
             __syncwarp();
             if (lane == 0) mbar_arrive(done + buf);
-            if (compute_any(*(volatile int*)err != 0)) break;
+            if (compute_any(tid == 0 && *(volatile int*)err != 0)) break;
         }
         if (!ok || *(volatile int*)err != 0) {
             if (tid == 0) {
@@ -330,7 +333,12 @@ static uint64_t support_of(const LOp& o) {
 // with them, or it and they are all diagonal.  Taking it moves it before the
 // ops passed over, which is then exact.  The scan gives up kWindow ops after
 // the first one it passed over.
-static std::vector<Pass> plan(int n, int dtype, const std::vector<LOp>& ops) {
+static size_t tc_op_bytes(int k);
+
+// tc_budget: tensor-core passes (c64): a pass also stops taking fused
+// unitaries of 3+ qubits once their operands would exceed the shared-memory
+// blob of the kernel.
+static std::vector<Pass> plan(int n, int dtype, const std::vector<LOp>& ops, bool tc_budget) {
     std::vector<Pass> passes;
     const bool whole = n <= tile_max_bits(dtype);
     const int m = whole ? n : stream_tile_bits(dtype);
@@ -344,7 +352,7 @@ static std::vector<Pass> plan(int n, int dtype, const std::vector<LOp>& ops) {
     while (!rest.empty()) {
         Pass cur;
         uint64_t S = rowmask, blk_any = 0, blk_nondiag = 0;
-        size_t skipped = 0;
+        size_t skipped = 0, blob = 0;
         left.clear();
         for (size_t i = 0; i < rest.size(); ++i) {
             const LOp* o = rest[i];
@@ -354,8 +362,10 @@ static std::vector<Pass> plan(int n, int dtype, const std::vector<LOp>& ops) {
             }
             const uint64_t sup = support_of(*o), t = targets_of(*o);
             const bool conflict = (sup & (o->diagonal() ? blk_nondiag : blk_any)) != 0;
-            if (!conflict && __builtin_popcountll(S | t) <= m) {
+            const size_t ob = (tc_budget && !whole && o->cls == L_MATK && o->k >= 3) ? tc_op_bytes(o->k) : 0;
+            if (!conflict && __builtin_popcountll(S | t) <= m && blob + ob <= kTcBlobMax) {
                 S |= t;
+                blob += ob;
                 cur.ops.push_back(o);
             } else {
                 left.push_back(o);
@@ -459,15 +469,18 @@ static size_t tc_op_bytes(int k) {
 // Index tables of a tensor-core op, appended to the blob after its B splits:
 // colbase[c] = tile index of data column c (c spread over the non-target
 // tile bits, ascending), offr[r] = tile-index bits of matrix row r (qubit
-// ltb[0] is the row's most significant bit).
-static void tc_tables(const TileOp& t, std::vector<unsigned char>& blob) {
+// ltb[0] is the row's most significant bit).  Also picks the op's lane split
+// for the operand gather (t.lt1 = lane bits on data columns, the rest on
+// matrix rows): the split whose first warps touch the fewest shared-memory
+// wavefronts, reading the padded tile (row stride kTcRowStride bytes) and
+// writing the 4-byte operand words.
+static void tc_tables(TileOp& t, std::vector<unsigned char>& blob) {
     const int k = t.k;
     uint32_t tmask = 0;
     for (int i = 0; i < k; ++i) tmask |= 1u << t.ltb[i];
     const uint32_t nmask = ((1u << kTcTileBits) - 1u) & ~tmask;
     const uint32_t cols = 1u << (kTcTileBits - k);
-    const size_t at = blob.size();
-    blob.resize(at + 1024 + 64, 0);
+    std::vector<uint32_t> colbase(cols), offr(1u << k);
     for (uint32_t c = 0; c < cols; ++c) {
         uint32_t x = c, j = 0;
         for (int b = 0; b < kTcTileBits; ++b)
@@ -475,16 +488,49 @@ static void tc_tables(const TileOp& t, std::vector<unsigned char>& blob) {
                 j |= (x & 1u) << b;
                 x >>= 1;
             }
-        const uint16_t v = (uint16_t)j;
-        std::memcpy(&blob[at + 2 * c], &v, 2);
+        colbase[c] = j;
     }
     for (uint32_t r = 0; r < (1u << k); ++r) {
         uint32_t off = 0;
         for (int i = 0; i < k; ++i)
             if ((r >> (k - 1 - i)) & 1u) off |= 1u << t.ltb[i];
-        const uint16_t v = (uint16_t)off;
+        offr[r] = off;
+    }
+    const size_t at = blob.size();
+    blob.resize(at + 1024 + 64, 0);
+    for (uint32_t c = 0; c < cols; ++c) {
+        const uint16_t v = (uint16_t)colbase[c];
+        std::memcpy(&blob[at + 2 * c], &v, 2);
+    }
+    for (uint32_t r = 0; r < (1u << k); ++r) {
+        const uint16_t v = (uint16_t)offr[r];
         std::memcpy(&blob[at + 1024 + 2 * r], &v, 2);
     }
+    // lane split: cb column bits, 5 - cb row bits (5 - cb <= k)
+    const uint32_t pad = (kTcRowStride - 256u) / 8u;  // float2 elements of padding per row
+    int best_cb = 3, best_cost = 1 << 30;
+    for (int cb = 2; cb <= 4; ++cb) {
+        const int rb = 5 - cb;
+        if (rb > k) continue;
+        int cost = 0;
+        for (uint32_t w = 0; w < 4; ++w) {
+            int rd[16] = {0}, wr[32] = {0};
+            for (uint32_t lane = 0; lane < 32; ++lane) {
+                const uint32_t u = w * 32 + lane, rest = u >> 5;
+                const uint32_t c = ((rest >> (k - rb)) << cb) | (lane >> rb);
+                const uint32_t r = ((rest & ((1u << (k - rb)) - 1u)) << rb) | (lane & ((1u << rb) - 1u));
+                const uint32_t j = colbase[c % cols] | offr[r];
+                ++rd[(j + (j >> 5) * pad) & 15u];
+                ++wr[(((c & 127u) & 7u) * 4u + (r & 3u)) & 31u];
+            }
+            cost += *std::max_element(rd, rd + 16) + 2 * *std::max_element(wr, wr + 32);
+        }
+        if (cost < best_cost) {
+            best_cost = cost;
+            best_cb = cb;
+        }
+    }
+    t.lt1 = best_cb;
 }
 
 // Encode the passes of `ops` into a table of TileOps and an operand pool.
@@ -496,7 +542,7 @@ int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, Tile
     plan->any_stream = false;
     plan->n = n;
     plan->dtype = dtype;
-    std::vector<Pass> passes = aqsg::plan(n, dtype, ops);
+    std::vector<Pass> passes = aqsg::plan(n, dtype, ops, tc_on && dtype == AQSG_C64);
     const size_t tsize = sizeof(TileOp);
     for (const Pass& p : passes) {
         TilePass tp;
