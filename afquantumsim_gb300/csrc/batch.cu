@@ -52,7 +52,7 @@ __device__ __forceinline__ double block_sum_b(double v, double* sh) {
 // Raw results per circuit, 2n doubles: S[b] = sum p over indices with bit b
 // set (b < n), X[b] = sum p over indices whose bits b and b+1 differ
 // (b < n-1), then the total T.  <Z_q> = T - 2 S[n-1-q].
-template <int EPT, int MAXT>
+template <int EPT, int MAXT, bool MATK>
 __global__ void __launch_bounds__(MAXT, 1)
 k_batch_small(const SmallItem* __restrict__ items, int count, int* counter, const TileOp* __restrict__ ops,
               const unsigned char* __restrict__ pool, double* __restrict__ out) {
@@ -71,20 +71,26 @@ k_batch_small(const SmallItem* __restrict__ items, int count, int* counter, cons
         const uint32_t size = 1u << n;
         for (uint32_t j = threadIdx.x; j < size; j += blockDim.x) s[j] = make_float2(j == 0 ? 1.f : 0.f, 0.f);
         __syncthreads();
-        tile_run_ops<float, EPT, false, FlatLay>(s, size, blockDim.x, 0, ops + it.op_first, it.nops, pool, nullptr,
-                                                 nullptr);
-        double T = 0, S[kZMaxBits], X[kZMaxBits];
-#pragma unroll
-        for (int b = 0; b < kZMaxBits; ++b) { S[b] = 0; X[b] = 0; }
+        tile_run_ops<float, EPT, false, FlatLay, CtaSync, MATK>(s, size, blockDim.x, 0, ops + it.op_first, it.nops,
+                                                                pool, nullptr, nullptr);
+        // exact |a|^2 and compensated sums on the FP32 pipe, FP64 across threads
+        FAcc fT, fS[kZMaxBits], fX[kZMaxBits];
         for (uint32_t j = threadIdx.x; j < size; j += blockDim.x) {
             const float2 a = s[j];
-            const double p = (double)a.x * a.x + (double)a.y * a.y;
-            T += p;
+            float h, l;
+            norm2_ff(a.x, a.y, h, l);
+            fT.add(h, l);
 #pragma unroll
             for (int b = 0; b < kZMaxBits; ++b) {
-                if (b < n && ((j >> b) & 1u)) S[b] += p;
-                if (b + 1 < n && (((j >> b) ^ (j >> (b + 1))) & 1u)) X[b] += p;
+                if (b < n && ((j >> b) & 1u)) fS[b].add(h, l);
+                if (b + 1 < n && (((j >> b) ^ (j >> (b + 1))) & 1u)) fX[b].add(h, l);
             }
+        }
+        double T = fT.value(), S[kZMaxBits], X[kZMaxBits];
+#pragma unroll
+        for (int b = 0; b < kZMaxBits; ++b) {
+            S[b] = fS[b].value();
+            X[b] = fX[b].value();
         }
         double* o = out + it.out;
 #pragma unroll
@@ -112,6 +118,26 @@ struct SmallClass {
 };
 static const SmallClass kClasses[3] = {{10, 128}, {12, 256}, {14, 512}};
 
+// The kernel of a size class, with or without the dense k-qubit op path (a
+// class whose circuits have none runs the lighter variant).
+struct SmallKernel {
+    void (*fn)(const SmallItem*, int, int*, const TileOp*, const unsigned char*, double*);
+    int threads;
+    void launch(int grid, size_t shm, cudaStream_t st, const SmallItem* items, int cnt, int* counter,
+                const TileOp* ops, const unsigned char* pool, double* out) const {
+        void* args[] = {(void*)&items, (void*)&cnt, (void*)&counter, (void*)&ops, (void*)&pool, (void*)&out};
+        cudaLaunchKernel((const void*)fn, dim3(grid), dim3(threads), args, shm, st);
+    }
+};
+
+static SmallKernel small_kernel(int c, bool matk) {
+    switch (c) {
+        case 0: return {matk ? k_batch_small<8, 128, true> : k_batch_small<8, 128, false>, 128};
+        case 1: return {matk ? k_batch_small<16, 256, true> : k_batch_small<16, 256, false>, 256};
+        default: return {matk ? k_batch_small<32, 512, true> : k_batch_small<32, 512, false>, 512};
+    }
+}
+
 static int class_of(int n) {
     for (int c = 0; c < 3; ++c)
         if (n <= kClasses[c].max_n) return c;
@@ -135,6 +161,7 @@ struct aqsg_batch_s {
     void* d_small_items[3] = {nullptr, nullptr, nullptr};
     void* d_small_ops[3] = {nullptr, nullptr, nullptr};
     int grid[3] = {0, 0, 0};
+    bool class_matk[3] = {false, false, false};  // a class has dense k-qubit ops
     // large registers
     std::vector<int> large;  // circuit indices
     std::vector<int> fuse;   // per large circuit: tuned fusion width (0 = none)
@@ -229,7 +256,10 @@ static int encode_batch(aqsg_batch_s* b, const aqsg_circuit* cs, bool first_time
             for (size_t at = 0; at < plan.table.size(); at += tsz) {
                 TileOp t;
                 std::memcpy(&t, &plan.table[at], tsz);
-                if (t.cls == L_MATK) t.mat += (int32_t)pbase;
+                if (t.cls == L_MATK) {
+                    t.mat += (int32_t)pbase;
+                    if (first_time) b->class_matk[cls] = true;
+                }
                 const size_t w = b->small_table[cls].size();
                 b->small_table[cls].resize(w + tsz);
                 std::memcpy(&b->small_table[cls][w], &t, tsz);
@@ -313,17 +343,8 @@ static int record_batch(aqsg_batch_s* b, cudaStream_t s) {
         const unsigned char* pool = (const unsigned char*)b->d_small_ops[c] + poff;
         const SmallItem* items = (const SmallItem*)b->d_small_items[c];
         const int cnt = (int)b->items[c].size();
-        switch (c) {
-            case 0:
-                k_batch_small<8, 128><<<b->grid[c], 128, shm, bs>>>(items, cnt, b->d_counters + c, ops, pool, b->d_out);
-                break;
-            case 1:
-                k_batch_small<16, 256><<<b->grid[c], 256, shm, bs>>>(items, cnt, b->d_counters + c, ops, pool, b->d_out);
-                break;
-            default:
-                k_batch_small<32, 512><<<b->grid[c], 512, shm, bs>>>(items, cnt, b->d_counters + c, ops, pool, b->d_out);
-                break;
-        }
+        small_kernel(c, b->class_matk[c]).launch(b->grid[c], shm, bs, items, cnt, b->d_counters + c, ops, pool,
+                                                 b->d_out);
         AQSG_CUDA_TRY(cudaGetLastError());
         b->kernels++;
     }
@@ -454,16 +475,9 @@ int aqsg_batch_create(aqsg_ctx ctx, const aqsg_circuit* circuits, int count, aqs
         if (b->items[c].empty()) continue;
         const size_t shm = (size_t)8 << kClasses[c].max_n;
         int per_sm = 1;
-        if (c == 0) {
-            cudaFuncSetAttribute(k_batch_small<8, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_small<8, 128>, 128, shm);
-        } else if (c == 1) {
-            cudaFuncSetAttribute(k_batch_small<16, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_small<16, 256>, 256, shm);
-        } else {
-            cudaFuncSetAttribute(k_batch_small<32, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_small<32, 512>, 512, shm);
-        }
+        const SmallKernel kern = small_kernel(c, b->class_matk[c]);
+        cudaFuncSetAttribute(kern.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern.fn, kern.threads, shm);
         if (per_sm < 1) per_sm = 1;
         const int want = per_sm * ctx->sm_count;
         b->grid[c] = (int)b->items[c].size() < want ? (int)b->items[c].size() : want;

@@ -36,6 +36,45 @@ __device__ __forceinline__ T cmul2(T m0, T a, T m1, T b) {
     return r;
 }
 
+// Compensated sums on the FP32 pipe (GB300's FP64 rate is a small fraction
+// of its FP32 rate).  FAcc holds an unevaluated float sum hi + lo: add() is
+// Knuth's TwoSum (the rounding error of each addition is kept in lo), and
+// add_sq() adds x*x exactly (Dekker's TwoProd via FMA).  Over the few
+// hundred terms one thread sums, the result carries ~44 significant bits;
+// threads then combine their value() in FP64.  The _rn intrinsics keep the
+// compiler from contracting or reassociating the error terms.
+struct FAcc {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add(float v) {
+        const float s = __fadd_rn(hi, v);
+        const float bp = __fsub_rn(s, hi);
+        const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(v, bp));
+        hi = s;
+        lo = __fadd_rn(lo, e);
+    }
+    // add an unevaluated sum v + vl
+    __device__ __forceinline__ void add(float v, float vl) {
+        add(v);
+        lo = __fadd_rn(lo, vl);
+    }
+    __device__ __forceinline__ void add_sq(float x) {
+        const float p = __fmul_rn(x, x);
+        add(p, __fmaf_rn(x, x, -p));
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+// |a|^2 of a c64 amplitude as an unevaluated sum h + l (exact up to one
+// rounding of the final sum)
+__device__ __forceinline__ void norm2_ff(float x, float y, float& h, float& l) {
+    const float px = __fmul_rn(x, x), py = __fmul_rn(y, y);
+    const float ex = __fmaf_rn(x, x, -px), ey = __fmaf_rn(y, y, -py);
+    h = __fadd_rn(px, py);
+    const float bp = __fsub_rn(h, px);
+    const float e = __fadd_rn(__fsub_rn(px, __fsub_rn(h, bp)), __fsub_rn(py, bp));
+    l = __fadd_rn(__fadd_rn(ex, ey), e);
+}
+
 // Insert NF fixed bits (ascending positions) into a free index, then OR in
 // their values.  NF == 0 is the identity.
 template <int NF>

@@ -121,6 +121,10 @@ int launch_scale(aqsg_state_s* st, double scale) {
     return AQSG_OK;
 }
 
+// component type of an amplitude type (float2 -> float, double2 -> double)
+template <typename T>
+using a_t = decltype(T{}.x);
+
 // ---- block reduction helpers ---------------------------------------------------
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -151,14 +155,28 @@ __global__ void __launch_bounds__(kRedThreads)
 k_prob_partial(const typename Cx<R>::T* __restrict__ sv, FX fx, uint64_t units, double* partial) {
     __shared__ double sh[32];
     double acc = 0;
-    for (uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < units;
-         u += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t i = fx.expand(u * VEC);
-        if constexpr (VEC == 2) {
-            const float4 f = __ldcs(reinterpret_cast<const float4*>(sv) + (i >> 1));
-            acc += (double)f.x * f.x + (double)f.y * f.y + (double)f.z * f.z + (double)f.w * f.w;
-        } else {
-            const auto a = __ldcs(sv + i);
+    if constexpr (sizeof(R) == 4) {
+        FAcc fa;  // c64: exact squares, compensated sums on the FP32 pipe
+        for (uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < units;
+             u += (uint64_t)gridDim.x * blockDim.x) {
+            const uint64_t i = fx.expand(u * VEC);
+            if constexpr (VEC == 2) {
+                const float4 f = __ldcs(reinterpret_cast<const float4*>(sv) + (i >> 1));
+                fa.add_sq(f.x);
+                fa.add_sq(f.y);
+                fa.add_sq(f.z);
+                fa.add_sq(f.w);
+            } else {
+                const auto a = __ldcs(sv + i);
+                fa.add_sq(a.x);
+                fa.add_sq(a.y);
+            }
+        }
+        acc = fa.value();
+    } else {
+        for (uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < units;
+             u += (uint64_t)gridDim.x * blockDim.x) {
+            const auto a = __ldcs(sv + fx.expand(u * VEC));
             acc += (double)a.x * a.x + (double)a.y * a.y;
         }
     }
@@ -270,9 +288,19 @@ __global__ void __launch_bounds__(256) k_chunk_sums(const T* __restrict__ sv, in
     const uint64_t base = (uint64_t)blockIdx.x << cb;
     const uint64_t len = 1ull << cb;
     double acc = 0;
-    for (uint64_t j = threadIdx.x; j < len; j += blockDim.x) {
-        const T a = sv[base + j];
-        acc += (double)a.x * a.x + (double)a.y * a.y;
+    if constexpr (sizeof(a_t<T>) == 4) {
+        FAcc fa;
+        for (uint64_t j = threadIdx.x; j < len; j += blockDim.x) {
+            const T a = sv[base + j];
+            fa.add_sq(a.x);
+            fa.add_sq(a.y);
+        }
+        acc = fa.value();
+    } else {
+        for (uint64_t j = threadIdx.x; j < len; j += blockDim.x) {
+            const T a = sv[base + j];
+            acc += (double)a.x * a.x + (double)a.y * a.y;
+        }
     }
     const double s = block_sum(acc, sh);
     if (threadIdx.x == 0) sums[blockIdx.x] = s;
@@ -588,15 +616,40 @@ k_expz_partial(const T* __restrict__ sv, int tb, int rb, double* partial) {
 #pragma unroll
     for (int i = 0; i < kZMaxS; ++i) { S[i] = 0; X[i] = 0; }
     const uint64_t iters = threadIdx.x < nt ? (1ull << sb) : 0;
-    for (uint64_t s = 0; s < iters; ++s) {
-        const double p = pr(sv[base + s * nt + threadIdx.x]);
-        tot += p;
+    if constexpr (sizeof(a_t<T>) == 4) {
+        // c64: exact |a|^2 and compensated sums on the FP32 pipe
+        FAcc ft, fs[kZMaxS], fx[kZMaxS];
+        for (uint64_t s = 0; s < iters; ++s) {
+            const T a = sv[base + s * nt + threadIdx.x];
+            float h, l;
+            norm2_ff(a.x, a.y, h, l);
+            ft.add(h, l);
+#pragma unroll
+            for (int i = 0; i < kZMaxS; ++i) {
+                if (i < sb) {
+                    const uint64_t bi = (s >> i) & 1ull;
+                    if (bi) fs[i].add(h, l);
+                    if (i + 1 < sb && (bi ^ ((s >> (i + 1)) & 1ull))) fx[i].add(h, l);
+                }
+            }
+        }
+        tot = ft.value();
 #pragma unroll
         for (int i = 0; i < kZMaxS; ++i) {
-            if (i < sb) {
-                const uint64_t bi = (s >> i) & 1ull;
-                if (bi) S[i] += p;
-                if (i + 1 < sb && (bi ^ ((s >> (i + 1)) & 1ull))) X[i] += p;
+            S[i] = fs[i].value();
+            X[i] = fx[i].value();
+        }
+    } else {
+        for (uint64_t s = 0; s < iters; ++s) {
+            const double p = pr(sv[base + s * nt + threadIdx.x]);
+            tot += p;
+#pragma unroll
+            for (int i = 0; i < kZMaxS; ++i) {
+                if (i < sb) {
+                    const uint64_t bi = (s >> i) & 1ull;
+                    if (bi) S[i] += p;
+                    if (i + 1 < sb && (bi ^ ((s >> (i + 1)) & 1ull))) X[i] += p;
+                }
             }
         }
     }
@@ -911,22 +964,54 @@ k_pauli_partial(const T* __restrict__ sv, uint64_t N, PauliChunk pc, double* par
     double re[kPauliChunk], im[kPauliChunk];
 #pragma unroll
     for (int s = 0; s < kPauliChunk; ++s) re[s] = im[s] = 0.0;
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < N;
-         k += (uint64_t)gridDim.x * blockDim.x) {
-        const T a = sv[k];
-        const double ar = a.x, ai = a.y;
+    if constexpr (sizeof(a_t<T>) == 4) {
+        // c64: exact products (TwoProd), compensated sums on the FP32 pipe
+        FAcc fr[kPauliChunk], fi[kPauliChunk];
+        auto prod = [](FAcc& acc, float x, float y, bool neg) {
+            const float p = __fmul_rn(x, y);
+            const float e = __fmaf_rn(x, y, -p);
+            if (neg) acc.add(-p, -e);
+            else acc.add(p, e);
+        };
+        for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < N;
+             k += (uint64_t)gridDim.x * blockDim.x) {
+            const T a = sv[k];
+#pragma unroll
+            for (int s = 0; s < kPauliChunk; ++s) {
+                if (s < pc.count) {
+                    const T b = sv[k ^ pc.x[s]];
+                    const bool neg = __popcll(k & pc.z[s]) & 1;
+                    // conj(b) a = (br ar + bi ai) + i (br ai - bi ar)
+                    prod(fr[s], b.x, a.x, neg);
+                    prod(fr[s], b.y, a.y, neg);
+                    prod(fi[s], b.x, a.y, neg);
+                    prod(fi[s], b.y, a.x, !neg);
+                }
+            }
+        }
 #pragma unroll
         for (int s = 0; s < kPauliChunk; ++s) {
-            if (s < pc.count) {
-                const T b = sv[k ^ pc.x[s]];
-                const double br = b.x, bi = b.y;
-                double pr = br * ar + bi * ai, pi = br * ai - bi * ar;
-                if (__popcll(k & pc.z[s]) & 1) {
-                    pr = -pr;
-                    pi = -pi;
+            re[s] = fr[s].value();
+            im[s] = fi[s].value();
+        }
+    } else {
+        for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < N;
+             k += (uint64_t)gridDim.x * blockDim.x) {
+            const T a = sv[k];
+            const double ar = a.x, ai = a.y;
+#pragma unroll
+            for (int s = 0; s < kPauliChunk; ++s) {
+                if (s < pc.count) {
+                    const T b = sv[k ^ pc.x[s]];
+                    const double br = b.x, bi = b.y;
+                    double pr = br * ar + bi * ai, pi = br * ai - bi * ar;
+                    if (__popcll(k & pc.z[s]) & 1) {
+                        pr = -pr;
+                        pi = -pi;
+                    }
+                    re[s] += pr;
+                    im[s] += pi;
                 }
-                re[s] += pr;
-                im[s] += pi;
             }
         }
     }

@@ -152,12 +152,15 @@ __device__ __forceinline__ bool compute_any(bool v) {
 // CTA per SM walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ...; a tile
 // is 128 rows of 256 contiguous bytes (the 5 low index bits) at the row
 // offsets of the pass's 7 high tile bits.  Warp 16 is the producer: it
-// bulk-copies tiles into two shared-memory buffers (full[b] completes when a
-// tile has arrived) and copies them back once the 16 compute warps have
-// released them (done[b]); so the next tile loads and the previous one stores
-// while the compute warps run the pass's ops on the current one.  The pass's
-// operand blob and op table are loaded once per CTA.  Every wait is bounded:
-// one that gives up sets the error flag and the CTA winds down.
+// copies tiles in 16-byte cp.async chunks into three shared-memory buffers
+// (full[b] completes when all 32 lanes' chunks have landed; many small
+// requests stay in flight without the per-request cost of bulk copies) and
+// writes them back with 128-bit stores once the 16 compute warps have
+// released them (done[b]); so the next tiles load and the previous one
+// stores while the compute warps run the pass's ops on the current one.
+// The pass's operand blob and op table are bulk-loaded once per CTA.  Every
+// wait is bounded: one that gives up sets the error flag and the CTA winds
+// down.
 __global__ void __launch_bounds__(kTcCta, 1)
 k_stream_tc(float2* __restrict__ sv, const TileGeom g, const TileOp* __restrict__ ops, int nops,
             const unsigned char* __restrict__ pool, int* err, uint32_t ntiles) {
@@ -184,7 +187,7 @@ k_stream_tc(float2* __restrict__ sv, const TileGeom g, const TileOp* __restrict_
     }
     if (tid == 0) {
         for (int b = 0; b < NB; ++b) {
-            mbar_init(full + b, 1);
+            mbar_init(full + b, 32);  // one cp.async arrival per producer lane
             mbar_init(done + b, kTcThreads / 32);
         }
         mbar_init(mma_bar, 1);
@@ -225,12 +228,14 @@ k_stream_tc(float2* __restrict__ sv, const TileGeom g, const TileOp* __restrict_
         }
         auto issue_load = [&](uint32_t i) {
             const uint32_t buf = i % NB;
-            const uint64_t base = tile_base(blockIdx.x + i * gridDim.x);
-            if (lane == 0) mbar_expect_tx(full + buf, kRows * kRowBytes);
-            __syncwarp();
+            const float2* src = sv + tile_base(blockIdx.x + i * gridDim.x);
             unsigned char* dst = smem_raw + buf * kBufBytes;
-            for (uint32_t r = lane; r < kRows; r += 32u)
-                bulk_load(dst + r * kRowStride, sv + base + rowoff[r], kRowBytes, full + buf);
+#pragma unroll 8
+            for (uint32_t q = lane; q < kRows * 16u; q += 32u) {
+                const uint32_t r = q >> 4, c = q & 15u;
+                cp_async16(dst + r * kRowStride + c * 16u, src + rowoff[r] + 2u * c);
+            }
+            cp_async_arrive(full + buf);
         };
         for (uint32_t q = 0; q < count && q < (uint32_t)NB; ++q) issue_load(q);
         for (uint32_t i = 0; i < count; ++i) {
@@ -239,17 +244,20 @@ k_stream_tc(float2* __restrict__ sv, const TileGeom g, const TileOp* __restrict_
                 if (lane == 0) atomicExch(err, 1);
                 break;
             }
-            const uint64_t base = tile_base(blockIdx.x + i * gridDim.x);
+            float2* dstg = sv + tile_base(blockIdx.x + i * gridDim.x);
             const unsigned char* src = smem_raw + buf * kBufBytes;
-            for (uint32_t r = lane; r < kRows; r += 32u)
-                bulk_store(sv + base + rowoff[r], src + r * kRowStride, kRowBytes);
-            bulk_commit();
-            if (i + NB < count) {
-                bulk_wait_read();  // the tile has left the buffer
-                __syncwarp();
-                issue_load(i + NB);
+#pragma unroll 8
+            for (uint32_t q = lane; q < kRows * 16u; q += 32u) {
+                const uint32_t r = q >> 4, c = q & 15u;
+                const uint4 v = *reinterpret_cast<const uint4*>(src + r * kRowStride + c * 16u);
+                __stcs(reinterpret_cast<uint4*>(dstg + rowoff[r]) + c, v);
             }
+            __syncwarp();  // every lane's reads of the buffer are done
+            if (i + NB < count) issue_load(i + NB);
         }
+        // the cp.async copies this warp started have landed (a wound-down
+        // CTA may leave some unconsumed)
+        asm volatile("cp.async.wait_all;" ::: "memory");
         bulk_wait_all();
     } else {
         // ---- compute warps ----
@@ -277,7 +285,9 @@ k_stream_tc(float2* __restrict__ sv, const TileGeom g, const TileOp* __restrict_
         if (!ok || *(volatile int*)err != 0) {
             if (tid == 0) {
                 atomicExch(err, 1);
-                // the MMAs this CTA issued finish before the tensor memory goes
+                // the operand copy and the MMAs this CTA issued finish before
+                // the shared and tensor memory go
+                mbar_wait_bounded(blob_bar, 0, err);
                 mbar_wait_bounded(mma_bar, tph.mma, err);
             }
         }
