@@ -226,42 +226,51 @@ struct TcPhase {
     uint32_t mma = 0;
 };
 
-// One fused unitary on the tile through the tensor cores.  All kTcThreads
-// threads call it.  A bounded wait that gives up sets the error flag (the
-// caller checks it once per tile).
+// One fused unitary on the tile through the tensor cores, for a unitary on KQ
+// tile bits whose operand gather puts CB lane bits on data columns (and
+// 5 - CB on matrix rows; op.lt1, chosen on the host).  All kTcThreads threads
+// call it.  A bounded wait that gives up sets the error flag (the caller
+// checks it once per tile).
 //
 // The op's blob entry holds B hi, B lo (2 N K bytes each), then colbase[c]
 // (tile index of data column c; 512 x u16) and offr[r] (tile-index bits of
 // matrix row r; 32 x u16).
-template <class LAY, class SYNC>
-__device__ __forceinline__ void tc_apply(float2* s, const TileOp& op, const TcSmem& t, TcPhase& ph) {
-    const int k = op.k, D = 1 << k;
-    const uint32_t K = 2u * D, N = 2u * D;
-    const uint32_t blocks = 1u << (kTcTileBits - k - 7);
-    const uint32_t bsplit = 2u * N * K;
-    const uint32_t tid = threadIdx.x;
+//
+// Operand gather: item it (0..7) of thread (warp w, lane l) is data column
+// c = c0 + it * 2^(9-KQ) and matrix row r (both fixed by w and l), so a
+// thread's row bits and its column's low bits stay in registers; the column
+// table is linear over disjoint bits, colbase[c] = colbase[c0] |
+// colbase[it * 2^(9-KQ)], and the operand offset advances by a constant.
+template <class LAY, class SYNC, int KQ, int CB>
+__device__ __forceinline__ void tc_apply_k(float2* s, const TileOp& op, const TcSmem& t, TcPhase& ph) {
+    constexpr uint32_t D = 1u << KQ, K = 2u * D, N = 2u * D;
+    constexpr uint32_t blocks = 1u << (kTcTileBits - KQ - 7);
+    constexpr uint32_t bsplit = 2u * N * K;
+    constexpr int RB = 5 - CB, KD = KQ - RB;
+    static_assert(RB >= 1 && KD >= 0 && KD <= 4, "lane split");
+    constexpr uint32_t CSTEP = 1u << (9 - KQ);          // column step per item
+    constexpr uint32_t OSTEP = (CSTEP / 8u) * 16u * K;   // operand offset step per item
+    const uint32_t tid = threadIdx.x, w = tid >> 5, lane = tid & 31u;
     const unsigned char* bsm = t.blob + op.mat;
     const uint16_t* colbase = reinterpret_cast<const uint16_t*>(bsm + 2u * bsplit);
     const uint16_t* offr = colbase + 512;
 
-    // A operand: each warp's lanes cover 2^cb data columns x 2^(5-cb) matrix
-    // rows (cb = op.lt1, chosen on the host to spread both the tile reads and
-    // the operand stores over the banks)
-    const int cb = op.lt1, rb = 5 - cb, kd = k - rb;
-#pragma unroll 2
-    for (uint32_t u = tid; u < (1u << kTcTileBits); u += kTcThreads) {
-        const uint32_t lane = u & 31u, rest = u >> 5;
-        const uint32_t c = ((rest >> kd) << cb) | (lane >> rb);
-        const uint32_t r = ((rest & ((1u << kd) - 1u)) << rb) | (lane & ((1u << rb) - 1u));
-        const float2 x = s[LAY::at((uint32_t)colbase[c] | (uint32_t)offr[r])];
-        const __nv_bfloat162 hi = __float22bfloat162_rn(x);
-        const float2 hf = __bfloat1622float2(hi);
-        const __nv_bfloat162 lo = __float22bfloat162_rn(make_float2(x.x - hf.x, x.y - hf.y));
-        const uint32_t row = c & 127u;
-        const uint32_t off = (c >> 7) * (256u * K) + (((row >> 3) * (K >> 3) + (r >> 2)) << 7) +
-                             ((row & 7u) << 4) + ((r & 3u) << 2);
-        *reinterpret_cast<__nv_bfloat162*>(t.a + off) = hi;
-        *reinterpret_cast<__nv_bfloat162*>(t.a + kTcABytes + off) = lo;
+    {
+        const uint32_t r = ((w & ((1u << KD) - 1u)) << RB) | (lane & ((1u << RB) - 1u));
+        const uint32_t c0 = ((w >> KD) << CB) | (lane >> RB);
+        const uint32_t j0 = (uint32_t)colbase[c0] | (uint32_t)offr[r];
+        const uint32_t off0 = (c0 >> 3) * 16u * K + (r >> 2) * 128u + (c0 & 7u) * 16u + (r & 3u) * 4u;
+        unsigned char* ahi = t.a + off0;
+#pragma unroll
+        for (int it = 0; it < 8; ++it) {
+            const uint32_t j = j0 | (uint32_t)colbase[CSTEP * it];
+            const float2 x = s[LAY::at(j)];
+            const __nv_bfloat162 hi = __float22bfloat162_rn(x);
+            const float2 hf = __bfloat1622float2(hi);
+            const __nv_bfloat162 lo = __float22bfloat162_rn(make_float2(x.x - hf.x, x.y - hf.y));
+            *reinterpret_cast<__nv_bfloat162*>(ahi + OSTEP * it) = hi;
+            *reinterpret_cast<__nv_bfloat162*>(ahi + kTcABytes + OSTEP * it) = lo;
+        }
     }
     fence_async_smem();
     SYNC::sync();
@@ -269,12 +278,14 @@ __device__ __forceinline__ void tc_apply(float2* s, const TileOp& op, const TcSm
     if (tid == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t idesc = tc_idesc(128, N);
-        const uint32_t sbo = (K / 8u) * 128u;
+        constexpr uint32_t sbo = (K / 8u) * 128u;
         const uint32_t a_hi = smem_u32(t.a), a_lo = a_hi + kTcABytes;
         const uint32_t b_hi = smem_u32(bsm), b_lo = b_hi + bsplit;
+#pragma unroll
         for (uint32_t blk = 0; blk < blocks; ++blk) {
             const uint32_t dcol = t.tmem + blk * N;
             const uint32_t aoff = blk * (256u * K);
+#pragma unroll
             for (uint32_t st = 0; st < K / 16u; ++st) {
                 const uint32_t ko = st * 256u;  // two core matrices along K
                 tc_mma(dcol, tc_desc(a_hi + aoff + ko, 128u, sbo), tc_desc(b_hi + ko, 128u, sbo), idesc,
@@ -291,19 +302,35 @@ __device__ __forceinline__ void tc_apply(float2* s, const TileOp& op, const TcSm
 
     // D straight to the tile: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its
     // data columns) and the 16 columns 16 (w / 4) .. + 15 (8 output rows)
-    const uint32_t w = tid >> 5, lane = tid & 31u, g = w & 3u, h = w >> 2;
+    const uint32_t g = w & 3u, h = w >> 2;
     uint32_t v[16];
     tc_ld16(t.tmem + ((g * 32u) << 16) + h * 16u, v);
     tc_ld_wait();
     const uint32_t tcol = h * 16u;
-    const uint32_t c = ((tcol >> (k + 1)) << 7) + g * 32u + lane;
+    const uint32_t c = ((tcol >> (KQ + 1)) << 7) + g * 32u + lane;
     const uint32_t r0 = (tcol & (N - 1u)) >> 1;
     const uint32_t cbase = colbase[c];
 #pragma unroll
     for (int i = 0; i < 8; ++i)
-        s[LAY::at(cbase | (uint32_t)offr[r0 + i])] = make_float2(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1]));
+        s[LAY::at(cbase | (uint32_t)offr[r0 + i])] =
+            make_float2(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1]));
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     SYNC::sync();
+}
+
+template <class LAY, class SYNC>
+__device__ __forceinline__ void tc_apply(float2* s, const TileOp& op, const TcSmem& t, TcPhase& ph) {
+    switch (op.k * 8 + op.lt1) {
+        case 3 * 8 + 2: tc_apply_k<LAY, SYNC, 3, 2>(s, op, t, ph); break;
+        case 3 * 8 + 3: tc_apply_k<LAY, SYNC, 3, 3>(s, op, t, ph); break;
+        case 3 * 8 + 4: tc_apply_k<LAY, SYNC, 3, 4>(s, op, t, ph); break;
+        case 4 * 8 + 2: tc_apply_k<LAY, SYNC, 4, 2>(s, op, t, ph); break;
+        case 4 * 8 + 3: tc_apply_k<LAY, SYNC, 4, 3>(s, op, t, ph); break;
+        case 4 * 8 + 4: tc_apply_k<LAY, SYNC, 4, 4>(s, op, t, ph); break;
+        case 5 * 8 + 2: tc_apply_k<LAY, SYNC, 5, 2>(s, op, t, ph); break;
+        case 5 * 8 + 3: tc_apply_k<LAY, SYNC, 5, 3>(s, op, t, ph); break;
+        default: tc_apply_k<LAY, SYNC, 5, 4>(s, op, t, ph); break;
+    }
 }
 
 // k-qubit dense unitary on CUDA cores: each thread updates one group of 2^K
