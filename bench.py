@@ -52,7 +52,7 @@ def parse_args():
     ap.add_argument("--cpu-sample-ops", type=int, default=8,
                     help="QFT gates in the CPU-baseline sample")
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--only", choices=["fused_brickwork", "plain12", "vqe_batch", "serving"],
+    ap.add_argument("--only", choices=["fused_brickwork", "plain12", "vqe_batch", "serving", "qft_grid"],
                     help="run one secondary workload alone (at --n qubits where it takes a size) "
                          "and print its JSON; for profiling")
     ap.add_argument("--depth", type=int, default=20, help="brick-work depth for --only fused_brickwork")
@@ -241,6 +241,25 @@ def bench_fused_brickwork(ctx, st, stream, n, depth):
     res["max_rel_err_scaled"] = mx * np.sqrt(N)  # error relative to a typical |a| = 2^(-n/2)
     res["l2_bytes_note"] = "fused/tiled passes move 2 x 8 B x 2^n each"
     return res
+
+
+def bench_qft_grid(ctx, stream, sizes=((24, "c64"), (28, "c64"), (24, "c128"), (28, "c128"), (30, "c128"))):
+    """The other sizes and dtypes of the QFT workload (with swaps, one gate per
+    pass, register resident in HBM, starting from |0...0>): gate-apps/s and
+    algorithmic HBM GB/s for each (n, dtype), 1 warm-up and 2 timed steps."""
+    import afquantumsim_gb300 as aq
+    out = {}
+    for n, dt in sizes:
+        amp_b = 8 if dt == "c64" else 16
+        total_bytes, _, _ = algorithmic_bytes(n, amp_b)
+        ops = aq.op_array(qft_ops(n))
+        with aq.State(ctx, n, aq.C64 if dt == "c64" else aq.C128) as st:
+            st.set_basis(0)  # the kernels do not branch on amplitude values
+            st.apply(ops, aq.EXEC_PER_GATE)  # warm-up
+            ms = _time_ms(stream, lambda: st.apply(ops, aq.EXEC_PER_GATE), 2)
+        out[f"qft{n}_{dt}"] = {"ms_per_step": round(ms, 2), "gate_apps_per_s": round(len(ops) / (ms / 1e3), 1),
+                               "hbm_gbs": round(total_bytes / (ms / 1e3) / 1e9, 1)}
+    return out
 
 
 def bench_plain12(ctx, stream, n=12, layers=10):
@@ -561,6 +580,7 @@ def run_ours(args, rank, world, local_rank):
         extras["tiled_ms_per_step"] = round(e0.elapsed_time(e1) / 2, 3)
         if args.dtype == "c64":
             extras["fused_brickwork"] = bench_fused_brickwork(ctx, st, stream, n, depth=20)
+        extras["qft_grid"] = bench_qft_grid(ctx, stream)
         extras["plain12"] = bench_plain12(ctx, stream)
         extras["vqe_batch"] = bench_vqe_batch(ctx)
         if args.dtype == "c64":
@@ -675,6 +695,8 @@ def run_only(args):
             res = bench_fused_brickwork(ctx, st, stream, args.n, args.depth)
     elif args.only == "plain12":
         res = bench_plain12(ctx, stream)
+    elif args.only == "qft_grid":
+        res = bench_qft_grid(ctx, stream)
     elif args.only == "vqe_batch":
         res = bench_vqe_batch(ctx, count=args.count or 4096)
     else:
