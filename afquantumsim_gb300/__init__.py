@@ -42,6 +42,7 @@ EXPORTS = [
     "aqsg_server_create", "aqsg_server_submit", "aqsg_server_start", "aqsg_server_poll",
     "aqsg_server_wait_idle", "aqsg_server_get_stats", "aqsg_server_destroy",
     "aqsg_expect_pauli", "aqsg_autotune", "aqsg_batch_tuning", "aqsg_selftest_bounded_wait",
+    "aqsg_state_download_async",
 ]
 
 _lib = None
@@ -100,6 +101,7 @@ def load_library(path: os.PathLike | str | None = None) -> C.CDLL:
         "aqsg_state_set_product": ([P, C.POINTER(C.c_float)], I),
         "aqsg_state_upload": ([P, P, I], I),
         "aqsg_state_download": ([P, P], I),
+        "aqsg_state_download_async": ([P, P], I),
         "aqsg_state_download_range": ([P, U64, U64, P], I),
         "aqsg_state_copy": ([P, P], I),
         "aqsg_check_ops": ([I, C.POINTER(Op), I], I),
@@ -350,6 +352,11 @@ class State:
 
     def download_ptr(self, ptr: int) -> None:
         _check(self.lib.aqsg_state_download(self.h, ptr))
+
+    def download_async_ptr(self, ptr: int) -> None:
+        """Enqueue the copy to host memory at ptr; complete after the
+        context's next synchronize()."""
+        _check(self.lib.aqsg_state_download_async(self.h, ptr))
 
     def compare(self, other: "State"):
         """(max |a - b|, <a|b>, |a|^2, |b|^2) in FP64, on the device."""

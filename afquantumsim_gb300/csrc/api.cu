@@ -436,6 +436,14 @@ int aqsg_state_download(aqsg_state st, void* host) {
     return AQSG_OK;
 }
 
+int aqsg_state_download_async(aqsg_state st, void* host) {
+    if (int rc = check_state(st)) return rc;
+    if (!host) return set_error(AQSG_ERR_NULL, "NULL host buffer");
+    AQSG_CUDA_TRY(cudaMemcpyAsync(host, st->d, st->amps * amp_bytes(st->dtype),
+                                  cudaMemcpyDeviceToHost, st->ctx->stream));
+    return AQSG_OK;
+}
+
 int aqsg_state_download_range(aqsg_state st, uint64_t begin, uint64_t count, void* host) {
     if (int rc = check_state(st)) return rc;
     if (!host) return set_error(AQSG_ERR_NULL, "NULL host buffer");

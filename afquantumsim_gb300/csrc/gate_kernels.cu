@@ -20,7 +20,10 @@ namespace aqsg {
 
 constexpr int kThreads = 256;
 
-enum PairOp { P_MAT2 = 0, P_DIAG2 = 1, P_PERMX = 2, P_PERMOR = 3 };
+// P_MAT2R: a 2x2 matrix with real entries (H, RotY, real unitaries): half the
+// multiplies of P_MAT2, which matters where arithmetic bounds the pass
+// (complex128 on a GPU whose FP64 rate is a small fraction of FP32).
+enum PairOp { P_MAT2 = 0, P_DIAG2 = 1, P_PERMX = 2, P_PERMOR = 3, P_MAT2R = 4 };
 
 template <typename R>
 struct M2 {
@@ -95,6 +98,14 @@ k_pair(typename Cx<R>::T* __restrict__ sv, FX fx, uint64_t tmask, uint64_t amask
             if constexpr (OP == P_MAT2) {
                 lo[it].a[v] = cmul2(m.m[0], a, m.m[1], b);
                 hi[it].a[v] = cmul2(m.m[2], a, m.m[3], b);
+            } else if constexpr (OP == P_MAT2R) {
+                T r0, r1;
+                r0.x = m.m[0].x * a.x + m.m[1].x * b.x;
+                r0.y = m.m[0].x * a.y + m.m[1].x * b.y;
+                r1.x = m.m[2].x * a.x + m.m[3].x * b.x;
+                r1.y = m.m[2].x * a.y + m.m[3].x * b.y;
+                lo[it].a[v] = r0;
+                hi[it].a[v] = r1;
             } else if constexpr (OP == P_DIAG2) {  // m[0] on t=0, m[1] on t=1
                 lo[it].a[v] = cmul(m.m[0], a);
                 hi[it].a[v] = cmul(m.m[1], b);
@@ -287,7 +298,8 @@ static int launch_typed(aqsg_state_s* st, const LOp& op) {
             FixedBits f = make_fixed(op.cmask | tmask, op.cval);
             M2<R> m;
             for (int e = 0; e < 4; ++e) m.m[e] = cval<R>(op.m[2 * e], op.m[2 * e + 1]);
-            const int OPK = op.cls == L_MAT2 ? P_MAT2 : op.cls == L_DIAG2 ? P_DIAG2
+            const bool real = op.m[1] == 0.0 && op.m[3] == 0.0 && op.m[5] == 0.0 && op.m[7] == 0.0;
+            const int OPK = op.cls == L_MAT2 ? (real ? P_MAT2R : P_MAT2) : op.cls == L_DIAG2 ? P_DIAG2
                           : op.cls == L_PERM_X ? P_PERMX : P_PERMOR;
             uint64_t units = N >> f.nf;
             const bool packed = is_f && op.t0 == 0;
@@ -297,6 +309,7 @@ static int launch_typed(aqsg_state_s* st, const LOp& op) {
                 constexpr bool P = decltype(packed_tag)::value;
                 switch (OPK) {
                     case P_MAT2: launch_pair_v<R, V, P, P_MAT2>(st, f, tmask, op.amask, units, m); break;
+                    case P_MAT2R: launch_pair_v<R, V, P, P_MAT2R>(st, f, tmask, op.amask, units, m); break;
                     case P_DIAG2: launch_pair_v<R, V, P, P_DIAG2>(st, f, tmask, op.amask, units, m); break;
                     case P_PERMX: launch_pair_v<R, V, P, P_PERMX>(st, f, tmask, op.amask, units, m); break;
                     default: launch_pair_v<R, V, P, P_PERMOR>(st, f, tmask, op.amask, units, m); break;

@@ -546,26 +546,42 @@ def run_ours(args, rank, world, local_rank):
         "Swap_pass": {"ms": round(sw_ms, 4), "GBps": round(per_kind["Swap"] / (sw_ms / 1e3) / 1e9, 1)},
     }
 
-    # end to end through the C-ABI with host buffers: upload, simulate, download
-    e2e_steps = max(2, min(args.steps, 3))
-    st.upload_ptr(host_in.data_ptr())
-    st.apply(ops, mode)
-    st.download_ptr(host_out.data_ptr())
+    # end to end through the C ABI with host buffers.  Per step: upload the
+    # step's input from pinned host memory, run the circuit, copy its result
+    # to pinned host memory.  Two registers on two contexts (streams) take the
+    # steps in turn, so the copies of one step overlap the gates of the other.
+    e2e_steps = max(4, args.steps)
+    ctx2 = aq.Context(local_rank)
+    st2 = aq.State(ctx2, n, aq.C64 if args.dtype == "c64" else aq.C128)
+    host_out2 = torch.empty(N, dtype=dt_t, pin_memory=True)
+    lanes = [(ctx, st, host_out), (ctx2, st2, host_out2)]
+    for c, r, ho in lanes:  # warm-up
+        r.upload_ptr(host_in.data_ptr())
+        r.apply(ops, mode)
+        r.download_async_ptr(ho.data_ptr())
+        c.synchronize()
     if world > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        st.upload_ptr(host_in.data_ptr())
-        st.apply(ops, mode)
-        st.download_ptr(host_out.data_ptr())
+    for step in range(e2e_steps):
+        c, r, ho = lanes[step % 2]
+        c.synchronize()  # this register's previous step (its result copy) is done
+        r.upload_ptr(host_in.data_ptr())
+        r.apply(ops, mode)
+        r.download_async_ptr(ho.data_ptr())
+    ctx.synchronize()
+    ctx2.synchronize()
     e2e_s = time.perf_counter() - t0
+    st2.free()
+    ctx2.close()
     if world > 1:
         t = torch.tensor([e2e_s], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e = {"value": round(world * gates * e2e_steps / e2e_s, 3), "unit": "gate-apps/s",
            "h2d_bytes_per_step": N * amp_b, "d2h_bytes_per_step": N * amp_b,
-           "ms_per_step": round(e2e_s / e2e_steps * 1e3, 3)}
+           "ms_per_step": round(e2e_s / e2e_steps * 1e3, 3), "steps": e2e_steps,
+           "pipeline": "two registers on two streams; each step uploads its input and reads its result"}
 
     extras = {}
     if not args.no_extras and rank == 0:

@@ -200,6 +200,13 @@ int aqsg_state_download(aqsg_state st, void* host);
 int aqsg_state_download_range(aqsg_state st, uint64_t begin, uint64_t count,
                               void* host);
 
+/* As aqsg_state_download, but only enqueued on the context's stream: the
+ * host buffer is complete after the next aqsg_synchronize of the context.
+ * With pinned host memory this lets a host pipeline registers on several
+ * contexts (copies of one overlapping the gates of another).  No reference
+ * counterpart (the reference reads the state synchronously). */
+int aqsg_state_download_async(aqsg_state st, void* host);
+
 /* Copy src into dst (same n and dtype). */
 int aqsg_state_copy(aqsg_state dst, aqsg_state src);
 
