@@ -128,6 +128,11 @@ int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, Tile
 // Launch the passes on `stream`; dev = device copy of table + pool.
 int launch_tile_plan(void* sv, const TilePlan& plan, const void* dev, cudaStream_t stream, int* d_err,
                      uint64_t* launches);
+// A plain (no tensor-core) complex64 streaming plan over `members` registers
+// at reg_stride amplitudes from one another, whose tables (the same geometry,
+// their own ops) sit dev_stride bytes apart from dev0: one launch per pass.
+int launch_tile_plan_multi(void* sv0, uint64_t reg_stride, int members, const TilePlan& plan, const void* dev0,
+                           uint64_t dev_stride, cudaStream_t stream, uint64_t* launches);
 // Runs ops through shared-memory tile passes; returns AQSG_OK.
 int run_tiled(aqsg_state_s* st, const std::vector<LOp>& ops);
 // Largest tile (log2 amplitudes) the tile kernel holds for a dtype.

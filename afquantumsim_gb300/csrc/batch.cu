@@ -15,6 +15,8 @@
 #include <cstring>
 #include <vector>
 
+#include <map>
+
 #include "tile_device.cuh"
 
 namespace aqsg {
@@ -111,6 +113,24 @@ k_batch_small(const SmallItem* __restrict__ items, int count, int* counter, cons
 }
 
 __global__ void k_basis0(float2* sv) { sv[0] = make_float2(1.f, 0.f); }
+// |0...0> in each of gridDim.x registers `stride` amplitudes apart (already zeroed)
+__global__ void k_basis0_multi(float2* sv, uint64_t stride) {
+    sv[(uint64_t)blockIdx.x * stride] = make_float2(1.f, 0.f);
+}
+
+// Large registers whose tile plans have the same geometry (qubits, passes,
+// tile bits, table and pool sizes) and no tensor-core passes run as a group:
+// one launch per pass for all of them, their registers side by side and
+// their op tables at a fixed stride in the device plan area.
+struct LargeGroup {
+    int n = 0;
+    std::vector<size_t> members;      // indices into aqsg_batch_s::large / plans
+    uint64_t dev_off = 0, stride = 0;  // first member's table in d_large, distance between members
+    void* regs = nullptr;              // members x 2^n amplitudes
+    double* partials = nullptr;        // members x expz_partial_doubles(n)
+    uint64_t* d_out_off = nullptr;     // members result offsets into d_out
+};
+constexpr uint64_t kGroupBytes = 1ull << 30;  // registers of one group at most
 
 // classes of small registers: (max qubits, threads, elements per thread)
 struct SmallClass {
@@ -168,6 +188,8 @@ struct aqsg_batch_s {
     std::vector<int> tc;     // per large circuit: fused unitaries on the tensor cores
     std::vector<TilePlan> plans;
     std::vector<size_t> plan_off;  // offset of each plan's table+pool in d_large
+    std::vector<LargeGroup> groups;
+    std::vector<char> grouped;     // per large circuit: runs in a group
     void* d_large = nullptr;
     // parallel branches of the graph: large circuits go round-robin to
     // branch streams, each with its own register and reduction scratch
@@ -187,6 +209,8 @@ struct aqsg_batch_s {
 namespace aqsg {
 
 int launch_expz_raw(const void* sv, int n, int dtype, double* partial, double* out_raw, cudaStream_t stream);
+int launch_expz_raw_multi(const void* sv0, uint64_t reg_stride, int members, int n, double* partial,
+                          const uint64_t* out_off, double* out_base, cudaStream_t stream);
 size_t expz_partial_doubles(int n);
 
 // Lower and encode every circuit; fills the host-side tables of b.
@@ -348,7 +372,24 @@ static int record_batch(aqsg_batch_s* b, cudaStream_t s) {
         AQSG_CUDA_TRY(cudaGetLastError());
         b->kernels++;
     }
+    for (size_t gi = 0; gi < b->groups.size(); ++gi) {
+        const LargeGroup& gr = b->groups[gi];
+        cudaStream_t bs = b->streams[(gi + 3) % b->streams.size()];
+        const uint64_t amps = 1ull << gr.n;
+        const int members = (int)gr.members.size();
+        AQSG_CUDA_TRY(cudaMemsetAsync(gr.regs, 0, (size_t)members * amps * 8, bs));
+        k_basis0_multi<<<members, 1, 0, bs>>>((float2*)gr.regs, amps);
+        AQSG_CUDA_TRY(cudaGetLastError());
+        const TilePlan& plan = b->plans[gr.members[0]];
+        if (int rc = launch_tile_plan_multi(gr.regs, amps, members, plan, (const char*)b->d_large + gr.dev_off,
+                                            gr.stride, bs, &b->kernels))
+            return rc;
+        if (int rc = launch_expz_raw_multi(gr.regs, amps, members, gr.n, gr.partials, gr.d_out_off, b->d_out, bs))
+            return rc;
+        b->kernels += 3;
+    }
     for (size_t k = 0; k < b->large.size(); ++k) {
+        if (b->grouped[k]) continue;
         const int i = b->large[k];
         const int n = b->n[i];
         const int br = branch_of_large(b, k);
@@ -378,6 +419,11 @@ static void free_batch(aqsg_batch_s* b) {
         if (b->d_small_ops[c]) cudaFree(b->d_small_ops[c]);
     }
     if (b->d_large) cudaFree(b->d_large);
+    for (LargeGroup& gr : b->groups) {
+        if (gr.regs) cudaFree(gr.regs);
+        if (gr.partials) cudaFree(gr.partials);
+        if (gr.d_out_off) cudaFree(gr.d_out_off);
+    }
     for (void* p : b->regs)
         if (p) cudaFree(p);
     for (void* p : b->partials)
@@ -437,12 +483,66 @@ int aqsg_batch_create(aqsg_ctx ctx, const aqsg_circuit* circuits, int count, aqs
             e = cudaMemcpy(b->d_small_items[c], b->items[c].data(), sizeof(SmallItem) * b->items[c].size(),
                            cudaMemcpyHostToDevice);
     }
+    // group the large registers with equal plan geometry (plain plans only)
+    b->grouped.assign(b->large.size(), 0);
+    {
+        std::map<std::vector<uint64_t>, std::vector<size_t>> by_key;
+        for (size_t k = 0; k < b->large.size(); ++k) {
+            const TilePlan& p = b->plans[k];
+            if (p.any_tc) continue;
+            std::vector<uint64_t> key = {(uint64_t)p.n, p.table.size(), p.pool.size(), p.passes.size()};
+            for (const TilePass& ps : p.passes) {
+                key.push_back(((uint64_t)ps.m << 48) | ((uint64_t)ps.L << 40) | ((uint64_t)ps.matk << 32) |
+                              ps.first);
+                key.push_back(ps.count);
+                uint64_t bits = 0;
+                for (int i = 0; i < ps.m; ++i) bits |= 1ull << ps.tbits[i];
+                key.push_back(bits);
+            }
+            by_key[key].push_back(k);
+        }
+        for (auto& kv : by_key) {
+            const int n = b->plans[kv.second[0]].n;
+            const size_t per_chunk = std::max<size_t>(1, std::min<size_t>(kGroupBytes >> (n + 3), 65535));
+            for (size_t at = 0; at < kv.second.size(); at += per_chunk) {
+                LargeGroup gr;
+                gr.n = n;
+                gr.members.assign(kv.second.begin() + (long)at,
+                                  kv.second.begin() + (long)std::min(kv.second.size(), at + per_chunk));
+                for (size_t k : gr.members) b->grouped[k] = 1;
+                b->groups.push_back(std::move(gr));
+            }
+        }
+    }
+    // device plan area: each group's members at a fixed stride, then the rest
+    b->plan_off.assign(b->plans.size(), 0);
     size_t large_bytes = 0;
-    for (const TilePlan& p : b->plans) {
-        b->plan_off.push_back(large_bytes);
+    for (LargeGroup& gr : b->groups) {
+        const TilePlan& p = b->plans[gr.members[0]];
+        gr.stride = (p.pool_offset() + p.pool.size() + 255) & ~size_t(255);
+        gr.dev_off = large_bytes;
+        for (size_t j = 0; j < gr.members.size(); ++j) b->plan_off[gr.members[j]] = large_bytes + j * gr.stride;
+        large_bytes += gr.members.size() * gr.stride;
+    }
+    for (size_t k = 0; k < b->plans.size(); ++k) {
+        if (b->grouped[k]) continue;
+        const TilePlan& p = b->plans[k];
+        b->plan_off[k] = large_bytes;
         large_bytes += (p.pool_offset() + p.pool.size() + 255) & ~size_t(255);
     }
     if (e == cudaSuccess && large_bytes) e = cudaMalloc(&b->d_large, large_bytes);
+    for (LargeGroup& gr : b->groups) {
+        if (e != cudaSuccess) break;
+        const size_t members = gr.members.size();
+        e = cudaMalloc(&gr.regs, members * ((size_t)8 << gr.n));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&gr.partials, sizeof(double) * members * expz_partial_doubles(gr.n));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&gr.d_out_off, sizeof(uint64_t) * members);
+        if (e == cudaSuccess) {
+            std::vector<uint64_t> off(members);
+            for (size_t j = 0; j < members; ++j) off[j] = b->out_off[b->large[gr.members[j]]];
+            e = cudaMemcpy(gr.d_out_off, off.data(), sizeof(uint64_t) * members, cudaMemcpyHostToDevice);
+        }
+    }
     // branch streams: three for the small classes, up to kMaxBranches overall
     int nb = 3;
     if ((int)b->large.size() + 3 > nb) nb = (int)b->large.size() + 3;
@@ -458,6 +558,7 @@ int aqsg_batch_create(aqsg_ctx ctx, const aqsg_circuit* circuits, int count, aqs
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
     std::vector<int> branch_max(nb, 0);
     for (size_t k = 0; k < b->large.size(); ++k) {
+        if (b->grouped[k]) continue;
         const int br = branch_of_large(b, k);
         branch_max[br] = std::max(branch_max[br], b->n[b->large[k]]);
     }

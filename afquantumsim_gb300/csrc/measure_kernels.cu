@@ -607,8 +607,11 @@ int launch_expz_raw(const void* sv, int n, int dtype, double* partial, double* o
 
 template <typename T>
 __global__ void __launch_bounds__(256)
-k_expz_partial(const T* __restrict__ sv, int tb, int rb, double* partial) {
+k_expz_partial(const T* __restrict__ sv, int tb, int rb, double* partial, uint64_t reg_stride = 0,
+               uint64_t partial_stride = 0) {
     __shared__ double sh[32];
+    sv += (uint64_t)blockIdx.y * reg_stride;  // grouped registers: one per blockIdx.y
+    partial += (uint64_t)blockIdx.y * partial_stride;
     const int sb = rb - tb;
     const uint64_t base = (uint64_t)blockIdx.x << rb;
     const uint64_t nt = 1ull << tb;  // threads that own indices (<= blockDim.x)
@@ -678,7 +681,10 @@ k_expz_partial(const T* __restrict__ sv, int tb, int rb, double* partial) {
 
 // One thread per output value: threads [0, n) -> S1 over index bits,
 // [n, 2n-1) -> X over neighbour bit pairs, thread 2n-1 -> total.
-__global__ void k_expz_final(const double* partial, int n, int rb, uint64_t nblocks, double* res) {
+__global__ void k_expz_final(const double* partial, int n, int rb, uint64_t nblocks, double* res,
+                             uint64_t partial_stride = 0, const uint64_t* res_off = nullptr) {
+    partial += (uint64_t)blockIdx.x * partial_stride;  // grouped registers: one block each
+    if (res_off) res += res_off[blockIdx.x];
     const int t = threadIdx.x;
     if (t >= 2 * n) return;
     const int stride = 2 * rb;
@@ -814,15 +820,23 @@ extern "C" int aqsg_state_compare(aqsg_state a, aqsg_state b, double* max_abs_di
 
 namespace aqsg {
 
+// Amplitudes per block of the expectation reduction: 2^12 (at most 2^16
+// blocks), the whole register when smaller.
+static int expz_rb(int n) {
+    int rb = n < 12 ? n : 12;
+    if (n - rb > 16) rb = n - 16;
+    return rb;
+}
+
 size_t expz_partial_doubles(int n) {
-    const int rb = n < 20 ? n : 20;
+    const int rb = expz_rb(n);
     return ((size_t)1 << (n - rb)) * 2 * (size_t)rb;
 }
 
 // Writes the 2n raw sums (S over index bits, X over neighbour bit pairs, then
 // the total) of register sv to out_raw, on `stream`, without synchronising.
 int launch_expz_raw(const void* sv, int n, int dtype, double* partial, double* out_raw, cudaStream_t stream) {
-    const int rb = n < 20 ? n : 20;
+    const int rb = expz_rb(n);
     int tb = rb < 8 ? rb : 8;
     if (rb - tb > kZMaxS) tb = rb - kZMaxS;
     const uint64_t nblocks = (1ull << n) >> rb;
@@ -832,6 +846,24 @@ int launch_expz_raw(const void* sv, int n, int dtype, double* partial, double* o
     else
         k_expz_partial<double2><<<(unsigned)nblocks, threads, 0, stream>>>((const double2*)sv, tb, rb, partial);
     k_expz_final<<<1, 128, 0, stream>>>(partial, n, rb, nblocks, out_raw);
+    AQSG_CUDA_TRY(cudaGetLastError());
+    return AQSG_OK;
+}
+
+// The raw sums of `members` c64 registers reg_stride amplitudes apart; the
+// sums of register j go to out_base + out_off[j] (device array).  partial
+// holds members x expz_partial_doubles(n) doubles.
+int launch_expz_raw_multi(const void* sv0, uint64_t reg_stride, int members, int n, double* partial,
+                          const uint64_t* out_off, double* out_base, cudaStream_t stream) {
+    const int rb = expz_rb(n);
+    int tb = rb < 8 ? rb : 8;
+    if (rb - tb > kZMaxS) tb = rb - kZMaxS;
+    const uint64_t nblocks = (1ull << n) >> rb;
+    const int threads = (1 << tb) < 32 ? 32 : (1 << tb);
+    const uint64_t pd = expz_partial_doubles(n);
+    k_expz_partial<float2><<<dim3((unsigned)nblocks, (unsigned)members), threads, 0, stream>>>(
+        (const float2*)sv0, tb, rb, partial, reg_stride, pd);
+    k_expz_final<<<(unsigned)members, 128, 0, stream>>>(partial, n, rb, nblocks, out_base, pd, out_off);
     AQSG_CUDA_TRY(cudaGetLastError());
     return AQSG_OK;
 }

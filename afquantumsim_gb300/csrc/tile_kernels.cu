@@ -59,9 +59,9 @@ k_tile(typename Cx<R>::T* __restrict__ sv, const TileGeom g, const TileOp* __res
 // loads, compute and stores.  MATK: the pass has dense k-qubit ops on CUDA
 // cores (their register groups allow two CTAs per SM instead of three).
 template <typename R, int EPT, bool MATK>
-__global__ void __launch_bounds__(256, MATK ? 2 : 3)
-k_tile_stream(typename Cx<R>::T* __restrict__ sv, const TileGeom g, const TileOp* __restrict__ ops, int nops,
-              const unsigned char* __restrict__ pool) {
+__device__ __forceinline__ void tile_stream_body(typename Cx<R>::T* __restrict__ sv, const TileGeom& g,
+                                                 const TileOp* __restrict__ ops, int nops,
+                                                 const unsigned char* __restrict__ pool, uint64_t tile) {
     using T = typename Cx<R>::T;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     const int m = g.m, L = g.L;
@@ -69,7 +69,7 @@ k_tile_stream(typename Cx<R>::T* __restrict__ sv, const TileGeom g, const TileOp
     T* s = reinterpret_cast<T*>(smem_raw);
     uint64_t* rowoff = reinterpret_cast<uint64_t*>(smem_raw + sizeof(T) * size);
     const uint32_t rows = 1u << (m - L), rowlen = 1u << L;
-    uint64_t base = blockIdx.x;  // the block index spread over the non-tile bits
+    uint64_t base = tile;  // the tile index spread over the non-tile bits
     for (int i = 0; i < m; ++i) {
         const int b = g.tbits[i];
         const uint64_t lo = base & ((1ull << b) - 1ull);
@@ -106,11 +106,29 @@ k_tile_stream(typename Cx<R>::T* __restrict__ sv, const TileGeom g, const TileOp
     }
 }
 
-// Streaming passes: a persistent CTA walks the tiles blockIdx.x,
-// blockIdx.x + gridDim.x, ...  A tile is kRows rows of 256 contiguous bytes
-// (the L low index bits); warp 0 moves them with bulk copies into kBufs
-// shared-memory buffers, so the next tiles load and the previous one stores
-// while this one computes.  Every wait is bounded (error flag, early exit).
+template <typename R, int EPT, bool MATK>
+__global__ void __launch_bounds__(256, MATK ? 2 : 3)
+k_tile_stream(typename Cx<R>::T* __restrict__ sv, const TileGeom g, const TileOp* __restrict__ ops, int nops,
+              const unsigned char* __restrict__ pool) {
+    tile_stream_body<R, EPT, MATK>(sv, g, ops, nops, pool, blockIdx.x);
+}
+
+// The same pass over `members` registers of equal shape and plan geometry,
+// one launch: block b runs tile b % tiles of register b / tiles, whose
+// amplitudes start reg_stride amplitudes after the previous register's and
+// whose op table + operand pool start dev_stride bytes after the previous
+// one's (the batched engine's groups of equal-structure circuits).
+template <typename R, int EPT, bool MATK>
+__global__ void __launch_bounds__(256, MATK ? 2 : 3)
+k_tile_stream_multi(typename Cx<R>::T* __restrict__ sv0, uint64_t reg_stride, const TileGeom g,
+                    const unsigned char* __restrict__ dev0, uint64_t dev_stride, uint32_t op_first, int nops,
+                    uint64_t pool_off, uint32_t tiles) {
+    const uint32_t member = blockIdx.x / tiles, tile = blockIdx.x % tiles;
+    const unsigned char* dev = dev0 + (uint64_t)member * dev_stride;
+    tile_stream_body<R, EPT, MATK>(sv0 + (uint64_t)member * reg_stride, g,
+                                   reinterpret_cast<const TileOp*>(dev) + op_first, nops, dev + pool_off, tile);
+}
+
 constexpr uint32_t kRowBytes = 256;
 constexpr uint32_t kRows = 128;                     // rows of a 2^12-amplitude c64 tile
 constexpr int kTcCta = kTcThreads + 32;             // 16 compute warps + 1 producer warp
@@ -711,6 +729,36 @@ static int launch_plan_t(void* sv, const TilePlan& plan, const void* dev, cudaSt
             (p.matk ? kplain_k : kplain)<<<(unsigned)(1ull << (n - geo.m)), 256, shm, stream>>>(
                 (T*)sv, geo, dops + p.first, (int)p.count, dpool);
         }
+        if (launches) ++*launches;
+        AQSG_CUDA_TRY(cudaGetLastError());
+    }
+    return AQSG_OK;
+}
+
+int launch_tile_plan_multi(void* sv0, uint64_t reg_stride, int members, const TilePlan& plan, const void* dev0,
+                           uint64_t dev_stride, cudaStream_t stream, uint64_t* launches) {
+    if (plan.dtype != AQSG_C64 || plan.any_tc)
+        return set_error(AQSG_ERR_RUNTIME, "Grouped tile passes take plain complex64 plans");
+    const int n = plan.n;
+    constexpr int EPT = (1 << 12) / 256;
+    auto kplain = k_tile_stream_multi<float, EPT, false>;
+    auto kplain_k = k_tile_stream_multi<float, EPT, true>;
+    for (const TilePass& p : plan.passes) {
+        if (p.m != 12 || p.m == n) return set_error(AQSG_ERR_RUNTIME, "Grouped tile passes take streaming plans");
+        TileGeom geo;
+        std::memset(&geo, 0, sizeof(geo));
+        geo.n = n;
+        geo.m = p.m;
+        geo.L = p.L;
+        for (int i = 0; i < p.m; ++i) geo.tbits[i] = p.tbits[i];
+        const uint32_t size = 1u << geo.m;
+        const size_t shm = sizeof(float2) * size + (size_t(1) << (geo.m - geo.L)) * sizeof(uint64_t);
+        const uint32_t tiles = 1u << (n - geo.m);
+        const uint64_t blocks = (uint64_t)tiles * (uint64_t)members;
+        if (blocks > 0x7fffffffull) return set_error(AQSG_ERR_RUNTIME, "Too many tiles in one grouped pass");
+        (p.matk ? kplain_k : kplain)<<<(unsigned)blocks, 256, shm, stream>>>(
+            (float2*)sv0, reg_stride, geo, (const unsigned char*)dev0, dev_stride, p.first, (int)p.count,
+            plan.pool_offset(), tiles);
         if (launches) ++*launches;
         AQSG_CUDA_TRY(cudaGetLastError());
     }

@@ -78,3 +78,25 @@ def test_batch_update_and_alone_vs_mix(gpu_ctx):
     with pytest.raises(aq.InvalidArgument):
         b.update(new[:-1] + [(new[-1][0], new[-1][1][:-1])])
     b.free()
+
+
+def test_batch_groups_of_equal_structure(gpu_ctx):
+    """Large registers with the same structure run as one group (one launch
+    per tile pass for all of them): each matches the oracle and equals the
+    same circuit run alone."""
+    rng = np.random.default_rng(21)
+    shapes = [(15, 3)] * 5 + [(16, 2)] * 3 + [(11, 2), (9, 3)]
+    items = [(n, circuits.vqe_ops_array(n, L, rng.uniform(-np.pi, np.pi, size=(L, n, 2)))) for n, L in shapes]
+    b = aq.Batch(gpu_ctx, items)
+    z, zz = b.run()
+    for (n, ops), zi, zzi in zip(items, z, zz):
+        wz, wzz = oracle_z(n, ops)
+        assert np.max(np.abs(zi - wz)) < 1e-5
+        assert np.max(np.abs(zzi - wzz)) < 1e-5
+    for k in (0, 4, 6):
+        n, ops = items[k]
+        alone = aq.Batch(gpu_ctx, [(n, ops)])
+        za, _ = alone.run()
+        assert np.max(np.abs(za[0] - z[k])) < 1e-12
+        alone.free()
+    b.free()
