@@ -162,6 +162,9 @@ int run_plan_async(aqsg_state_s* st, const TilePlan& plan, const void* dev_table
 // aqsg_autotune, optionally without the one-gate-per-pass candidate.
 int autotune_impl(aqsg_ctx ctx, int n, int dtype, const aqsg_op* ops, int count, int reps, bool tiled_only,
                   aqsg_tune_entry* best, aqsg_tune_entry* all, int capacity, int* count_out);
+// Fusion width for a batched large register, timed as a group of replicas
+// on the CUDA cores (cached per context and structure).
+int autotune_grouped(aqsg_ctx ctx, int n, const aqsg_op* ops, int count, int* fuse_out);
 // Drop the autotuner's cached choices of a context (it is shutting down).
 void autotune_forget(aqsg_ctx ctx);
 // The fused op list of a compiled program.

@@ -238,16 +238,15 @@ static int encode_batch(aqsg_batch_s* b, const aqsg_circuit* cs, bool first_time
         const int cls = class_of(ci.n);
         int fuse = 0, tc = 0;
         if (cls < 0) {
-            // large register: run as the autotuner finds fastest for its
-            // structure (cached per structure, so equal structures tune once
-            // and a circuit runs the same way alone and in any batch)
+            // large register: the fusion width the grouped tuner finds
+            // fastest for its structure (timed as the batch runs it, over a
+            // replica count that depends on n only, and cached per structure,
+            // so a circuit runs the same way alone and in any batch)
             if (first_time) {
-                aqsg_tune_entry best;
-                if (int rc = autotune_impl(b->ctx, ci.n, AQSG_C64, ci.ops, ci.count, 1, true, &best, nullptr, 0,
-                                           nullptr))
-                    return rc;
-                b->fuse.push_back(best.fuse_qubits);
-                b->tc.push_back(best.tensor_cores);
+                int best_fuse = 0;
+                if (int rc = autotune_grouped(b->ctx, ci.n, ci.ops, ci.count, &best_fuse)) return rc;
+                b->fuse.push_back(best_fuse);
+                b->tc.push_back(0);
             }
             fuse = b->fuse[li];
             tc = b->tc[li];

@@ -362,29 +362,47 @@ __device__ __noinline__ void matk_apply(T* s, uint32_t size, uint32_t nthr, cons
             if ((r >> (K - 1 - i)) & 1) off |= tb[i];
         return off;
     };
-    for (uint32_t p = threadIdx.x; p < (size >> K); p += nthr) {
-        uint32_t j = p;
+    // G groups per thread and step share each matrix element load (small K)
+    constexpr int G = K <= 3 ? 2 : 1;
+    const uint32_t groups = size >> K;
+    for (uint32_t p0 = threadIdx.x; p0 < groups; p0 += G * nthr) {
+        uint32_t jg[G];
+        bool on[G];
+        T v[G][D];
 #pragma unroll
-        for (int i = 0; i < K; ++i) j = ins0(j, srt[i]);
-        if ((j & cm) != cv) continue;
-        T v[D];
+        for (int g = 0; g < G; ++g) {
+            const uint32_t p = p0 + g * nthr;
+            uint32_t j = p;
 #pragma unroll
-        for (int r = 0; r < D; ++r) v[r] = s[LAY::at(j | off_of(r))];
+            for (int i = 0; i < K; ++i) j = ins0(j, srt[i]);
+            jg[g] = j;
+            on[g] = p < groups && (j & cm) == cv;
+#pragma unroll
+            for (int r = 0; r < D; ++r) v[g][r] = on[g] ? s[LAY::at(j | off_of(r))] : T{};
+        }
 #pragma unroll 1
         for (int r = 0; r < D; ++r) {
-            T acc;
-            acc.x = 0;
-            acc.y = 0;
+            T acc[G];
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                acc[g].x = 0;
+                acc[g].y = 0;
+            }
 #pragma unroll
             for (int c = 0; c < D; ++c) {
                 const T mm = mat[r * D + c];
-                acc.x += mm.x * v[c].x - mm.y * v[c].y;
-                acc.y += mm.x * v[c].y + mm.y * v[c].x;
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    acc[g].x += mm.x * v[g][c].x - mm.y * v[g][c].y;
+                    acc[g].y += mm.x * v[g][c].y + mm.y * v[g][c].x;
+                }
             }
             uint32_t off = 0;
             for (int i = 0; i < K; ++i)
                 if ((r >> (K - 1 - i)) & 1) off |= tb[i];
-            s[LAY::at(j | off)] = acc;
+#pragma unroll
+            for (int g = 0; g < G; ++g)
+                if (on[g]) s[LAY::at(jg[g] | off)] = acc[g];
         }
     }
 }

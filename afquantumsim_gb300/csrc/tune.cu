@@ -160,3 +160,113 @@ int autotune_impl(aqsg_ctx ctx, int n, int dtype, const aqsg_op* ops, int count,
 }
 
 }  // namespace aqsg
+
+namespace aqsg {
+
+// Fusion width for a large register of the batched engine, timed the way the
+// batch runs it: the plain (CUDA-core) tile plan over a group of replicas
+// whose size depends only on n (so the choice does not depend on the rest of
+// the batch), one launch per pass.  Cached per context and structure.
+int autotune_grouped(aqsg_ctx ctx, int n, const aqsg_op* ops, int count, int* fuse_out) {
+    if (int rc = aqsg_check_ops(n, ops, count)) return rc;
+    const uint64_t key = structure_hash(n, AQSG_C64, ops, count) ^ 0xC2B2AE3D27D4EB4Full;
+    TuneCache& cache = tune_cache();
+    {
+        std::lock_guard<std::mutex> g(cache.mu);
+        auto it = cache.best.find({(const void*)ctx, key});
+        if (it != cache.best.end()) {
+            *fuse_out = it->second.fuse_qubits;
+            return AQSG_OK;
+        }
+    }
+    if (n < 13 || n > 30) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Grouped tuning takes 13 to 30 qubits");
+    const int replicas = n >= 22 ? 1 : (1 << (22 - n));
+    const uint64_t amps = 1ull << n;
+    void* regs = nullptr;
+    void* tables = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    AQSG_CUDA_TRY(cudaSetDevice(ctx->device));
+    int rc = AQSG_OK;
+    cudaError_t e = cudaMalloc(&regs, (size_t)replicas * amps * 8);
+    if (e == cudaSuccess) e = cudaMemsetAsync(regs, 0, (size_t)replicas * amps * 8, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e != cudaSuccess) rc = cuda_error(e, "autotune_grouped");
+    double best_ms = 1e300;
+    int best_fuse = 0;
+    size_t table_cap = 0;
+    for (int fuse : {0, 2, 3, 4, 5}) {
+        if (rc != AQSG_OK) break;
+        std::vector<LOp> low;
+        if (fuse > 0) {
+            aqsg_program p = nullptr;
+            if ((rc = aqsg_compile(n, AQSG_C64, ops, count, fuse, &p))) break;
+            low = program_ops(p);
+            aqsg_program_free(p);
+        } else {
+            for (int i = 0; i < count && rc == AQSG_OK; ++i) {
+                LOp o;
+                rc = lower_op(n, AQSG_C64, ops[i], &o);
+                if (rc == AQSG_OK && o.cls != L_NOP) low.push_back(std::move(o));
+            }
+            if (rc) break;
+        }
+        TilePlan plan;
+        if ((rc = encode_tiled(n, AQSG_C64, low, false, &plan, false))) break;
+        const size_t stride = (plan.pool_offset() + plan.pool.size() + 255) & ~size_t(255);
+        if (stride * replicas > table_cap) {
+            if (tables) cudaFree(tables);
+            table_cap = stride * replicas;
+            if ((e = cudaMalloc(&tables, table_cap)) != cudaSuccess) {
+                tables = nullptr;
+                rc = cuda_error(e, "autotune_grouped");
+                break;
+            }
+        }
+        for (int r = 0; r < replicas && e == cudaSuccess; ++r) {
+            char* dst = (char*)tables + (size_t)r * stride;
+            e = cudaMemcpyAsync(dst, plan.table.data(), plan.table.size(), cudaMemcpyHostToDevice, ctx->stream);
+            if (e == cudaSuccess && !plan.pool.empty())
+                e = cudaMemcpyAsync(dst + plan.pool_offset(), plan.pool.data(), plan.pool.size(),
+                                    cudaMemcpyHostToDevice, ctx->stream);
+        }
+        if (e != cudaSuccess) {
+            rc = cuda_error(e, "autotune_grouped");
+            break;
+        }
+        uint64_t launches = 0;
+        if ((rc = launch_tile_plan_multi(regs, amps, replicas, plan, tables, stride, ctx->stream, &launches))) break;
+        cudaEventRecord(e0, ctx->stream);
+        if ((rc = launch_tile_plan_multi(regs, amps, replicas, plan, tables, stride, ctx->stream, &launches))) break;
+        cudaEventRecord(e1, ctx->stream);
+        if ((e = cudaEventSynchronize(e1)) != cudaSuccess) {
+            rc = cuda_error(e, "autotune_grouped");
+            break;
+        }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best_ms) {
+            best_ms = ms;
+            best_fuse = fuse;
+        }
+    }
+    cudaStreamSynchronize(ctx->stream);
+    if (tables) cudaFree(tables);
+    if (regs) cudaFree(regs);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (rc != AQSG_OK) return rc;
+    aqsg_tune_entry en;
+    std::memset(&en, 0, sizeof(en));
+    en.exec_mode = AQSG_EXEC_TILED;
+    en.fuse_qubits = best_fuse;
+    en.ms = best_ms / replicas;
+    {
+        std::lock_guard<std::mutex> g(cache.mu);
+        cache.best[{(const void*)ctx, key}] = en;
+    }
+    *fuse_out = best_fuse;
+    return AQSG_OK;
+}
+
+}  // namespace aqsg

@@ -299,10 +299,12 @@ typedef struct aqsg_batch_s* aqsg_batch;
  * parameter set) to a whole sweep.  Registers of up to 14 qubits run
  * entirely in shared memory (a persistent kernel per size class, one CTA per
  * circuit); larger ones (up to 30) run as tile passes over one reused device
- * register, each compiled with the fusion width (and tensor-core use) that
- * the autotuner picks for its structure (tile passes only; cached per
- * structure, so a circuit runs the same way alone and in any batch).  The
- * whole run is captured once as a CUDA graph. */
+ * register, each compiled with the fusion width the autotuner picks for its
+ * structure, timed the way the batch runs it: registers of equal structure
+ * run as a group, one launch per tile pass for all of them (the choice is
+ * cached per structure and timed over a group size that depends on n only,
+ * so a circuit runs the same way alone and in any batch).  The whole run is
+ * captured once as a CUDA graph. */
 int aqsg_batch_create(aqsg_ctx ctx, const aqsg_circuit* circuits, int count, aqsg_batch* out);
 
 /* Swap in new parameters (angles, matrices): the same count, qubit counts,
