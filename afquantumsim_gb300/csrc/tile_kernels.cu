@@ -276,7 +276,6 @@ k_stream_tc(float2* __restrict__ sv, const TileGeom g, const TileOp* __restrict_
         // the cp.async copies this warp started have landed (a wound-down
         // CTA may leave some unconsumed)
         asm volatile("cp.async.wait_all;" ::: "memory");
-        bulk_wait_all();
     } else {
         // ---- compute warps ----
         TcSmem tcs;

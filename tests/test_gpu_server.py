@@ -97,3 +97,37 @@ def test_server_rejects_bad_requests():
     srv.close()
     with pytest.raises(aq.InvalidArgument):
         aq.Server(0, aq.C64, 1 << 10, 2, 12, 64)  # budget below one 12-qubit register
+
+
+def test_server_c128_zero_shots_and_late_submit(gpu_ctx):
+    """complex128 server; a request with no shots completes; requests
+    submitted after start with arrival -1 are admitted at once."""
+    srv = aq.Server(0, aq.C128, 1 << 24, 2, 16, 64)
+    srv.start()
+    reqs = requests(4, seed=31, n_range=(6, 16), depth_range=(2, 4))
+    tickets = [srv.submit(r["n"], r["ops"], 64 if k else 0, r["seed"], -1.0, 0) for k, r in enumerate(reqs)]
+    srv.wait_idle(120)
+    done = {d["ticket"]: d for d in srv.poll(16)}
+    assert set(done) == set(tickets) and all(d["status"] == 0 for d in done.values())
+    assert done[tickets[0]]["outcomes"].size == 0
+    for k in range(1, 4):  # same draws as the direct complex128 path
+        r = reqs[k]
+        with aq.State(gpu_ctx, r["n"], aq.C128) as st:
+            st.set_basis(0)
+            st.apply(r["ops"], aq.EXEC_TILED)
+            want = st.sample_seeded(r["seed"], 64)
+        np.testing.assert_array_equal(done[tickets[k]]["outcomes"], want)
+    srv.close()
+
+
+def test_server_close_with_queued_requests():
+    """Requests still queued (arrival far in the future) are dropped on
+    close; the call returns promptly."""
+    import time
+    srv = aq.Server(0, aq.C64, 1 << 22, 1, 12, 8)
+    for k in range(5):
+        srv.submit(10, circuits.brickwork(10, 2, seed=k), 8, k, 3600.0, 0)
+    srv.start()
+    t0 = time.perf_counter()
+    srv.close()
+    assert time.perf_counter() - t0 < 5.0
