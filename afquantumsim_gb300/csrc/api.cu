@@ -18,6 +18,8 @@ int set_error(int code, const std::string& msg) {
     return code;
 }
 
+std::string last_error_message() { return g_last_error; }
+
 int cuda_error(cudaError_t e, const char* where) {
     std::string msg = std::string("CUDA error ") + cudaGetErrorName(e) + " (" +
                       cudaGetErrorString(e) + ") at " + where;

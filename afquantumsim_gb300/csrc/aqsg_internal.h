@@ -14,6 +14,7 @@ namespace aqsg {
 
 // ---- errors ---------------------------------------------------------------
 int set_error(int code, const std::string& msg);
+std::string last_error_message();  // this thread's last set_error text
 int cuda_error(cudaError_t e, const char* where);
 #define AQSG_CUDA_TRY(expr)                                     \
     do {                                                        \

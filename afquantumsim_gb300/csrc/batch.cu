@@ -12,10 +12,12 @@
 // sequence is captured once; aqsg_batch_update swaps in new angles without
 // re-planning, and aqsg_batch_run replays the graph.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
-#include <vector>
-
 #include <map>
+#include <string>
+#include <thread>
+#include <vector>
 
 #include "tile_device.cuh"
 
@@ -213,7 +215,54 @@ int launch_expz_raw_multi(const void* sv0, uint64_t reg_stride, int members, int
                           const uint64_t* out_off, double* out_base, cudaStream_t stream);
 size_t expz_partial_doubles(int n);
 
-// Lower and encode every circuit; fills the host-side tables of b.
+// Lower one circuit (fused at the given width, or gate by gate) and encode
+// it as tile passes.  Host-only and independent of every other circuit.
+static int encode_circuit(const aqsg_circuit& ci, int fuse, bool tc, TilePlan* plan) {
+    std::vector<LOp> low;
+    if (fuse > 0) {
+        aqsg_program p = nullptr;
+        if (int rc = aqsg_compile(ci.n, AQSG_C64, ci.ops, ci.count, fuse, &p)) return rc;
+        low = program_ops(p);
+        aqsg_program_free(p);
+    } else {
+        low.reserve(ci.count);
+        for (int k = 0; k < ci.count; ++k) {
+            LOp o;
+            if (int rc = lower_op(ci.n, AQSG_C64, ci.ops[k], &o)) return rc;
+            if (o.cls != L_NOP) low.push_back(std::move(o));
+        }
+    }
+    // the tensor-core choice may not depend on parameter values, so that an
+    // update keeps the captured graph's shape
+    return encode_tiled(ci.n, AQSG_C64, low, tc, plan, false);
+}
+
+// Run body(i) for i in [0, count) on up to hardware_concurrency threads,
+// in chunks claimed from an atomic counter.
+template <class F>
+static void parallel_for(int count, F body) {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int threads = (int)std::min<unsigned>(hw, (unsigned)std::max(1, count / 16));
+    std::atomic<int> next{0};
+    auto work = [&]() {
+        for (;;) {
+            const int at = next.fetch_add(16);
+            if (at >= count) return;
+            const int end = std::min(count, at + 16);
+            for (int i = at; i < end; ++i) body(i);
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < threads; ++t) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
+}
+
+// Lower and encode every circuit; fills the host-side tables of b.  The
+// first call also tunes each large structure (on the GPU, serially); the
+// per-circuit lowering and encoding then run on all host threads, and the
+// tables are assembled in circuit order, so the result does not depend on
+// the thread count.
 static int encode_batch(aqsg_batch_s* b, const aqsg_circuit* cs, bool first_time) {
     for (int c = 0; c < 3; ++c) {
         b->small_table[c].clear();
@@ -229,45 +278,44 @@ static int encode_batch(aqsg_batch_s* b, const aqsg_circuit* cs, bool first_time
         b->fuse.clear();
         b->tc.clear();
     }
-    size_t li = 0;
-    std::vector<size_t> seen(3, 0);
+    // validation, and (first call) the tuned fusion width of each large
+    // register: the width the grouped tuner finds fastest for its structure
+    // (timed as the batch runs it, over a replica count that depends on n
+    // only, and cached per structure, so a circuit runs the same way alone
+    // and in any batch)
+    std::vector<int> large_index(b->count, -1);
+    int nlarge = 0;
     for (int i = 0; i < b->count; ++i) {
         const aqsg_circuit& ci = cs[i];
         if (ci.n != b->n[i]) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Batch structure changed (qubit count)");
         if (int rc = aqsg_check_ops(ci.n, ci.ops, ci.count)) return rc;
-        const int cls = class_of(ci.n);
-        int fuse = 0, tc = 0;
-        if (cls < 0) {
-            // large register: the fusion width the grouped tuner finds
-            // fastest for its structure (timed as the batch runs it, over a
-            // replica count that depends on n only, and cached per structure,
-            // so a circuit runs the same way alone and in any batch)
-            if (first_time) {
-                int best_fuse = 0;
-                if (int rc = autotune_grouped(b->ctx, ci.n, ci.ops, ci.count, &best_fuse)) return rc;
-                b->fuse.push_back(best_fuse);
-                b->tc.push_back(0);
-            }
-            fuse = b->fuse[li];
-            tc = b->tc[li];
+        if (class_of(ci.n) >= 0) continue;
+        large_index[i] = nlarge++;
+        if (first_time) {
+            int best_fuse = 0;
+            if (int rc = autotune_grouped(b->ctx, ci.n, ci.ops, ci.count, &best_fuse)) return rc;
+            b->fuse.push_back(best_fuse);
+            b->tc.push_back(0);
         }
-        std::vector<LOp> low;
-        if (fuse > 0) {
-            aqsg_program p = nullptr;
-            if (int rc = aqsg_compile(ci.n, AQSG_C64, ci.ops, ci.count, fuse, &p)) return rc;
-            low = program_ops(p);
-            aqsg_program_free(p);
-        } else {
-            for (int k = 0; k < ci.count; ++k) {
-                LOp o;
-                if (int rc = lower_op(ci.n, AQSG_C64, ci.ops[k], &o)) return rc;
-                if (o.cls != L_NOP) low.push_back(std::move(o));
-            }
-        }
-        TilePlan plan;
-        // the tensor-core choice may not depend on parameter values, so that
-        // an update keeps the captured graph's shape
-        if (int rc = encode_tiled(ci.n, AQSG_C64, low, tc != 0, &plan, false)) return rc;
+    }
+    // per-circuit lowering and encoding on all host threads
+    std::vector<TilePlan> plans(b->count);
+    std::vector<int> rcs(b->count, AQSG_OK);
+    std::vector<std::string> msgs(b->count);
+    parallel_for(b->count, [&](int i) {
+        const int li = large_index[i];
+        const int fuse = li >= 0 ? b->fuse[li] : 0;
+        const bool tc = li >= 0 && b->tc[li] != 0;
+        rcs[i] = encode_circuit(cs[i], fuse, tc, &plans[i]);
+        if (rcs[i]) msgs[i] = last_error_message();
+    });
+    for (int i = 0; i < b->count; ++i)
+        if (rcs[i]) return set_error(rcs[i], msgs[i]);
+    // assemble the tables in circuit order
+    std::vector<size_t> seen(3, 0);
+    for (int i = 0; i < b->count; ++i) {
+        const int cls = class_of(cs[i].n);
+        TilePlan& plan = plans[i];
         if (cls >= 0) {
             // one whole-register pass; append its ops to the class table with
             // their pool offsets shifted to the class pool
@@ -279,7 +327,7 @@ static int encode_batch(aqsg_batch_s* b, const aqsg_circuit* cs, bool first_time
             for (size_t at = 0; at < plan.table.size(); at += tsz) {
                 TileOp t;
                 std::memcpy(&t, &plan.table[at], tsz);
-                if (t.cls == L_MATK) {
+                if (t.cls == L_MATK || t.cls == T_RMATK) {
                     t.mat += (int32_t)pbase;
                     if (first_time) b->class_matk[cls] = true;
                 }
@@ -290,7 +338,7 @@ static int encode_batch(aqsg_batch_s* b, const aqsg_circuit* cs, bool first_time
             const int nops = (int)(plan.table.size() / tsz);
             if (first_time) {
                 SmallItem it;
-                it.n = ci.n;
+                it.n = cs[i].n;
                 it.nops = nops;
                 it.op_first = first;
                 it.out = (uint32_t)b->out_off[i];
@@ -303,6 +351,7 @@ static int encode_batch(aqsg_batch_s* b, const aqsg_circuit* cs, bool first_time
             }
             seen[cls]++;
         } else {
+            const int li = large_index[i];
             if (first_time) {
                 b->large.push_back(i);
                 b->plans.push_back(std::move(plan));
@@ -314,7 +363,6 @@ static int encode_batch(aqsg_batch_s* b, const aqsg_circuit* cs, bool first_time
                 old.table = std::move(plan.table);
                 old.pool = std::move(plan.pool);
             }
-            ++li;
         }
     }
     return AQSG_OK;

@@ -397,6 +397,252 @@ __device__ __noinline__ void matk_apply(T* s, uint32_t size, uint32_t nthr, cons
     }
 }
 
+// ---- register phases -------------------------------------------------------------
+//
+// A register phase applies a run of ops with one shared-memory round trip:
+// the tile is split into slots of 2^RB amplitudes that differ only in the
+// phase's RB register bits; a thread loads a slot into registers, applies
+// every op of the run to it and stores it back.  Ops whose target bits are
+// register bits (2x2 gates, permutations, k <= RB dense unitaries) act
+// within the slot; diagonal ops act on any bits.  Controls on the slot's
+// other bits are one test per thread, controls on register bits a per-slot
+// mask the host precomputes.  Table layout: a header (cls T_RPHASE, k = ops
+// in the run, lt0 = RB, am_loc = the register bits' tile positions,
+// cm_loc = the tile position of each slot-index bit, 4 bits each), then the
+// run's ops in register form:
+//   T_RMAT2  2x2 on register bit lt0, coefficients (type T) in m, pad & 1:
+//            real coefficients
+//   T_RPERM  swap pairs on register bit lt0 where the control holds and
+//            the OR condition holds: (slot index & am_loc) != 0, or
+//            (base & am_ext) != 0, or the pair's register bits are in
+//            ltb[3] (PERM_X: ltb[3] = all)
+//   T_RSWAP  exchange register bits lt0 < lt1 (pairs with bit lt0 = 0 and
+//            lt1 = 1 against their partner)
+//   T_RDIAG  multiply by m[0] (or by m[1] where the target bit is 1: target
+//            a register bit (pad & 2, mask ltb[3]), a slot-index position
+//            lt0 >= 0, or a bit outside the tile ext_t >= 0)
+//   T_RMATK  2^k x 2^k unitary, k = 2 or 3 (type T, row-major, at pool
+//            offset mat) on the register bits of mask ltb[0]; matrix index
+//            bit i = the i-th lowest of those bits
+// Every register-form op: cm_ext/cv_ext as usual; cm_loc/cv_loc the control
+// on slot-index bits (tile positions); ltb[4] the mask of slot elements (the
+// pair's or group's element with its target bits 0) whose register-bit
+// control holds.
+enum TileCls : int { T_RPHASE = 8, T_RMAT2 = 9, T_RPERM = 10, T_RSWAP = 11, T_RDIAG = 12, T_RMATK = 13 };
+
+// Shared-memory position of tile element j with the low S bits XORed with
+// the XOR of the higher S-bit groups: the 2^S elements a half warp (c64,
+// S = 4) or a quarter warp (c128, S = 3) touches at once fall into distinct
+// banks whenever their varying index bits have distinct residues mod S.
+template <int S>
+struct SwzLay {
+    static __device__ __forceinline__ uint32_t at(uint32_t j) {
+        uint32_t f = 0;
+#pragma unroll
+        for (int sh = S; sh < 16; sh += S) f ^= j >> sh;
+        return j ^ (f & ((1u << S) - 1u));
+    }
+};
+
+template <typename T, int RB, int I>
+__device__ __forceinline__ void r_mat2(T (&v)[1 << RB], const T* c, uint32_t em, bool real) {
+    const T m00 = c[0], m01 = c[1], m10 = c[2], m11 = c[3];
+#pragma unroll
+    for (int e = 0; e < (1 << RB); ++e) {
+        if (e & (1 << I)) continue;
+        if (!((em >> e) & 1u)) continue;
+        const T a = v[e], b = v[e | (1 << I)];
+        if (real) {
+            v[e].x = m00.x * a.x + m01.x * b.x;
+            v[e].y = m00.x * a.y + m01.x * b.y;
+            v[e | (1 << I)].x = m10.x * a.x + m11.x * b.x;
+            v[e | (1 << I)].y = m10.x * a.y + m11.x * b.y;
+        } else {
+            v[e] = cmul2(m00, a, m01, b);
+            v[e | (1 << I)] = cmul2(m10, a, m11, b);
+        }
+    }
+}
+
+template <typename T, int RB, int I>
+__device__ __forceinline__ void r_perm(T (&v)[1 << RB], uint32_t pm) {
+#pragma unroll
+    for (int e = 0; e < (1 << RB); ++e) {
+        if (e & (1 << I)) continue;
+        const bool on = (pm >> e) & 1u;
+        const T a = v[e], b = v[e | (1 << I)];
+        v[e] = on ? b : a;
+        v[e | (1 << I)] = on ? a : b;
+    }
+}
+
+template <typename T, int RB, int I, int J>
+__device__ __forceinline__ void r_swap(T (&v)[1 << RB], uint32_t em) {
+#pragma unroll
+    for (int e = 0; e < (1 << RB); ++e) {
+        if ((e & (1 << I)) || !(e & (1 << J))) continue;
+        const int f = e ^ (1 << I) ^ (1 << J);
+        const bool on = (em >> e) & 1u;
+        const T a = v[e], b = v[f];
+        v[e] = on ? b : a;
+        v[f] = on ? a : b;
+    }
+}
+
+template <int RM, int K>
+__device__ __forceinline__ constexpr int r_dep(int r) {  // matrix index -> slot element bits
+    int out = 0, bit = 0;
+    for (int b = 0; b < 8; ++b)
+        if ((RM >> b) & 1) {
+            if ((r >> bit) & 1) out |= 1 << b;
+            ++bit;
+        }
+    return out;
+}
+
+template <typename T, int RB, int RM>
+__device__ __forceinline__ void r_matk(T (&v)[1 << RB], const T* __restrict__ mat, uint32_t em) {
+    constexpr int K = __builtin_popcount(RM), D = 1 << K, E = 1 << RB;
+    T a[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) a[e] = v[e];
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+        T row[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) row[c] = mat[r * D + c];
+#pragma unroll
+        for (int e0 = 0; e0 < E; ++e0) {
+            if (e0 & RM) continue;
+            if (!((em >> e0) & 1u)) continue;
+            T acc;
+            acc.x = 0;
+            acc.y = 0;
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                const T x = a[e0 | r_dep<RM, K>(c)];
+                acc.x += row[c].x * x.x - row[c].y * x.y;
+                acc.y += row[c].x * x.y + row[c].y * x.x;
+            }
+            v[e0 | r_dep<RM, K>(r)] = acc;
+        }
+    }
+}
+
+// One register phase: hp[0] the header, hp[1..k] its ops.  LAY must be
+// linear over GF(2) (the identity or SwzLay): the position of slot element
+// e is then at(jt) ^ at(e's register bits), an XOR of per-bit offsets.
+template <typename T, int RB, class LAY, bool MATK>
+__device__ __forceinline__ void rphase_run(T* s, uint32_t size, uint32_t nthr, uint64_t base,
+                                           const TileOp* __restrict__ hp, const unsigned char* __restrict__ pool) {
+    constexpr int E = 1 << RB;
+    constexpr uint32_t ALL = (1u << E) - 1u;
+    const int nops = hp[0].k;
+    const uint64_t rpos = hp[0].am_loc, tpos = hp[0].cm_loc;
+    const int tbits = 31 - __clz(size) - RB;
+    uint32_t bo[RB];  // byte offset of each register bit under LAY
+#pragma unroll
+    for (int i = 0; i < RB; ++i) bo[i] = LAY::at(1u << ((rpos >> (4 * i)) & 15u)) * (uint32_t)sizeof(T);
+    unsigned char* sb = reinterpret_cast<unsigned char*>(s);
+    auto off_of = [&](uint32_t ajt, int e) {
+        uint32_t o = ajt;
+#pragma unroll
+        for (int i = 0; i < RB; ++i)
+            if ((e >> i) & 1) o ^= bo[i];
+        return o;
+    };
+    for (uint32_t slot = threadIdx.x; slot < (size >> RB); slot += nthr) {
+        uint32_t jt = 0;
+        for (int i = 0; i < tbits; ++i) jt |= ((slot >> i) & 1u) << ((tpos >> (4 * i)) & 15u);
+        const uint32_t ajt = LAY::at(jt) * (uint32_t)sizeof(T);
+        T v[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e) v[e] = *reinterpret_cast<const T*>(sb + off_of(ajt, e));
+        for (int q = 1; q <= nops; ++q) {
+            const TileOp& op = hp[q];
+            if ((base & op.cm_ext) != op.cv_ext) continue;
+            if ((jt & (uint32_t)op.cm_loc) != (uint32_t)op.cv_loc) continue;
+            const uint32_t em = (uint32_t)op.ltb[4];
+            const T* c = reinterpret_cast<const T*>(op.m);
+            switch (op.cls) {
+                case T_RMAT2: {
+                    const bool real = op.pad & 1;
+                    switch (op.lt0) {
+                        case 0: r_mat2<T, RB, 0>(v, c, em, real); break;
+                        case 1: r_mat2<T, RB, 1>(v, c, em, real); break;
+                        case 2: r_mat2<T, RB, 2>(v, c, em, real); break;
+                        default: if constexpr (RB > 3) r_mat2<T, RB, RB - 1>(v, c, em, real); break;
+                    }
+                    break;
+                }
+                case T_RPERM: {
+                    const bool or_t = ((jt & (uint32_t)op.am_loc) != 0u) || ((base & op.am_ext) != 0ull);
+                    const uint32_t pm = em & (or_t ? ALL : (uint32_t)op.ltb[3]);
+                    switch (op.lt0) {
+                        case 0: r_perm<T, RB, 0>(v, pm); break;
+                        case 1: r_perm<T, RB, 1>(v, pm); break;
+                        case 2: r_perm<T, RB, 2>(v, pm); break;
+                        default: if constexpr (RB > 3) r_perm<T, RB, RB - 1>(v, pm); break;
+                    }
+                    break;
+                }
+                case T_RSWAP:
+                    switch (op.lt0 * 4 + op.lt1) {
+                        case 0 * 4 + 1: r_swap<T, RB, 0, 1>(v, em); break;
+                        case 0 * 4 + 2: r_swap<T, RB, 0, 2>(v, em); break;
+                        case 1 * 4 + 2: r_swap<T, RB, 1, 2>(v, em); break;
+                        default:
+                            if constexpr (RB > 3) {
+                                switch (op.lt0 * 4 + op.lt1) {
+                                    case 0 * 4 + 3: r_swap<T, RB, 0, RB - 1>(v, em); break;
+                                    case 1 * 4 + 3: r_swap<T, RB, 1, RB - 1>(v, em); break;
+                                    default: r_swap<T, RB, 2, RB - 1>(v, em); break;
+                                }
+                            }
+                            break;
+                    }
+                    break;
+                case T_RDIAG: {
+                    uint32_t wm = 0;
+                    if (op.pad & 2) wm = (uint32_t)op.ltb[3];
+                    else if (op.lt0 >= 0) wm = ((jt >> op.lt0) & 1u) ? ALL : 0u;
+                    else if (op.ext_t >= 0) wm = ((base >> op.ext_t) & 1ull) ? ALL : 0u;
+                    const T c0 = c[0], c1 = c[1];
+#pragma unroll
+                    for (int e = 0; e < E; ++e)
+                        if ((em >> e) & 1u) v[e] = cmul(((wm >> e) & 1u) ? c1 : c0, v[e]);
+                    break;
+                }
+                default:
+                    if constexpr (MATK) {
+                        const T* mat = reinterpret_cast<const T*>(pool + op.mat);
+                        switch (op.ltb[0]) {
+                            case 0x3: r_matk<T, RB, 0x3>(v, mat, em); break;
+                            case 0x5: r_matk<T, RB, 0x5>(v, mat, em); break;
+                            case 0x6: r_matk<T, RB, 0x6>(v, mat, em); break;
+                            case 0x7: r_matk<T, RB, 0x7>(v, mat, em); break;
+                            default:
+                                if constexpr (RB > 3) {
+                                    switch (op.ltb[0]) {
+                                        case 0x9: r_matk<T, RB, 0x9>(v, mat, em); break;
+                                        case 0xA: r_matk<T, RB, 0xA>(v, mat, em); break;
+                                        case 0xC: r_matk<T, RB, 0xC>(v, mat, em); break;
+                                        case 0xB: r_matk<T, RB, 0xB>(v, mat, em); break;
+                                        case 0xD: r_matk<T, RB, 0xD>(v, mat, em); break;
+                                        default: r_matk<T, RB, 0xE>(v, mat, em); break;
+                                    }
+                                }
+                                break;
+                        }
+                    }
+                    break;
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < E; ++e) *reinterpret_cast<T*>(sb + off_of(ajt, e)) = v[e];
+    }
+}
+
 // Apply a pass's ops to the 2^m-amplitude tile s in shared memory (all
 // nthr threads that SYNC covers call this; EPT x nthr >= 2^m).  base = the
 // tile's global base index (its bits outside the tile).  With TC, ops the
@@ -405,7 +651,7 @@ __device__ __noinline__ void matk_apply(T* s, uint32_t size, uint32_t nthr, cons
 // consecutive diagonal
 // ops runs from registers: each thread keeps the same EPT elements for the
 // whole run, so the run costs one shared-memory round trip and one barrier.
-template <typename R, int EPT, bool TC, class LAY, class SYNC = CtaSync, bool MATK = true>
+template <typename R, int EPT, bool TC, class LAY, class SYNC = CtaSync, bool MATK = true, bool RPH = !TC>
 __device__ __forceinline__ void tile_run_ops(typename Cx<R>::T* s, uint32_t size, uint32_t nthr, uint64_t base,
                                              const TileOp* __restrict__ ops, int nops,
                                              const unsigned char* __restrict__ pool, const TcSmem* tcs,
@@ -414,6 +660,14 @@ __device__ __forceinline__ void tile_run_ops(typename Cx<R>::T* s, uint32_t size
     for (int oi = 0; oi < nops;) {
         const TileOp& op = ops[oi];
         const int cls = op.cls;
+        if constexpr (RPH) {
+            if (cls == T_RPHASE) {
+                rphase_run<T, (sizeof(R) == 4 ? 4 : 3), LAY, MATK>(s, size, nthr, base, ops + oi, pool);
+                SYNC::sync();
+                oi += 1 + op.k;
+                continue;
+            }
+        }
         if (cls == L_DIAG1 || cls == L_DIAG2) {
             T reg[EPT];
 #pragma unroll

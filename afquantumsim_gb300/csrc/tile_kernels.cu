@@ -26,6 +26,11 @@ int tile_max_bits(int dtype) { return dtype == AQSG_C64 ? 14 : 13; }
 static int stream_tile_bits(int dtype) { return dtype == AQSG_C64 ? 12 : 11; }
 static int row_bits(int dtype) { return dtype == AQSG_C64 ? 5 : 4; }
 
+// Shared-memory layout of the CUDA-core tile kernels: XOR-swizzled in groups
+// of 4 index bits (complex64: 16 x 8 B = the 32 banks) or 3 (complex128).
+template <typename R>
+using TileSwz = SwzLay<sizeof(R) == 4 ? 4 : 3>;
+
 // Whole-register passes (n <= 14 c64 / 13 c128): one CTA holds the register.
 // EPT: elements per thread in register runs; MATK: the pass has dense
 // k-qubit ops on CUDA cores.
@@ -34,22 +39,28 @@ __global__ void __launch_bounds__(512, 1)
 k_tile(typename Cx<R>::T* __restrict__ sv, const TileGeom g, const TileOp* __restrict__ ops, int nops,
        const unsigned char* __restrict__ pool) {
     using T = typename Cx<R>::T;
+    using LAY = TileSwz<R>;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     const uint32_t size = 1u << g.m;
     T* s = reinterpret_cast<T*>(smem_raw);
     if constexpr (sizeof(R) == 4) {
-        for (uint32_t i = threadIdx.x; i < (size >> 1); i += blockDim.x)
-            reinterpret_cast<float4*>(s)[i] = __ldcs(reinterpret_cast<const float4*>(sv) + i);
+        for (uint32_t i = threadIdx.x; i < (size >> 1); i += blockDim.x) {
+            const float4 x = __ldcs(reinterpret_cast<const float4*>(sv) + i);
+            s[LAY::at(2 * i)] = make_float2(x.x, x.y);
+            s[LAY::at(2 * i + 1)] = make_float2(x.z, x.w);
+        }
     } else {
-        for (uint32_t j = threadIdx.x; j < size; j += blockDim.x) s[j] = __ldcs(sv + j);
+        for (uint32_t j = threadIdx.x; j < size; j += blockDim.x) s[LAY::at(j)] = __ldcs(sv + j);
     }
     __syncthreads();
-    tile_run_ops<R, EPT, false, FlatLay, CtaSync, MATK>(s, size, blockDim.x, 0, ops, nops, pool, nullptr, nullptr);
+    tile_run_ops<R, EPT, false, LAY, CtaSync, MATK>(s, size, blockDim.x, 0, ops, nops, pool, nullptr, nullptr);
     if constexpr (sizeof(R) == 4) {
-        for (uint32_t i = threadIdx.x; i < (size >> 1); i += blockDim.x)
-            __stcs(reinterpret_cast<float4*>(sv) + i, reinterpret_cast<const float4*>(s)[i]);
+        for (uint32_t i = threadIdx.x; i < (size >> 1); i += blockDim.x) {
+            const float2 a = s[LAY::at(2 * i)], b = s[LAY::at(2 * i + 1)];
+            __stcs(reinterpret_cast<float4*>(sv) + i, make_float4(a.x, a.y, b.x, b.y));
+        }
     } else {
-        for (uint32_t j = threadIdx.x; j < size; j += blockDim.x) __stcs(sv + j, s[j]);
+        for (uint32_t j = threadIdx.x; j < size; j += blockDim.x) __stcs(sv + j, s[LAY::at(j)]);
     }
 }
 
@@ -63,6 +74,7 @@ __device__ __forceinline__ void tile_stream_body(typename Cx<R>::T* __restrict__
                                                  const TileOp* __restrict__ ops, int nops,
                                                  const unsigned char* __restrict__ pool, uint64_t tile) {
     using T = typename Cx<R>::T;
+    using LAY = TileSwz<R>;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     const int m = g.m, L = g.L;
     const uint32_t size = 1u << m;
@@ -86,28 +98,31 @@ __device__ __forceinline__ void tile_stream_body(typename Cx<R>::T* __restrict__
         for (uint32_t i = threadIdx.x; i < (size >> 1); i += blockDim.x) {
             const uint32_t j = i << 1;
             const uint64_t gi = base + rowoff[j >> L] + (j & (rowlen - 1));
-            reinterpret_cast<float4*>(s)[i] = __ldcs(reinterpret_cast<const float4*>(sv) + (gi >> 1));
+            const float4 x = __ldcs(reinterpret_cast<const float4*>(sv) + (gi >> 1));
+            s[LAY::at(j)] = make_float2(x.x, x.y);
+            s[LAY::at(j + 1)] = make_float2(x.z, x.w);
         }
     } else {
         for (uint32_t j = threadIdx.x; j < size; j += blockDim.x)
-            s[j] = __ldcs(sv + base + rowoff[j >> L] + (j & (rowlen - 1)));
+            s[LAY::at(j)] = __ldcs(sv + base + rowoff[j >> L] + (j & (rowlen - 1)));
     }
     __syncthreads();
-    tile_run_ops<R, EPT, false, FlatLay, CtaSync, MATK>(s, size, blockDim.x, base, ops, nops, pool, nullptr, nullptr);
+    tile_run_ops<R, EPT, false, LAY, CtaSync, MATK>(s, size, blockDim.x, base, ops, nops, pool, nullptr, nullptr);
     if constexpr (sizeof(R) == 4) {
         for (uint32_t i = threadIdx.x; i < (size >> 1); i += blockDim.x) {
             const uint32_t j = i << 1;
             const uint64_t gi = base + rowoff[j >> L] + (j & (rowlen - 1));
-            __stcs(reinterpret_cast<float4*>(sv) + (gi >> 1), reinterpret_cast<const float4*>(s)[i]);
+            const float2 a = s[LAY::at(j)], b = s[LAY::at(j + 1)];
+            __stcs(reinterpret_cast<float4*>(sv) + (gi >> 1), make_float4(a.x, a.y, b.x, b.y));
         }
     } else {
         for (uint32_t j = threadIdx.x; j < size; j += blockDim.x)
-            __stcs(sv + base + rowoff[j >> L] + (j & (rowlen - 1)), s[j]);
+            __stcs(sv + base + rowoff[j >> L] + (j & (rowlen - 1)), s[LAY::at(j)]);
     }
 }
 
 template <typename R, int EPT, bool MATK>
-__global__ void __launch_bounds__(256, MATK ? 2 : 3)
+__global__ void __launch_bounds__(256, 2)
 k_tile_stream(typename Cx<R>::T* __restrict__ sv, const TileGeom g, const TileOp* __restrict__ ops, int nops,
               const unsigned char* __restrict__ pool) {
     tile_stream_body<R, EPT, MATK>(sv, g, ops, nops, pool, blockIdx.x);
@@ -119,7 +134,7 @@ k_tile_stream(typename Cx<R>::T* __restrict__ sv, const TileGeom g, const TileOp
 // whose op table + operand pool start dev_stride bytes after the previous
 // one's (the batched engine's groups of equal-structure circuits).
 template <typename R, int EPT, bool MATK>
-__global__ void __launch_bounds__(256, MATK ? 2 : 3)
+__global__ void __launch_bounds__(256, 2)
 k_tile_stream_multi(typename Cx<R>::T* __restrict__ sv0, uint64_t reg_stride, const TileGeom g,
                     const unsigned char* __restrict__ dev0, uint64_t dev_stride, uint32_t op_first, int nops,
                     uint64_t pool_off, uint32_t tiles) {
@@ -561,6 +576,209 @@ static void tc_tables(TileOp& t, std::vector<unsigned char>& blob) {
 }
 
 // Encode the passes of `ops` into a table of TileOps and an operand pool.
+// ---- register phases (host side) ------------------------------------------------
+//
+// Runs of consecutive ops of a CUDA-core pass become register phases (see
+// tile_device.cuh): a run grows while the union of the register bits its
+// ops need stays within RB (2x2 gates and permutations need their targets,
+// dense unitaries of k <= 3 qubits their k bits, diagonal ops none).  Dense
+// unitaries of more qubits stay single ops on the shared-memory path.
+constexpr int kPhaseMinSlotBits = 5;  // at least 32 slots (one warp) per tile
+
+static int phase_reg_bits(int dtype) { return dtype == AQSG_C64 ? 4 : 3; }
+
+static bool reg_needs(const TileOp& t, int rb, uint32_t* need) {
+    switch (t.cls) {
+        case L_DIAG1:
+        case L_DIAG2: *need = 0; return true;
+        case L_MAT2:
+        case L_PERM_X:
+        case L_PERM_OR: *need = 1u << t.lt0; return true;
+        case L_PERM_SWAP: *need = (1u << t.lt0) | (1u << t.lt1); return true;
+        case L_MATK: {
+            if (t.pad || t.k > 3 || t.k > rb) return false;
+            uint32_t b = 0;
+            for (int j = 0; j < t.k; ++j) b |= 1u << t.ltb[j];
+            *need = b;
+            return true;
+        }
+        default: return false;
+    }
+}
+
+static std::vector<TileOp> register_phases(const std::vector<TileOp>& ops, int m, int dtype,
+                                           std::vector<unsigned char>& pool) {
+    const int rb = phase_reg_bits(dtype);
+    if (m < rb + kPhaseMinSlotBits || m > 15) return ops;
+    const uint32_t E = 1u << rb, ALL = (1u << E) - 1u;
+    std::vector<TileOp> out;
+    out.reserve(ops.size() + 8);
+    size_t i = 0;
+    while (i < ops.size()) {
+        uint32_t R = 0;
+        if (!reg_needs(ops[i], rb, &R)) {
+            out.push_back(ops[i++]);
+            continue;
+        }
+        size_t j = i + 1;
+        for (uint32_t nd; j < ops.size() && reg_needs(ops[j], rb, &nd) && __builtin_popcount(R | nd) <= rb; ++j)
+            R |= nd;
+        // pad the register bits with the highest free positions
+        for (int b = m - 1; b >= 0 && __builtin_popcount(R) < rb; --b) R |= 1u << b;
+        int rpos[8], rix[16];
+        for (int b = 0, c = 0; b < 16; ++b) {
+            rix[b] = -1;
+            if ((R >> b) & 1u) {
+                rix[b] = c;
+                rpos[c++] = b;
+            }
+        }
+        // slot-index bits: first one position of each residue mod rb (the
+        // bits a half / quarter warp varies fall into distinct banks under
+        // the swizzled layout), then the rest in ascending order
+        std::vector<int> tpos;
+        uint32_t used = 0, seen_res = 0;
+        for (int b = 0; b < m; ++b)
+            if (!((R >> b) & 1u) && !((seen_res >> (b % rb)) & 1u)) {
+                seen_res |= 1u << (b % rb);
+                used |= 1u << b;
+                tpos.push_back(b);
+            }
+        for (int b = 0; b < m; ++b)
+            if (!((R >> b) & 1u) && !((used >> b) & 1u)) tpos.push_back(b);
+        auto dep = [&](uint32_t e) {
+            uint32_t o = 0;
+            for (int q = 0; q < rb; ++q)
+                if ((e >> q) & 1u) o |= 1u << rpos[q];
+            return o;
+        };
+        TileOp h;
+        std::memset(&h, 0, sizeof(h));
+        h.cls = T_RPHASE;
+        h.k = (int32_t)(j - i);
+        h.lt0 = rb;
+        h.ext_t = -1;
+        for (int q = 0; q < rb; ++q) h.am_loc |= (uint64_t)rpos[q] << (4 * q);
+        for (size_t q = 0; q < tpos.size(); ++q) h.cm_loc |= (uint64_t)tpos[q] << (4 * q);
+        out.push_back(h);
+        for (size_t q = i; q < j; ++q) {
+            const TileOp& t = ops[q];
+            TileOp r = t;
+            const uint32_t cm = (uint32_t)t.cm_loc, cv = (uint32_t)t.cv_loc;
+            r.cm_loc = cm & ~R;
+            r.cv_loc = cv & ~R;
+            auto ctl = [&](uint32_t idx) { return (idx & cm & R) == (cv & R); };
+            uint32_t em = 0;
+            for (uint32_t e = 0; e < E; ++e)
+                if (ctl(dep(e))) em |= 1u << e;
+            r.ltb[4] = (int32_t)em;
+            auto store_coef = [&](int count) {  // coefficients as the kernel's complex type
+                if (dtype != AQSG_C64) return;
+                float f[16] = {};
+                for (int c = 0; c < 2 * count; ++c) f[c] = (float)t.m[c];
+                std::memset(r.m, 0, sizeof(r.m));
+                std::memcpy(r.m, f, sizeof(float) * 2 * count);
+            };
+            switch (t.cls) {
+                case L_MAT2: {
+                    r.cls = T_RMAT2;
+                    r.lt0 = rix[t.lt0];
+                    r.pad = (t.m[1] == 0.0 && t.m[3] == 0.0 && t.m[5] == 0.0 && t.m[7] == 0.0) ? 1 : 0;
+                    store_coef(4);
+                    break;
+                }
+                case L_PERM_X:
+                case L_PERM_OR: {
+                    r.cls = T_RPERM;
+                    r.lt0 = rix[t.lt0];
+                    if (t.cls == L_PERM_X) {
+                        r.am_loc = 0;
+                        r.am_ext = 0;
+                        r.ltb[3] = (int32_t)ALL;
+                    } else {
+                        const uint32_t am = (uint32_t)t.am_loc;
+                        r.am_loc = am & ~R;
+                        uint32_t om = 0;
+                        for (uint32_t e = 0; e < E; ++e)
+                            if (dep(e) & am & R) om |= 1u << e;
+                        r.ltb[3] = (int32_t)om;
+                    }
+                    break;
+                }
+                case L_PERM_SWAP: {
+                    r.cls = T_RSWAP;
+                    const int a = rix[t.lt0], b = rix[t.lt1];
+                    r.lt0 = a < b ? a : b;
+                    r.lt1 = a < b ? b : a;
+                    if (a > b) {  // the control is checked at (a = 0, b = 1)
+                        em = 0;
+                        for (uint32_t e = 0; e < E; ++e)
+                            if (ctl(dep(e ^ (1u << a) ^ (1u << b)))) em |= 1u << e;
+                        r.ltb[4] = (int32_t)em;
+                    }
+                    break;
+                }
+                case L_DIAG1:
+                case L_DIAG2: {
+                    r.cls = T_RDIAG;
+                    r.pad = 0;
+                    r.lt0 = -1;
+                    r.ext_t = -1;
+                    if (t.cls == L_DIAG2) {
+                        if (t.lt0 >= 0 && ((R >> t.lt0) & 1u)) {
+                            uint32_t wm = 0;
+                            for (uint32_t e = 0; e < E; ++e)
+                                if ((dep(e) >> t.lt0) & 1u) wm |= 1u << e;
+                            r.pad = 2;
+                            r.ltb[3] = (int32_t)wm;
+                        } else if (t.lt0 >= 0) {
+                            r.lt0 = t.lt0;
+                        } else {
+                            r.ext_t = t.ext_t;
+                        }
+                    }
+                    store_coef(2);
+                    break;
+                }
+                default: {  // L_MATK, k <= 3, all bits register bits
+                    r.cls = T_RMATK;
+                    const int k = t.k, D = 1 << k;
+                    int rmask = 0;
+                    for (int q2 = 0; q2 < k; ++q2) rmask |= 1 << rix[t.ltb[q2]];
+                    // old matrix bit (k-1-q2) <-> register index rix[ltb[q2]];
+                    // new matrix bit b <-> the b-th lowest register index
+                    int oldbit_of_new[8];
+                    for (int b = 0, c = 0; b < rb; ++b)
+                        if ((rmask >> b) & 1)
+                            for (int q2 = 0; q2 < k; ++q2)
+                                if (rix[t.ltb[q2]] == b) oldbit_of_new[c++] = k - 1 - q2;
+                    auto old_index = [&](int nidx) {
+                        int o = 0;
+                        for (int b = 0; b < k; ++b)
+                            if ((nidx >> b) & 1) o |= 1 << oldbit_of_new[b];
+                        return o;
+                    };
+                    const size_t esz = dtype == AQSG_C64 ? 8 : 16;
+                    std::vector<unsigned char> src(pool.begin() + t.mat, pool.begin() + t.mat + esz * D * D);
+                    for (int rr = 0; rr < D; ++rr)
+                        for (int cc = 0; cc < D; ++cc)
+                            std::memcpy(&pool[t.mat + esz * (rr * D + cc)],
+                                        &src[esz * (old_index(rr) * D + old_index(cc))], esz);
+                    r.ltb[0] = rmask;
+                    em = 0;
+                    for (uint32_t e = 0; e < E; ++e)
+                        if (!(e & (uint32_t)rmask) && ctl(dep(e))) em |= 1u << e;
+                    r.ltb[4] = (int32_t)em;
+                    break;
+                }
+            }
+            out.push_back(r);
+        }
+        i = j;
+    }
+    return out;
+}
+
 int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, TilePlan* plan, bool exact_perm) {
     plan->table.clear();
     plan->pool.clear();
@@ -584,6 +802,7 @@ int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, Tile
         for (size_t i = 0; i < p.bits.size(); ++i) local[p.bits[i]] = (int)i;
         const bool tc_pass = tc_on && dtype == AQSG_C64 && tp.m == kTcTileBits;
         std::vector<unsigned char> blob;  // this pass's tensor-core operands
+        std::vector<TileOp> pops;         // this pass's table
         for (const LOp* o : p.ops) {
             TileOp t;
             std::memset(&t, 0, sizeof(t));
@@ -628,6 +847,11 @@ int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, Tile
                     }
                 }
             }
+            pops.push_back(t);
+        }
+        // passes on the CUDA cores: runs of ops as register phases
+        if (!tp.tc) pops = register_phases(pops, tp.m, dtype, plan->pool);
+        for (const TileOp& t : pops) {
             const size_t at = plan->table.size();
             plan->table.resize(at + tsize);
             std::memcpy(&plan->table[at], &t, tsize);
