@@ -125,6 +125,7 @@ struct TilePlan {
 };
 // exact_perm: fused permutation matrices stay off the tensor cores (bit-exact
 // moves); false makes the choice depend on the op structure only.
+bool relocate_tile_matrices(unsigned char* table, size_t count, int32_t delta);
 int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, TilePlan* plan, bool exact_perm = true);
 // Launch the passes on `stream`; dev = device copy of table + pool.
 int launch_tile_plan(void* sv, const TilePlan& plan, const void* dev, cudaStream_t stream, int* d_err,

@@ -324,17 +324,11 @@ static int encode_batch(aqsg_batch_s* b, const aqsg_circuit* cs, bool first_time
             const size_t pbase = (b->small_pool[cls].size() + 255) & ~size_t(255);
             b->small_pool[cls].resize(pbase);
             b->small_pool[cls].insert(b->small_pool[cls].end(), plan.pool.begin(), plan.pool.end());
-            for (size_t at = 0; at < plan.table.size(); at += tsz) {
-                TileOp t;
-                std::memcpy(&t, &plan.table[at], tsz);
-                if (t.cls == L_MATK || t.cls == T_RMATK) {
-                    t.mat += (int32_t)pbase;
-                    if (first_time) b->class_matk[cls] = true;
-                }
-                const size_t w = b->small_table[cls].size();
-                b->small_table[cls].resize(w + tsz);
-                std::memcpy(&b->small_table[cls][w], &t, tsz);
-            }
+            const size_t w = b->small_table[cls].size();
+            b->small_table[cls].insert(b->small_table[cls].end(), plan.table.begin(), plan.table.end());
+            if (relocate_tile_matrices(&b->small_table[cls][w], plan.table.size() / tsz, (int32_t)pbase) &&
+                first_time)
+                b->class_matk[cls] = true;
             const int nops = (int)(plan.table.size() / tsz);
             if (first_time) {
                 SmallItem it;

@@ -403,37 +403,48 @@ __device__ __noinline__ void matk_apply(T* s, uint32_t size, uint32_t nthr, cons
 // the tile is split into slots of 2^RB amplitudes that differ only in the
 // phase's RB register bits; a thread loads a slot into registers, applies
 // every op of the run to it and stores it back.  Ops whose target bits are
-// register bits (2x2 gates, permutations, k <= RB dense unitaries) act
-// within the slot; diagonal ops act on any bits.  Controls on the slot's
-// other bits are one test per thread, controls on register bits a per-slot
-// mask the host precomputes.  Table layout: a header (cls T_RPHASE, k = ops
-// in the run, lt0 = RB, am_loc = the register bits' tile positions,
-// cm_loc = the tile position of each slot-index bit, 4 bits each), then the
-// run's ops in register form:
-//   T_RMAT2  2x2 on register bit lt0, coefficients (type T) in m, pad & 1:
-//            real coefficients
-//   T_RPERM  swap pairs on register bit lt0 where the control holds and
-//            the OR condition holds: (slot index & am_loc) != 0, or
-//            (base & am_ext) != 0, or the pair's register bits are in
-//            ltb[3] (PERM_X: ltb[3] = all)
-//   T_RSWAP  exchange register bits lt0 < lt1 (pairs with bit lt0 = 0 and
-//            lt1 = 1 against their partner)
-//   T_RDIAG  multiply by m[0] (or by m[1] where the target bit is 1: target
-//            a register bit (pad & 2, mask ltb[3]), a slot-index position
-//            lt0 >= 0, or a bit outside the tile ext_t >= 0)
-//   T_RMATK  2^k x 2^k unitary, k = 2 or 3 (type T, row-major, at pool
-//            offset mat) on the register bits of mask ltb[0]; matrix index
-//            bit i = the i-th lowest of those bits
-// Every register-form op: cm_ext/cv_ext as usual; cm_loc/cv_loc the control
-// on slot-index bits (tile positions); ltb[4] the mask of slot elements (the
-// pair's or group's element with its target bits 0) whose register-bit
-// control holds.
-enum TileCls : int { T_RPHASE = 8, T_RMAT2 = 9, T_RPERM = 10, T_RSWAP = 11, T_RDIAG = 12, T_RMATK = 13 };
+// register bits (2x2 gates, permutations, dense unitaries of 2 or 3 qubits)
+// act within the slot; diagonal ops act on any bits.  A control on the
+// slot's other bits is one test per thread; a control on register bits is a
+// mask of slot elements the host precomputes.
+//
+// Table layout: a header TileOp (cls T_RPHASE, k = ops in the run, lt0 = RB,
+// am_loc = tile position of each register bit, cm_loc = tile position of
+// each slot-index bit, 4 bits each), then k ROps in TileOp-sized slots.
+enum TileCls : int { T_RPHASE = 8 };
+
+enum RKind : uint32_t {
+    RK_MAT2C = 1,  // complex 2x2 on register bit a: coefficients c[0..3]
+    RK_MAT2R = 2,  // real 2x2 on register bit a: coefficients r[0..3] (floats of the kernel's type)
+    RK_PERM = 3,   // swap the pairs on register bit a (PERM_X / PERM_OR)
+    RK_SWAP = 4,   // exchange register bits a < b
+    RK_DIAG = 5,   // multiply by c[0], or by c[1] where a target outside the register bits is 1
+    RK_DIAGR = 6,  // multiply by c[0] / c[1] where register bit a is 0 / 1
+    RK_MATK = 7    // 2^k x 2^k unitary (k = 2, 3) on the register bits of mask a (bits 8-15)
+};
+constexpr uint32_t RF_EXT = 1u << 16;   // controls outside the tile (cm_ext / cv_ext)
+constexpr uint32_t RF_OR = 1u << 17;    // RK_PERM: OR condition (PERM_OR)
+constexpr uint32_t RF_TTHR = 1u << 18;  // RK_DIAG: target = slot-index position `extra`
+constexpr uint32_t RF_TEXT = 1u << 19;  // RK_DIAG: target = bit ext_t outside the tile
+
+struct ROp {
+    uint32_t code;    // kind | a << 8 | b << 12 | flags
+    uint32_t ctl;     // control on slot-index bits: tile-position mask (bits 0-15), value (16-31)
+    uint32_t em;      // slot elements (the pair's / group's element with target bits 0) whose
+                      // register-bit control holds (bits 0-15); RK_PERM: OR mask (16-31)
+    uint32_t extra;   // RK_MATK: pool offset of the matrix; RK_DIAG: target position
+    uint64_t cm_ext, cv_ext, am_ext;
+    int32_t ext_t;    // RK_DIAG with RF_TEXT: global target bit
+    uint32_t amt;     // RK_PERM with RF_OR: OR mask on slot-index bits (tile positions)
+    unsigned char coef[112];  // 16-byte aligned; complex values of the kernel's type
+};
+static_assert(sizeof(ROp) == sizeof(TileOp), "register ops overlay the op table");
 
 // Shared-memory position of tile element j with the low S bits XORed with
 // the XOR of the higher S-bit groups: the 2^S elements a half warp (c64,
 // S = 4) or a quarter warp (c128, S = 3) touches at once fall into distinct
 // banks whenever their varying index bits have distinct residues mod S.
+// The map is linear over GF(2).
 template <int S>
 struct SwzLay {
     static __device__ __forceinline__ uint32_t at(uint32_t j) {
@@ -444,49 +455,77 @@ struct SwzLay {
     }
 };
 
-template <typename T, int RB, int I>
-__device__ __forceinline__ void r_mat2(T (&v)[1 << RB], const T* c, uint32_t em, bool real) {
+template <bool P>
+__device__ __forceinline__ bool r_on(uint32_t em, int e) {
+    return !P || ((em >> e) & 1u);
+}
+
+template <typename T, int RB, int I, bool P>
+__device__ __forceinline__ void r_mat2c(T (&v)[1 << RB], const T* c, uint32_t em) {
     const T m00 = c[0], m01 = c[1], m10 = c[2], m11 = c[3];
 #pragma unroll
     for (int e = 0; e < (1 << RB); ++e) {
         if (e & (1 << I)) continue;
-        if (!((em >> e) & 1u)) continue;
+        if (!r_on<P>(em, e)) continue;
         const T a = v[e], b = v[e | (1 << I)];
-        if (real) {
-            v[e].x = m00.x * a.x + m01.x * b.x;
-            v[e].y = m00.x * a.y + m01.x * b.y;
-            v[e | (1 << I)].x = m10.x * a.x + m11.x * b.x;
-            v[e | (1 << I)].y = m10.x * a.y + m11.x * b.y;
-        } else {
-            v[e] = cmul2(m00, a, m01, b);
-            v[e | (1 << I)] = cmul2(m10, a, m11, b);
-        }
+        v[e] = cmul2(m00, a, m01, b);
+        v[e | (1 << I)] = cmul2(m10, a, m11, b);
     }
 }
 
-template <typename T, int RB, int I>
+template <typename T, typename R, int RB, int I, bool P>
+__device__ __forceinline__ void r_mat2r(T (&v)[1 << RB], const R* r, uint32_t em) {
+    const R m00 = r[0], m01 = r[1], m10 = r[2], m11 = r[3];
+#pragma unroll
+    for (int e = 0; e < (1 << RB); ++e) {
+        if (e & (1 << I)) continue;
+        if (!r_on<P>(em, e)) continue;
+        const T a = v[e], b = v[e | (1 << I)];
+        v[e].x = m00 * a.x + m01 * b.x;
+        v[e].y = m00 * a.y + m01 * b.y;
+        v[e | (1 << I)].x = m10 * a.x + m11 * b.x;
+        v[e | (1 << I)].y = m10 * a.y + m11 * b.y;
+    }
+}
+
+template <typename T, int RB, int I, bool P>
 __device__ __forceinline__ void r_perm(T (&v)[1 << RB], uint32_t pm) {
 #pragma unroll
     for (int e = 0; e < (1 << RB); ++e) {
         if (e & (1 << I)) continue;
-        const bool on = (pm >> e) & 1u;
+        const bool on = r_on<P>(pm, e);
         const T a = v[e], b = v[e | (1 << I)];
         v[e] = on ? b : a;
         v[e | (1 << I)] = on ? a : b;
     }
 }
 
-template <typename T, int RB, int I, int J>
+template <typename T, int RB, int I, int J, bool P>
 __device__ __forceinline__ void r_swap(T (&v)[1 << RB], uint32_t em) {
 #pragma unroll
     for (int e = 0; e < (1 << RB); ++e) {
         if ((e & (1 << I)) || !(e & (1 << J))) continue;
         const int f = e ^ (1 << I) ^ (1 << J);
-        const bool on = (em >> e) & 1u;
+        const bool on = r_on<P>(em, e);
         const T a = v[e], b = v[f];
         v[e] = on ? b : a;
         v[f] = on ? a : b;
     }
+}
+
+template <typename T, int RB, bool P>
+__device__ __forceinline__ void r_diag(T (&v)[1 << RB], T ph, uint32_t em) {
+#pragma unroll
+    for (int e = 0; e < (1 << RB); ++e)
+        if (r_on<P>(em, e)) v[e] = cmul(ph, v[e]);
+}
+
+template <typename T, int RB, int I, bool P>
+__device__ __forceinline__ void r_diagr(T (&v)[1 << RB], const T* c, uint32_t em) {
+    const T c0 = c[0], c1 = c[1];
+#pragma unroll
+    for (int e = 0; e < (1 << RB); ++e)
+        if (r_on<P>(em, e)) v[e] = cmul(((e >> I) & 1) ? c1 : c0, v[e]);
 }
 
 template <int RM, int K>
@@ -529,17 +568,42 @@ __device__ __forceinline__ void r_matk(T (&v)[1 << RB], const T* __restrict__ ma
     }
 }
 
-// One register phase: hp[0] the header, hp[1..k] its ops.  LAY must be
+// Dispatch of a per-register-bit template over a runtime bit index a < RB
+// and the predicated / unpredicated variant.
+#define AQSG_R_BIT(RB, a, pred, CALL)                                   \
+    do {                                                                \
+        if (pred) {                                                     \
+            constexpr bool P_ = true;                                   \
+            switch (a) {                                                \
+                case 0: { constexpr int I_ = 0; CALL; } break;          \
+                case 1: { constexpr int I_ = 1; CALL; } break;          \
+                case 2: { constexpr int I_ = 2; CALL; } break;          \
+                default: if constexpr (RB > 3) { constexpr int I_ = RB > 3 ? 3 : 0; CALL; } break; \
+            }                                                           \
+        } else {                                                        \
+            constexpr bool P_ = false;                                  \
+            switch (a) {                                                \
+                case 0: { constexpr int I_ = 0; CALL; } break;          \
+                case 1: { constexpr int I_ = 1; CALL; } break;          \
+                case 2: { constexpr int I_ = 2; CALL; } break;          \
+                default: if constexpr (RB > 3) { constexpr int I_ = RB > 3 ? 3 : 0; CALL; } break; \
+            }                                                           \
+        }                                                               \
+    } while (0)
+
+// One register phase: hp[0] the header, hp[1..k] its ROps.  LAY must be
 // linear over GF(2) (the identity or SwzLay): the position of slot element
 // e is then at(jt) ^ at(e's register bits), an XOR of per-bit offsets.
 template <typename T, int RB, class LAY, bool MATK>
 __device__ __forceinline__ void rphase_run(T* s, uint32_t size, uint32_t nthr, uint64_t base,
                                            const TileOp* __restrict__ hp, const unsigned char* __restrict__ pool) {
+    using R = decltype(T{}.x);
     constexpr int E = 1 << RB;
     constexpr uint32_t ALL = (1u << E) - 1u;
     const int nops = hp[0].k;
     const uint64_t rpos = hp[0].am_loc, tpos = hp[0].cm_loc;
     const int tbits = 31 - __clz(size) - RB;
+    const ROp* __restrict__ rops = reinterpret_cast<const ROp*>(hp + 1);
     uint32_t bo[RB];  // byte offset of each register bit under LAY
 #pragma unroll
     for (int i = 0; i < RB; ++i) bo[i] = LAY::at(1u << ((rpos >> (4 * i)) & 15u)) * (uint32_t)sizeof(T);
@@ -558,72 +622,93 @@ __device__ __forceinline__ void rphase_run(T* s, uint32_t size, uint32_t nthr, u
         T v[E];
 #pragma unroll
         for (int e = 0; e < E; ++e) v[e] = *reinterpret_cast<const T*>(sb + off_of(ajt, e));
-        for (int q = 1; q <= nops; ++q) {
-            const TileOp& op = hp[q];
-            if ((base & op.cm_ext) != op.cv_ext) continue;
-            if ((jt & (uint32_t)op.cm_loc) != (uint32_t)op.cv_loc) continue;
-            const uint32_t em = (uint32_t)op.ltb[4];
-            const T* c = reinterpret_cast<const T*>(op.m);
-            switch (op.cls) {
-                case T_RMAT2: {
-                    const bool real = op.pad & 1;
-                    switch (op.lt0) {
-                        case 0: r_mat2<T, RB, 0>(v, c, em, real); break;
-                        case 1: r_mat2<T, RB, 1>(v, c, em, real); break;
-                        case 2: r_mat2<T, RB, 2>(v, c, em, real); break;
-                        default: if constexpr (RB > 3) r_mat2<T, RB, RB - 1>(v, c, em, real); break;
-                    }
+        for (int q = 0; q < nops; ++q) {
+            const ROp* op = rops + q;
+            const uint4 hd = *reinterpret_cast<const uint4*>(op);
+            const uint32_t code = hd.x;
+            if (code & RF_EXT) {
+                if ((base & op->cm_ext) != op->cv_ext) continue;
+            }
+            if ((jt & (hd.y & 0xFFFFu)) != (hd.y >> 16)) continue;
+            const uint32_t em = hd.z & ALL;
+            const bool pred = em != ALL;
+            const int a = (code >> 8) & 15;
+            const T* c = reinterpret_cast<const T*>(op->coef);
+            switch (code & 0xFFu) {
+                case RK_MAT2C: AQSG_R_BIT(RB, a, pred, (r_mat2c<T, RB, I_, P_>(v, c, em))); break;
+                case RK_MAT2R: {
+                    const R* rc = reinterpret_cast<const R*>(op->coef);
+                    AQSG_R_BIT(RB, a, pred, (r_mat2r<T, R, RB, I_, P_>(v, rc, em)));
                     break;
                 }
-                case T_RPERM: {
-                    const bool or_t = ((jt & (uint32_t)op.am_loc) != 0u) || ((base & op.am_ext) != 0ull);
-                    const uint32_t pm = em & (or_t ? ALL : (uint32_t)op.ltb[3]);
-                    switch (op.lt0) {
-                        case 0: r_perm<T, RB, 0>(v, pm); break;
-                        case 1: r_perm<T, RB, 1>(v, pm); break;
-                        case 2: r_perm<T, RB, 2>(v, pm); break;
-                        default: if constexpr (RB > 3) r_perm<T, RB, RB - 1>(v, pm); break;
+                case RK_PERM: {
+                    uint32_t pm = em;
+                    if (code & RF_OR) {
+                        const bool or_t = ((jt & op->amt) != 0u) || ((base & op->am_ext) != 0ull);
+                        pm = em & (or_t ? ALL : (hd.z >> 16));
                     }
+                    AQSG_R_BIT(RB, a, pm != ALL, (r_perm<T, RB, I_, P_>(v, pm)));
                     break;
                 }
-                case T_RSWAP:
-                    switch (op.lt0 * 4 + op.lt1) {
-                        case 0 * 4 + 1: r_swap<T, RB, 0, 1>(v, em); break;
-                        case 0 * 4 + 2: r_swap<T, RB, 0, 2>(v, em); break;
-                        case 1 * 4 + 2: r_swap<T, RB, 1, 2>(v, em); break;
-                        default:
-                            if constexpr (RB > 3) {
-                                switch (op.lt0 * 4 + op.lt1) {
-                                    case 0 * 4 + 3: r_swap<T, RB, 0, RB - 1>(v, em); break;
-                                    case 1 * 4 + 3: r_swap<T, RB, 1, RB - 1>(v, em); break;
-                                    default: r_swap<T, RB, 2, RB - 1>(v, em); break;
+                case RK_SWAP: {
+                    const int b = (code >> 12) & 15;
+                    if (pred) {
+                        switch (a * 4 + b) {
+                            case 0 * 4 + 1: r_swap<T, RB, 0, 1, true>(v, em); break;
+                            case 0 * 4 + 2: r_swap<T, RB, 0, 2, true>(v, em); break;
+                            case 1 * 4 + 2: r_swap<T, RB, 1, 2, true>(v, em); break;
+                            default:
+                                if constexpr (RB > 3) {
+                                    constexpr int H = RB > 3 ? 3 : 0;
+                                    switch (a) {
+                                        case 0: r_swap<T, RB, 0, H, true>(v, em); break;
+                                        case 1: r_swap<T, RB, 1, H, true>(v, em); break;
+                                        default: r_swap<T, RB, 2, H, true>(v, em); break;
+                                    }
                                 }
-                            }
-                            break;
+                                break;
+                        }
+                    } else {
+                        switch (a * 4 + b) {
+                            case 0 * 4 + 1: r_swap<T, RB, 0, 1, false>(v, em); break;
+                            case 0 * 4 + 2: r_swap<T, RB, 0, 2, false>(v, em); break;
+                            case 1 * 4 + 2: r_swap<T, RB, 1, 2, false>(v, em); break;
+                            default:
+                                if constexpr (RB > 3) {
+                                    constexpr int H = RB > 3 ? 3 : 0;
+                                    switch (a) {
+                                        case 0: r_swap<T, RB, 0, H, false>(v, em); break;
+                                        case 1: r_swap<T, RB, 1, H, false>(v, em); break;
+                                        default: r_swap<T, RB, 2, H, false>(v, em); break;
+                                    }
+                                }
+                                break;
+                        }
                     }
                     break;
-                case T_RDIAG: {
-                    uint32_t wm = 0;
-                    if (op.pad & 2) wm = (uint32_t)op.ltb[3];
-                    else if (op.lt0 >= 0) wm = ((jt >> op.lt0) & 1u) ? ALL : 0u;
-                    else if (op.ext_t >= 0) wm = ((base >> op.ext_t) & 1ull) ? ALL : 0u;
-                    const T c0 = c[0], c1 = c[1];
-#pragma unroll
-                    for (int e = 0; e < E; ++e)
-                        if ((em >> e) & 1u) v[e] = cmul(((wm >> e) & 1u) ? c1 : c0, v[e]);
+                }
+                case RK_DIAG: {
+                    bool one = false;
+                    if (code & RF_TTHR) one = (jt >> hd.w) & 1u;
+                    else if (code & RF_TEXT) one = (base >> op->ext_t) & 1ull;
+                    const T ph = one ? c[1] : c[0];
+                    if (pred) r_diag<T, RB, true>(v, ph, em);
+                    else r_diag<T, RB, false>(v, ph, em);
                     break;
                 }
+                case RK_DIAGR: AQSG_R_BIT(RB, a, pred, (r_diagr<T, RB, I_, P_>(v, c, em))); break;
                 default:
                     if constexpr (MATK) {
-                        const T* mat = reinterpret_cast<const T*>(pool + op.mat);
-                        switch (op.ltb[0]) {
+                        const T* mat = reinterpret_cast<const T*>(pool + hd.w);
+                        const int rm = (code >> 8) & 0xFF;
+                        switch (rm) {
                             case 0x3: r_matk<T, RB, 0x3>(v, mat, em); break;
                             case 0x5: r_matk<T, RB, 0x5>(v, mat, em); break;
                             case 0x6: r_matk<T, RB, 0x6>(v, mat, em); break;
                             case 0x7: r_matk<T, RB, 0x7>(v, mat, em); break;
                             default:
                                 if constexpr (RB > 3) {
-                                    switch (op.ltb[0]) {
+                                    switch (rm) {
                                         case 0x9: r_matk<T, RB, 0x9>(v, mat, em); break;
                                         case 0xA: r_matk<T, RB, 0xA>(v, mat, em); break;
                                         case 0xC: r_matk<T, RB, 0xC>(v, mat, em); break;
@@ -642,6 +727,7 @@ __device__ __forceinline__ void rphase_run(T* s, uint32_t size, uint32_t nthr, u
         for (int e = 0; e < E; ++e) *reinterpret_cast<T*>(sb + off_of(ajt, e)) = v[e];
     }
 }
+#undef AQSG_R_BIT
 
 // Apply a pass's ops to the 2^m-amplitude tile s in shared memory (all
 // nthr threads that SYNC covers call this; EPT x nthr >= 2^m).  base = the

@@ -663,85 +663,96 @@ static std::vector<TileOp> register_phases(const std::vector<TileOp>& ops, int m
         out.push_back(h);
         for (size_t q = i; q < j; ++q) {
             const TileOp& t = ops[q];
-            TileOp r = t;
+            ROp r;
+            std::memset(&r, 0, sizeof(r));
             const uint32_t cm = (uint32_t)t.cm_loc, cv = (uint32_t)t.cv_loc;
-            r.cm_loc = cm & ~R;
-            r.cv_loc = cv & ~R;
+            r.ctl = (cm & ~R) | ((cv & ~R) << 16);
+            r.cm_ext = t.cm_ext;
+            r.cv_ext = t.cv_ext;
+            r.ext_t = -1;
+            uint32_t flags = t.cm_ext ? RF_EXT : 0u;
             auto ctl = [&](uint32_t idx) { return (idx & cm & R) == (cv & R); };
             uint32_t em = 0;
             for (uint32_t e = 0; e < E; ++e)
                 if (ctl(dep(e))) em |= 1u << e;
-            r.ltb[4] = (int32_t)em;
-            auto store_coef = [&](int count) {  // coefficients as the kernel's complex type
-                if (dtype != AQSG_C64) return;
-                float f[16] = {};
-                for (int c = 0; c < 2 * count; ++c) f[c] = (float)t.m[c];
-                std::memset(r.m, 0, sizeof(r.m));
-                std::memcpy(r.m, f, sizeof(float) * 2 * count);
+            auto put_complex = [&](int count) {  // t.m[0 .. 2 count) as the kernel's complex type
+                if (dtype == AQSG_C64) {
+                    float f[8];
+                    for (int c = 0; c < 2 * count; ++c) f[c] = (float)t.m[c];
+                    std::memcpy(r.coef, f, sizeof(float) * 2 * count);
+                } else {
+                    std::memcpy(r.coef, t.m, sizeof(double) * 2 * count);
+                }
             };
+            uint32_t kind = 0, ra = 0, rbb = 0;
             switch (t.cls) {
                 case L_MAT2: {
-                    r.cls = T_RMAT2;
-                    r.lt0 = rix[t.lt0];
-                    r.pad = (t.m[1] == 0.0 && t.m[3] == 0.0 && t.m[5] == 0.0 && t.m[7] == 0.0) ? 1 : 0;
-                    store_coef(4);
+                    ra = (uint32_t)rix[t.lt0];
+                    const bool real = t.m[1] == 0.0 && t.m[3] == 0.0 && t.m[5] == 0.0 && t.m[7] == 0.0;
+                    if (real) {
+                        kind = RK_MAT2R;
+                        if (dtype == AQSG_C64) {
+                            const float f[4] = {(float)t.m[0], (float)t.m[2], (float)t.m[4], (float)t.m[6]};
+                            std::memcpy(r.coef, f, sizeof(f));
+                        } else {
+                            const double d[4] = {t.m[0], t.m[2], t.m[4], t.m[6]};
+                            std::memcpy(r.coef, d, sizeof(d));
+                        }
+                    } else {
+                        kind = RK_MAT2C;
+                        put_complex(4);
+                    }
                     break;
                 }
                 case L_PERM_X:
                 case L_PERM_OR: {
-                    r.cls = T_RPERM;
-                    r.lt0 = rix[t.lt0];
-                    if (t.cls == L_PERM_X) {
-                        r.am_loc = 0;
-                        r.am_ext = 0;
-                        r.ltb[3] = (int32_t)ALL;
-                    } else {
+                    kind = RK_PERM;
+                    ra = (uint32_t)rix[t.lt0];
+                    if (t.cls == L_PERM_OR) {
+                        flags |= RF_OR;
+                        if (t.am_ext) flags |= RF_EXT;
                         const uint32_t am = (uint32_t)t.am_loc;
-                        r.am_loc = am & ~R;
+                        r.amt = am & ~R;
+                        r.am_ext = t.am_ext;
                         uint32_t om = 0;
                         for (uint32_t e = 0; e < E; ++e)
                             if (dep(e) & am & R) om |= 1u << e;
-                        r.ltb[3] = (int32_t)om;
+                        em |= om << 16;
                     }
                     break;
                 }
                 case L_PERM_SWAP: {
-                    r.cls = T_RSWAP;
-                    const int a = rix[t.lt0], b = rix[t.lt1];
-                    r.lt0 = a < b ? a : b;
-                    r.lt1 = a < b ? b : a;
-                    if (a > b) {  // the control is checked at (a = 0, b = 1)
+                    kind = RK_SWAP;
+                    const int a2 = rix[t.lt0], b2 = rix[t.lt1];
+                    ra = (uint32_t)(a2 < b2 ? a2 : b2);
+                    rbb = (uint32_t)(a2 < b2 ? b2 : a2);
+                    if (a2 > b2) {  // the control is checked at (a = 0, b = 1)
                         em = 0;
                         for (uint32_t e = 0; e < E; ++e)
-                            if (ctl(dep(e ^ (1u << a) ^ (1u << b)))) em |= 1u << e;
-                        r.ltb[4] = (int32_t)em;
+                            if (ctl(dep(e ^ (1u << a2) ^ (1u << b2)))) em |= 1u << e;
                     }
                     break;
                 }
                 case L_DIAG1:
                 case L_DIAG2: {
-                    r.cls = T_RDIAG;
-                    r.pad = 0;
-                    r.lt0 = -1;
-                    r.ext_t = -1;
+                    kind = RK_DIAG;
+                    put_complex(2);
                     if (t.cls == L_DIAG2) {
                         if (t.lt0 >= 0 && ((R >> t.lt0) & 1u)) {
-                            uint32_t wm = 0;
-                            for (uint32_t e = 0; e < E; ++e)
-                                if ((dep(e) >> t.lt0) & 1u) wm |= 1u << e;
-                            r.pad = 2;
-                            r.ltb[3] = (int32_t)wm;
+                            kind = RK_DIAGR;
+                            ra = (uint32_t)rix[t.lt0];
                         } else if (t.lt0 >= 0) {
-                            r.lt0 = t.lt0;
+                            flags |= RF_TTHR;
+                            r.extra = (uint32_t)t.lt0;
                         } else {
+                            flags |= RF_TEXT;
                             r.ext_t = t.ext_t;
                         }
                     }
-                    store_coef(2);
                     break;
                 }
                 default: {  // L_MATK, k <= 3, all bits register bits
-                    r.cls = T_RMATK;
+                    kind = RK_MATK;
                     const int k = t.k, D = 1 << k;
                     int rmask = 0;
                     for (int q2 = 0; q2 < k; ++q2) rmask |= 1 << rix[t.ltb[q2]];
@@ -764,19 +775,52 @@ static std::vector<TileOp> register_phases(const std::vector<TileOp>& ops, int m
                         for (int cc = 0; cc < D; ++cc)
                             std::memcpy(&pool[t.mat + esz * (rr * D + cc)],
                                         &src[esz * (old_index(rr) * D + old_index(cc))], esz);
-                    r.ltb[0] = rmask;
+                    ra = (uint32_t)rmask;
+                    r.extra = (uint32_t)t.mat;
                     em = 0;
                     for (uint32_t e = 0; e < E; ++e)
                         if (!(e & (uint32_t)rmask) && ctl(dep(e))) em |= 1u << e;
-                    r.ltb[4] = (int32_t)em;
                     break;
                 }
             }
-            out.push_back(r);
+            if (r.ext_t >= 0) flags |= RF_EXT;
+            r.code = kind | (ra << 8) | (rbb << 12) | flags;
+            r.em = em;
+            TileOp slot;
+            std::memcpy(&slot, &r, sizeof(slot));
+            out.push_back(slot);
         }
         i = j;
     }
     return out;
+}
+
+// Shift the pool offsets of a pass table's dense matrices by delta (tables
+// moved into a larger pool); returns whether the table has any.
+bool relocate_tile_matrices(unsigned char* table, size_t count, int32_t delta) {
+    bool any = false;
+    for (size_t q = 0; q < count; ++q) {
+        TileOp t;
+        std::memcpy(&t, table + q * sizeof(TileOp), sizeof(TileOp));
+        if (t.cls == T_RPHASE) {
+            for (int k = 0; k < t.k; ++k) {
+                ROp r;
+                unsigned char* at = table + (q + 1 + k) * sizeof(TileOp);
+                std::memcpy(&r, at, sizeof(ROp));
+                if ((r.code & 0xFFu) == RK_MATK) {
+                    r.extra += (uint32_t)delta;
+                    any = true;
+                    std::memcpy(at, &r, sizeof(ROp));
+                }
+            }
+            q += (size_t)t.k;
+        } else if (t.cls == L_MATK) {
+            t.mat += delta;
+            any = true;
+            std::memcpy(table + q * sizeof(TileOp), &t, sizeof(TileOp));
+        }
+    }
+    return any;
 }
 
 int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, TilePlan* plan, bool exact_perm) {
