@@ -154,9 +154,9 @@ struct SmallKernel {
 
 static SmallKernel small_kernel(int c, bool matk) {
     switch (c) {
-        case 0: return {matk ? k_batch_small<8, 128, true> : k_batch_small<8, 128, false>, 128};
-        case 1: return {matk ? k_batch_small<16, 256, true> : k_batch_small<16, 256, false>, 256};
-        default: return {matk ? k_batch_small<32, 512, true> : k_batch_small<32, 512, false>, 512};
+        case 0: return {matk ? k_batch_small<2, 128, true> : k_batch_small<2, 128, false>, 128};
+        case 1: return {matk ? k_batch_small<2, 256, true> : k_batch_small<2, 256, false>, 256};
+        default: return {matk ? k_batch_small<2, 512, true> : k_batch_small<2, 512, false>, 512};
     }
 }
 

@@ -894,7 +894,16 @@ int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, Tile
             pops.push_back(t);
         }
         // passes on the CUDA cores: runs of ops as register phases
-        if (!tp.tc) pops = register_phases(pops, tp.m, dtype, plan->pool);
+        if (!tp.tc) {
+            pops = register_phases(pops, tp.m, dtype, plan->pool);
+            // the kernels size their diagonal runs for tiles without phases
+            if (tp.m >= phase_reg_bits(dtype) + kPhaseMinSlotBits)
+                for (size_t q = 0; q < pops.size(); ++q) {
+                    if (pops[q].cls == T_RPHASE) q += (size_t)pops[q].k;  // skip the phase's ROps
+                    else if (pops[q].cls == L_DIAG1 || pops[q].cls == L_DIAG2)
+                        return set_error(AQSG_ERR_RUNTIME, "Diagonal op outside a register phase");
+                }
+        }
         for (const TileOp& t : pops) {
             const size_t at = plan->table.size();
             plan->table.resize(at + tsize);
@@ -952,7 +961,10 @@ static int launch_plan_t(void* sv, const TilePlan& plan, const void* dev, cudaSt
     const int n = plan.n;
     const TileOp* dops = (const TileOp*)dev;
     const unsigned char* dpool = (const unsigned char*)dev + plan.pool_offset();
-    constexpr int EPT_WHOLE = sizeof(R) == 4 ? 32 : 16;  // 2^14 / 512, 2^13 / 512
+    // whole registers: register phases cover every diagonal op once the
+    // register has 2^(RB + kPhaseMinSlotBits) amplitudes; below that the
+    // diagonal runs need 2 elements per thread (threads >= size / 2)
+    constexpr int EPT_WHOLE = 2;
     constexpr int M_STREAM = sizeof(R) == 4 ? 12 : 11;
     auto kwhole = k_tile<R, EPT_WHOLE, false>;
     auto kwhole_k = k_tile<R, EPT_WHOLE, true>;
@@ -986,7 +998,8 @@ static int launch_plan_t(void* sv, const TilePlan& plan, const void* dev, cudaSt
             k_stream_tc<<<grid, kTcCta, TcStreamSmem::kBytes, stream>>>((float2*)sv, geo, dops + p.first,
                                                                         (int)p.count, dpool, d_err, tiles);
         } else if (geo.m == n) {
-            int threads = (int)(size / EPT_WHOLE);
+            const int rb = phase_reg_bits(plan.dtype);
+            int threads = (int)(geo.m >= rb + kPhaseMinSlotBits ? size >> rb : size / EPT_WHOLE);
             threads = threads < 32 ? 32 : (threads > 512 ? 512 : threads);
             (p.matk ? kwhole_k : kwhole)<<<1, threads, sizeof(T) * size, stream>>>((T*)sv, geo, dops + p.first,
                                                                                (int)p.count, dpool);
