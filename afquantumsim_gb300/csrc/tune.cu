@@ -91,6 +91,7 @@ int autotune_impl(aqsg_ctx ctx, int n, int dtype, const aqsg_op* ops, int count,
     std::vector<Cand> cands;
     if (!tiled_only) cands.push_back({AQSG_EXEC_PER_GATE, 0, 0});
     cands.push_back({AQSG_EXEC_TILED, 0, 0});
+    cands.push_back({AQSG_EXEC_TILED, 1, 0});  // consecutive 1-qubit gates merged
     for (int k = 2; k <= AQSG_MAX_UNITARY_QUBITS; ++k) {
         cands.push_back({AQSG_EXEC_TILED, k, 0});
         if (dtype == AQSG_C64) cands.push_back({AQSG_EXEC_TILED, k, 1});
@@ -195,7 +196,7 @@ int autotune_grouped(aqsg_ctx ctx, int n, const aqsg_op* ops, int count, int* fu
     double best_ms = 1e300;
     int best_fuse = 0;
     size_t table_cap = 0;
-    for (int fuse : {0, 2, 3, 4, 5}) {
+    for (int fuse : {0, 1, 2, 3, 4, 5}) {
         if (rc != AQSG_OK) break;
         std::vector<LOp> low;
         if (fuse > 0) {

@@ -271,8 +271,9 @@ typedef struct aqsg_tune_entry {
 } aqsg_tune_entry;
 
 /* Time the circuit (on a scratch n-qubit register of dtype, from |0...0>)
- * one gate per pass, in tile passes, and compiled with fusion widths 2..5
- * with and without the tensor cores; reps timed runs each after one warm-up.
+ * one gate per pass, in tile passes, compiled with fusion width 1 (runs of
+ * 1-qubit gates merged) and with widths 2..5 with and without the tensor
+ * cores; reps timed runs each after one warm-up.
  * *best receives the fastest.  The choice is cached per context by the
  * circuit's structure (kinds and operands, not angles or matrix entries):
  * with all == NULL a cached choice returns at once.  all (capacity entries,

@@ -17,9 +17,9 @@ def test_autotune_candidates_and_cache(gpu_ctx):
     n = 16
     ops = circuits.brickwork(n, 6, seed=3)
     best, every = aq.autotune(gpu_ctx, n, ops, aq.C64, reps=1)
-    assert len(every) == 2 + 4 * 2  # per gate, tiled, widths 2..5 x tensor cores on/off
+    assert len(every) == 3 + 4 * 2  # per gate, tiled, width 1, widths 2..5 x tensor cores on/off
     assert {(e["exec_mode"], e["fuse_qubits"], e["tensor_cores"]) for e in every} == \
-        {(aq.EXEC_PER_GATE, 0, 0), (aq.EXEC_TILED, 0, 0)} | \
+        {(aq.EXEC_PER_GATE, 0, 0), (aq.EXEC_TILED, 0, 0), (aq.EXEC_TILED, 1, 0)} | \
         {(aq.EXEC_TILED, k, t) for k in range(2, 6) for t in (0, 1)}
     assert all(e["ms"] > 0 for e in every)
     assert best["ms"] == min(e["ms"] for e in every)
@@ -50,4 +50,4 @@ def test_autotune_candidates_and_cache(gpu_ctx):
 def test_autotune_c128_has_no_tensor_core_candidates(gpu_ctx):
     ops = circuits.plain_layers(10, 3, seed=2)
     best, every = aq.autotune(gpu_ctx, 10, ops, aq.C128, reps=1)
-    assert len(every) == 2 + 4 and not any(e["tensor_cores"] for e in every)
+    assert len(every) == 3 + 4 and not any(e["tensor_cores"] for e in every)
