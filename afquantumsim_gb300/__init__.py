@@ -28,7 +28,7 @@ LIB_PATH = PKG_DIR / "_build" / "libaqsg.so"
 
 EXPORTS = [
     "aqsg_version", "aqsg_last_error", "aqsg_init", "aqsg_shutdown",
-    "aqsg_set_exec_mode", "aqsg_set_tensor_cores", "aqsg_synchronize", "aqsg_ctx_stream",
+    "aqsg_set_exec_mode", "aqsg_set_tensor_cores", "aqsg_synchronize", "aqsg_ctx_after", "aqsg_ctx_stream",
     "aqsg_launch_count",
     "aqsg_state_alloc", "aqsg_state_free", "aqsg_state_info",
     "aqsg_state_set_basis_index", "aqsg_state_set_product", "aqsg_state_upload",
@@ -92,6 +92,7 @@ def load_library(path: os.PathLike | str | None = None) -> C.CDLL:
         "aqsg_set_exec_mode": ([P, I], I),
         "aqsg_set_tensor_cores": ([P, I], I),
         "aqsg_synchronize": ([P], I),
+        "aqsg_ctx_after": ([P, P], I),
         "aqsg_ctx_stream": ([P, C.POINTER(P)], I),
         "aqsg_launch_count": ([P, C.POINTER(U64)], I),
         "aqsg_state_alloc": ([P, I, I, C.POINTER(P)], I),
@@ -275,6 +276,11 @@ class Context:
 
     def synchronize(self) -> None:
         _check(self.lib.aqsg_synchronize(self.h))
+
+    def after(self, other: "Context") -> None:
+        """aqsg_ctx_after: work queued here from now on waits for the work
+        queued on `other` so far (no host blocking)."""
+        _check(self.lib.aqsg_ctx_after(self.h, other.h))
 
     def stream_handle(self) -> int:
         """The context's cudaStream_t as an integer."""

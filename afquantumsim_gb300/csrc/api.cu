@@ -303,7 +303,9 @@ int aqsg_init(int device, aqsg_ctx* out) {
     if (e == cudaSuccess) e = cudaMallocHost((void**)&c->host_result, 4096);
     if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_err, 256);
     if (e == cudaSuccess) e = cudaMemset(c->d_err, 0, 256);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->order, cudaEventDisableTiming);
     if (e != cudaSuccess) {
+        if (c->order) cudaEventDestroy(c->order);
         if (c->stream) cudaStreamDestroy(c->stream);
         delete c;
         return cuda_error(e, "aqsg_init");
@@ -324,6 +326,7 @@ int aqsg_shutdown(aqsg_ctx ctx) {
         if (s->ptr) cudaFree(s->ptr);
     if (ctx->host_result) cudaFreeHost(ctx->host_result);
     if (ctx->d_err) cudaFree(ctx->d_err);
+    if (ctx->order) cudaEventDestroy(ctx->order);
     cudaStreamDestroy(ctx->stream);
     autotune_forget(ctx);
     delete ctx;
@@ -347,6 +350,17 @@ int aqsg_set_tensor_cores(aqsg_ctx ctx, int enable) {
 int aqsg_synchronize(aqsg_ctx ctx) {
     if (!ctx) return set_error(AQSG_ERR_NULL, "NULL context");
     AQSG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return AQSG_OK;
+}
+
+int aqsg_ctx_after(aqsg_ctx ctx, aqsg_ctx other) {
+    if (!ctx || !other) return set_error(AQSG_ERR_NULL, "NULL context");
+    if (ctx == other) return AQSG_OK;  // a stream is already ordered with itself
+    if (ctx->device != other->device)
+        return set_error(AQSG_ERR_INVALID_ARGUMENT, "Contexts on different devices");
+    AQSG_CUDA_TRY(cudaSetDevice(ctx->device));
+    AQSG_CUDA_TRY(cudaEventRecord(other->order, other->stream));
+    AQSG_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, other->order, 0));
     return AQSG_OK;
 }
 

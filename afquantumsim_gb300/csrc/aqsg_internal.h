@@ -81,6 +81,7 @@ struct aqsg_ctx_s {
     double* host_result = nullptr;  // pinned FP64 results
     int* d_err = nullptr;           // device flag: a bounded kernel wait gave up
     int tensor_cores = 1;           // fused unitaries on tcgen05 (c64 tiles)
+    cudaEvent_t order = nullptr;    // marks this stream's queue for aqsg_ctx_after
 };
 
 struct aqsg_state_s {

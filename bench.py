@@ -52,10 +52,11 @@ def parse_args():
     ap.add_argument("--cpu-sample-ops", type=int, default=8,
                     help="QFT gates in the CPU-baseline sample")
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--only", choices=["fused_brickwork", "plain12", "vqe_batch", "serving", "qft_grid"],
+    ap.add_argument("--only", choices=["fused_brickwork", "plain12", "vqe_batch", "vqe_ansatz", "serving", "qft_grid"],
                     help="run one secondary workload alone (at --n qubits where it takes a size) "
                          "and print its JSON; for profiling")
-    ap.add_argument("--depth", type=int, default=20, help="brick-work depth for --only fused_brickwork")
+    ap.add_argument("--depth", type=int, default=20,
+                    help="brick-work depth for --only fused_brickwork, layers for --only vqe_ansatz")
     ap.add_argument("--count", type=int, default=0, help="circuits for --only vqe_batch / serving")
     return ap.parse_args()
 
@@ -260,6 +261,38 @@ def bench_qft_grid(ctx, stream, sizes=((24, "c64"), (28, "c64"), (24, "c128"), (
         out[f"qft{n}_{dt}"] = {"ms_per_step": round(ms, 2), "gate_apps_per_s": round(len(ops) / (ms / 1e3), 1),
                                "hbm_gbs": round(total_bytes / (ms / 1e3) / 1e9, 1)}
     return out
+
+
+def bench_vqe_ansatz(ctx, stream, n=26, layers=8, reps=3):
+    """One large VQE ansatz register (RotY + RotZ on every qubit and a CX ring
+    per layer; angles seeded) in tile passes at every fusion width, on the
+    CUDA cores (register phases) and, for widths >= 3, with the fused
+    unitaries on the tensor cores: ms per run and passes (launches) per run,
+    from |0...0>."""
+    import afquantumsim_gb300 as aq
+    from afquantumsim_gb300 import circuits
+    params = np.random.default_rng(1).uniform(-np.pi, np.pi, size=(layers, n, 2)).astype(np.float32)
+    ops = aq.op_array(circuits.vqe_ansatz(n, layers, params))
+    res = {"workload": f"vqe_ansatz{n}x{layers}", "gates": len(ops), "runs": {}}
+    with aq.State(ctx, n, aq.C64) as st:
+        st.set_basis(0)
+        for fuse in range(0, 6):
+            for tc in ((False, True) if fuse >= 3 else (False,)):
+                ctx.set_tensor_cores(tc)
+                prog = aq.Program(n, ops, max_qubits=fuse) if fuse else None
+                run = (lambda: prog.run(st, aq.EXEC_TILED)) if prog else (lambda: st.apply(ops, aq.EXEC_TILED))
+                run()
+                l0 = ctx.launch_count()
+                ms = _time_ms(stream, run, reps)
+                key = f"fuse{fuse}{'_tc' if tc else ''}"
+                res["runs"][key] = {"ms": round(ms, 3), "launches": (ctx.launch_count() - l0) // reps,
+                                    "ops": prog.info()[0] if prog else len(ops)}
+                if prog:
+                    prog.free()
+        ctx.set_tensor_cores(True)
+    best = min(res["runs"], key=lambda k: res["runs"][k]["ms"])
+    res["best"] = best
+    return res
 
 
 def bench_plain12(ctx, stream, n=12, layers=10):
@@ -549,7 +582,10 @@ def run_ours(args, rank, world, local_rank):
     # end to end through the C ABI with host buffers.  Per step: upload the
     # step's input from pinned host memory, run the circuit, copy its result
     # to pinned host memory.  Two registers on two contexts (streams) take the
-    # steps in turn, so the copies of one step overlap the gates of the other.
+    # steps in turn: a step's upload and the previous step's result copy
+    # overlap the gates of the other register, and aqsg_ctx_after keeps the
+    # two registers' gates one after the other (HBM-bound passes of two
+    # registers interleaved run slower than back to back).
     e2e_steps = max(4, args.steps)
     ctx2 = aq.Context(local_rank)
     st2 = aq.State(ctx2, n, aq.C64 if args.dtype == "c64" else aq.C128)
@@ -567,8 +603,15 @@ def run_ours(args, rank, world, local_rank):
         c, r, ho = lanes[step % 2]
         c.synchronize()  # this register's previous step (its result copy) is done
         r.upload_ptr(host_in.data_ptr())
-        r.apply(ops, mode)
-        r.download_async_ptr(ho.data_ptr())
+        if step > 0:
+            pc, pr, pho = lanes[(step - 1) % 2]
+            c.after(pc)  # after the previous step's gates (its queue holds nothing else)
+            r.apply(ops, mode)
+            pr.download_async_ptr(pho.data_ptr())  # previous result, under this step's gates
+        else:
+            r.apply(ops, mode)
+    c, r, ho = lanes[(e2e_steps - 1) % 2]
+    r.download_async_ptr(ho.data_ptr())
     ctx.synchronize()
     ctx2.synchronize()
     e2e_s = time.perf_counter() - t0
@@ -581,7 +624,8 @@ def run_ours(args, rank, world, local_rank):
     e2e = {"value": round(world * gates * e2e_steps / e2e_s, 3), "unit": "gate-apps/s",
            "h2d_bytes_per_step": N * amp_b, "d2h_bytes_per_step": N * amp_b,
            "ms_per_step": round(e2e_s / e2e_steps * 1e3, 3), "steps": e2e_steps,
-           "pipeline": "two registers on two streams; each step uploads its input and reads its result"}
+           "pipeline": "two registers on two streams, gates of consecutive steps ordered (aqsg_ctx_after); "
+                       "each step uploads its input and reads its result under the other register's gates"}
 
     extras = {}
     if not args.no_extras and rank == 0:
@@ -715,6 +759,8 @@ def run_only(args):
         res = bench_qft_grid(ctx, stream)
     elif args.only == "vqe_batch":
         res = bench_vqe_batch(ctx, count=args.count or 4096)
+    elif args.only == "vqe_ansatz":
+        res = bench_vqe_ansatz(ctx, stream, n=args.n, layers=args.depth)
     else:
         res = bench_serving(ctx, count=args.count or 160)
     ctx.close()

@@ -162,6 +162,15 @@ int aqsg_set_tensor_cores(aqsg_ctx ctx, int enable);
 /* Wait for all work queued on the context's stream. */
 int aqsg_synchronize(aqsg_ctx ctx);
 
+/* Order two contexts of one device without blocking the host: work queued on
+ * ctx after this call starts only once everything queued on other before it
+ * has finished.  A pipeline over two registers uses it to keep one step's
+ * gates from running alongside the previous step's (HBM-bound passes of two
+ * registers interleaved run slower than one after the other) while each
+ * step's host copies overlap the other step's gates.  The reference has no
+ * counterpart (one simulator, one implicit ArrayFire queue). */
+int aqsg_ctx_after(aqsg_ctx ctx, aqsg_ctx other);
+
 /* The context's CUDA stream (a cudaStream_t), for callers that order their
  * own work or timing events with the engine's. */
 int aqsg_ctx_stream(aqsg_ctx ctx, void** stream);
