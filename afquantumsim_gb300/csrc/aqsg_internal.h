@@ -135,7 +135,7 @@ int launch_tile_plan(void* sv, const TilePlan& plan, const void* dev, cudaStream
 // at reg_stride amplitudes from one another, whose tables (the same geometry,
 // their own ops) sit dev_stride bytes apart from dev0: one launch per pass.
 int launch_tile_plan_multi(void* sv0, uint64_t reg_stride, int members, const TilePlan& plan, const void* dev0,
-                           uint64_t dev_stride, cudaStream_t stream, uint64_t* launches);
+                           uint64_t dev_stride, cudaStream_t stream, int* d_err, uint64_t* launches);
 // Runs ops through shared-memory tile passes; returns AQSG_OK.
 int run_tiled(aqsg_state_s* st, const std::vector<LOp>& ops);
 // Largest tile (log2 amplitudes) the tile kernel holds for a dtype.
@@ -167,7 +167,7 @@ int autotune_impl(aqsg_ctx ctx, int n, int dtype, const aqsg_op* ops, int count,
                   aqsg_tune_entry* best, aqsg_tune_entry* all, int capacity, int* count_out);
 // Fusion width for a batched large register, timed as a group of replicas
 // on the CUDA cores (cached per context and structure).
-int autotune_grouped(aqsg_ctx ctx, int n, const aqsg_op* ops, int count, int* fuse_out);
+int autotune_grouped(aqsg_ctx ctx, int n, const aqsg_op* ops, int count, int* fuse_out, int* tc_out);
 // Drop the autotuner's cached choices of a context (it is shutting down).
 void autotune_forget(aqsg_ctx ctx);
 // The fused op list of a compiled program.

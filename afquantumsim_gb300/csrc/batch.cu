@@ -121,7 +121,8 @@ __global__ void k_basis0_multi(float2* sv, uint64_t stride) {
 }
 
 // Large registers whose tile plans have the same geometry (qubits, passes,
-// tile bits, table and pool sizes) and no tensor-core passes run as a group:
+// tile bits, tensor-core use, table, pool and operand-blob sizes) run as a
+// group:
 // one launch per pass for all of them, their registers side by side and
 // their op tables at a fixed stride in the device plan area.
 struct LargeGroup {
@@ -292,10 +293,10 @@ static int encode_batch(aqsg_batch_s* b, const aqsg_circuit* cs, bool first_time
         if (class_of(ci.n) >= 0) continue;
         large_index[i] = nlarge++;
         if (first_time) {
-            int best_fuse = 0;
-            if (int rc = autotune_grouped(b->ctx, ci.n, ci.ops, ci.count, &best_fuse)) return rc;
+            int best_fuse = 0, best_tc = 0;
+            if (int rc = autotune_grouped(b->ctx, ci.n, ci.ops, ci.count, &best_fuse, &best_tc)) return rc;
             b->fuse.push_back(best_fuse);
-            b->tc.push_back(0);
+            b->tc.push_back(best_tc);
         }
     }
     // per-circuit lowering and encoding on all host threads
@@ -423,7 +424,7 @@ static int record_batch(aqsg_batch_s* b, cudaStream_t s) {
         AQSG_CUDA_TRY(cudaGetLastError());
         const TilePlan& plan = b->plans[gr.members[0]];
         if (int rc = launch_tile_plan_multi(gr.regs, amps, members, plan, (const char*)b->d_large + gr.dev_off,
-                                            gr.stride, bs, &b->kernels))
+                                            gr.stride, bs, b->ctx->d_err, &b->kernels))
             return rc;
         if (int rc = launch_expz_raw_multi(gr.regs, amps, members, gr.n, gr.partials, gr.d_out_off, b->d_out, bs))
             return rc;
@@ -524,18 +525,18 @@ int aqsg_batch_create(aqsg_ctx ctx, const aqsg_circuit* circuits, int count, aqs
             e = cudaMemcpy(b->d_small_items[c], b->items[c].data(), sizeof(SmallItem) * b->items[c].size(),
                            cudaMemcpyHostToDevice);
     }
-    // group the large registers with equal plan geometry (plain plans only)
+    // group the large registers with equal plan geometry
     b->grouped.assign(b->large.size(), 0);
     {
         std::map<std::vector<uint64_t>, std::vector<size_t>> by_key;
         for (size_t k = 0; k < b->large.size(); ++k) {
             const TilePlan& p = b->plans[k];
-            if (p.any_tc) continue;
             std::vector<uint64_t> key = {(uint64_t)p.n, p.table.size(), p.pool.size(), p.passes.size()};
             for (const TilePass& ps : p.passes) {
-                key.push_back(((uint64_t)ps.m << 48) | ((uint64_t)ps.L << 40) | ((uint64_t)ps.matk << 32) |
-                              ps.first);
+                key.push_back(((uint64_t)ps.m << 48) | ((uint64_t)ps.L << 40) | ((uint64_t)ps.tc << 36) |
+                              ((uint64_t)ps.matk << 32) | ps.first);
                 key.push_back(ps.count);
+                key.push_back(((uint64_t)ps.tc_blob << 32) | ps.tc_bytes);
                 uint64_t bits = 0;
                 for (int i = 0; i < ps.m; ++i) bits |= 1ull << ps.tbits[i];
                 key.push_back(bits);
@@ -658,7 +659,12 @@ int aqsg_batch_run(aqsg_batch b, double* z, double* zz) {
     c->launches += b->kernels;
     AQSG_CUDA_TRY(cudaMemcpyAsync(b->h_out, b->d_out, sizeof(double) * b->out_doubles, cudaMemcpyDeviceToHost,
                                   c->stream));
+    AQSG_CUDA_TRY(cudaMemcpyAsync(c->host_result, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     AQSG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (*reinterpret_cast<volatile int*>(c->host_result) != 0) {  // a tensor-core pass's bounded wait gave up
+        AQSG_CUDA_TRY(cudaMemset(c->d_err, 0, sizeof(int)));
+        return set_error(AQSG_ERR_TIMEOUT, "A bounded device wait gave up during the batch");
+    }
     size_t zo = 0, zzo = 0;
     for (int i = 0; i < b->count; ++i) {
         const int n = b->n[i];

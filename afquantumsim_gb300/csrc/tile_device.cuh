@@ -97,6 +97,17 @@ __device__ __forceinline__ uint32_t mbar_try_wait(uint64_t* bar, uint32_t parity
     return ok;
 }
 
+// Wait for the phase of `bar` with the given parity, at most kWaitNs of wall
+// time (for winding down: copies or MMAs already issued must land before
+// the shared or tensor memory goes, whatever the error flag says).
+__device__ __forceinline__ bool mbar_wait_timeout(uint64_t* bar, uint32_t parity) {
+    const uint64_t t0 = globaltimer_ns();
+    for (uint32_t it = 0;; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 63u) == 63u && globaltimer_ns() - t0 > kWaitNs) return false;
+    }
+}
+
 // Wait for the phase of `bar` with the given parity; gives up after kWaitNs
 // of wall time, or early once the device error flag is set.  Returns whether
 // the phase completed.

@@ -182,21 +182,30 @@ __device__ __forceinline__ bool compute_any(bool v) {
 }
 
 // Tensor-core streaming passes (c64, 4096-amplitude tiles).  A persistent
-// CTA per SM walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ...; a tile
-// is 128 rows of 256 contiguous bytes (the 5 low index bits) at the row
-// offsets of the pass's 7 high tile bits.  Warp 16 is the producer: it
-// copies tiles in 16-byte cp.async chunks into three shared-memory buffers
-// (full[b] completes when all 32 lanes' chunks have landed; many small
-// requests stay in flight without the per-request cost of bulk copies) and
-// writes them back with 128-bit stores once the 16 compute warps have
-// released them (done[b]); so the next tiles load and the previous one
-// stores while the compute warps run the pass's ops on the current one.
-// The pass's operand blob and op table are bulk-loaded once per CTA.  Every
-// wait is bounded: one that gives up sets the error flag and the CTA winds
-// down.
+// CTA per SM walks its tiles; a tile is 128 rows of 256 contiguous bytes
+// (the 5 low index bits) at the row offsets of the pass's 7 high tile bits.
+// Warp 16 is the producer: it copies tiles in 16-byte cp.async chunks into
+// three shared-memory buffers (full[b] completes when all 32 lanes' chunks
+// have landed; many small requests stay in flight without the per-request
+// cost of bulk copies) and writes them back with 128-bit stores once the 16
+// compute warps have released them (done[b]); so the next tiles load and the
+// previous one stores while the compute warps run the pass's ops on the
+// current one.  The pass's operand blob and op table are bulk-loaded into
+// shared memory.  Every wait is bounded: one that gives up sets the error
+// flag and the CTA winds down.
+//
+// One register (MULTI false): CTA b takes tiles b, b + grid, ...  A group of
+// `members` registers of equal plan geometry (MULTI true; the batched
+// engine): register m starts reg_stride amplitudes after register m-1, its
+// op table and pool dev_stride bytes after m-1's; CTA b takes a contiguous
+// run of the members' tiles, and where the run crosses into the next
+// register the producer reloads the blob and op table once the compute warps
+// have released the last tile of the previous one.
+template <bool MULTI>
 __global__ void __launch_bounds__(kTcCta, 1)
-k_stream_tc(float2* __restrict__ sv, const TileGeom g, const TileOp* __restrict__ ops, int nops,
-            const unsigned char* __restrict__ pool, int* err, uint32_t ntiles) {
+k_stream_tc(float2* __restrict__ sv0, const TileGeom g, const unsigned char* __restrict__ dev0, uint32_t op_first,
+            int nops, uint64_t pool_off, int* err, uint32_t ntiles, uint32_t members, uint64_t reg_stride,
+            uint64_t dev_stride) {
     using SM = TcStreamSmem;
     constexpr int NB = SM::kBufs;
     constexpr int L = 5, M = 12;
@@ -246,22 +255,41 @@ k_stream_tc(float2* __restrict__ sv, const TileGeom g, const TileOp* __restrict_
         }
         return base;
     };
-    const uint32_t count = blockIdx.x < ntiles ? (ntiles - 1u - blockIdx.x) / gridDim.x + 1u : 0u;
+    // this CTA's tiles: the i-th is tile local_of(i) of register member_of(i)
+    uint32_t count, first = 0;
+    if constexpr (MULTI) {
+        const uint64_t total = (uint64_t)ntiles * members;
+        const uint64_t chunk = (total + gridDim.x - 1) / gridDim.x;
+        const uint64_t start = (uint64_t)blockIdx.x * chunk;
+        count = start < total ? (uint32_t)(total - start < chunk ? total - start : chunk) : 0u;
+        first = (uint32_t)start;
+    } else {
+        count = blockIdx.x < ntiles ? (ntiles - 1u - blockIdx.x) / gridDim.x + 1u : 0u;
+    }
+    auto tile_of = [&](uint32_t i) { return MULTI ? first + i : blockIdx.x + i * gridDim.x; };
+    auto member_of = [&](uint32_t i) { return MULTI ? tile_of(i) / ntiles : 0u; };
+    auto local_of = [&](uint32_t i) { return MULTI ? tile_of(i) % ntiles : tile_of(i); };
+    auto dev_of = [&](uint32_t m) { return dev0 + (uint64_t)m * dev_stride; };
+    auto sv_of = [&](uint32_t m) { return sv0 + (uint64_t)m * reg_stride; };
 
     if (warp == kTcThreads / 32) {
         // ---- producer warp ----
-        if (lane == 0) {
+        uint32_t blob_loads = 0;
+        auto load_blob = [&](uint32_t m) {  // lane 0
+            const unsigned char* pool = dev_of(m) + pool_off;
             const uint32_t opb = ops_in_smem ? (uint32_t)nops * (uint32_t)sizeof(TileOp) : 0u;
             mbar_expect_tx(blob_bar, g.tc_bytes + opb);
             for (uint32_t o = 0; o < g.tc_bytes; o += 32768u) {
                 const uint32_t len = g.tc_bytes - o < 32768u ? g.tc_bytes - o : 32768u;
                 bulk_load(smem_raw + SM::kBlob + o, pool + g.tc_blob + o, len, blob_bar);
             }
-            if (opb) bulk_load(sops, ops, opb, blob_bar);
-        }
+            if (opb) bulk_load(sops, reinterpret_cast<const TileOp*>(dev_of(m)) + op_first, opb, blob_bar);
+            ++blob_loads;
+        };
+        if (lane == 0) load_blob(count ? member_of(0) : 0u);
         auto issue_load = [&](uint32_t i) {
             const uint32_t buf = i % NB;
-            const float2* src = sv + tile_base(blockIdx.x + i * gridDim.x);
+            const float2* src = sv_of(member_of(i)) + tile_base(local_of(i));
             unsigned char* dst = smem_raw + buf * kBufBytes;
 #pragma unroll 8
             for (uint32_t q = lane; q < kRows * 16u; q += 32u) {
@@ -277,7 +305,10 @@ k_stream_tc(float2* __restrict__ sv, const TileGeom g, const TileOp* __restrict_
                 if (lane == 0) atomicExch(err, 1);
                 break;
             }
-            float2* dstg = sv + tile_base(blockIdx.x + i * gridDim.x);
+            // the compute warps have released tile i: at a change of register
+            // its blob and op table may be replaced
+            if (MULTI && lane == 0 && i + 1 < count && member_of(i + 1) != member_of(i)) load_blob(member_of(i + 1));
+            float2* dstg = sv_of(member_of(i)) + tile_base(local_of(i));
             const unsigned char* src = smem_raw + buf * kBufBytes;
 #pragma unroll 8
             for (uint32_t q = lane; q < kRows * 16u; q += 32u) {
@@ -288,9 +319,10 @@ k_stream_tc(float2* __restrict__ sv, const TileGeom g, const TileOp* __restrict_
             __syncwarp();  // every lane's reads of the buffer are done
             if (i + NB < count) issue_load(i + NB);
         }
-        // the cp.async copies this warp started have landed (a wound-down
-        // CTA may leave some unconsumed)
+        // the copies this warp started have landed before the shared memory
+        // goes (a wound-down CTA may leave some unconsumed)
         asm volatile("cp.async.wait_all;" ::: "memory");
+        if (lane == 0 && blob_loads > 0) mbar_wait_timeout(blob_bar, (blob_loads - 1u) & 1u);
     } else {
         // ---- compute warps ----
         TcSmem tcs;
@@ -300,15 +332,22 @@ k_stream_tc(float2* __restrict__ sv, const TileGeom g, const TileOp* __restrict_
         tcs.mma_bar = mma_bar;
         tcs.tmem = *reinterpret_cast<volatile uint32_t*>(smem_raw + SM::kTmemSlot);
         tcs.err = err;
-        const TileOp* optab = ops_in_smem ? sops : ops;
+        uint32_t blob_par = 0, cur = count ? member_of(0) : 0u;
         bool ok = !compute_any(!mbar_wait_bounded(blob_bar, 0, err));
         for (uint32_t i = 0; ok && i < count; ++i) {
             const uint32_t buf = i % NB;
+            const uint32_t m = member_of(i);
+            if (MULTI && m != cur) {  // the producer reloads the blob after tile i - 1
+                blob_par ^= 1u;
+                if (compute_any(!mbar_wait_bounded(blob_bar, blob_par, err))) break;
+                cur = m;
+            }
             if (compute_any(!mbar_wait_bounded(full + buf, (i / NB) & 1u, err))) break;
             float2* s = reinterpret_cast<float2*>(smem_raw + buf * kBufBytes);
-            const uint64_t base = tile_base(blockIdx.x + i * gridDim.x);
-            tile_run_ops<float, EPT, true, LAY, ComputeSync512>(s, 1u << M, kTcThreads, base, optab, nops, pool,
-                                                               &tcs, &tph);
+            const uint64_t base = tile_base(local_of(i));
+            const TileOp* optab = ops_in_smem ? sops : reinterpret_cast<const TileOp*>(dev_of(m)) + op_first;
+            tile_run_ops<float, EPT, true, LAY, ComputeSync512>(s, 1u << M, kTcThreads, base, optab, nops,
+                                                               dev_of(m) + pool_off, &tcs, &tph);
             fence_async_smem();
             __syncwarp();
             if (lane == 0) mbar_arrive(done + buf);
@@ -317,10 +356,12 @@ k_stream_tc(float2* __restrict__ sv, const TileGeom g, const TileOp* __restrict_
         if (!ok || *(volatile int*)err != 0) {
             if (tid == 0) {
                 atomicExch(err, 1);
-                // the operand copy and the MMAs this CTA issued finish before
-                // the shared and tensor memory go
-                mbar_wait_bounded(blob_bar, 0, err);
-                mbar_wait_bounded(mma_bar, tph.mma, err);
+                // the MMAs this CTA issued finish before the shared and
+                // tensor memory go (the producer waits for its own copies):
+                // the last issued commit is the phase of parity tph.mma ^ 1
+                // (already complete, or never started on a fresh barrier,
+                // when nothing is outstanding)
+                mbar_wait_timeout(mma_bar, tph.mma ^ 1u);
             }
         }
     }
@@ -989,14 +1030,15 @@ static int launch_plan_t(void* sv, const TilePlan& plan, const void* dev, cudaSt
             if (geo.m != kTcTileBits || sizeof(R) != 4)
                 return set_error(AQSG_ERR_RUNTIME, "Tensor-core pass with an unexpected tile shape");
             if (!have_t) {
-                if (int rc = stream_shape(k_stream_tc, kTcCta, (int)TcStreamSmem::kBytes, &tshape)) return rc;
+                if (int rc = stream_shape(k_stream_tc<false>, kTcCta, (int)TcStreamSmem::kBytes, &tshape)) return rc;
                 have_t = true;
             }
             if (p.tc_bytes > kTcBlobMax) return set_error(AQSG_ERR_RUNTIME, "Tensor-core operands exceed the blob");
             const uint32_t tiles = 1u << (n - geo.m);
             const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)(tshape.sms * tshape.per_sm));
-            k_stream_tc<<<grid, kTcCta, TcStreamSmem::kBytes, stream>>>((float2*)sv, geo, dops + p.first,
-                                                                        (int)p.count, dpool, d_err, tiles);
+            k_stream_tc<false><<<grid, kTcCta, TcStreamSmem::kBytes, stream>>>(
+                (float2*)sv, geo, (const unsigned char*)dev, p.first, (int)p.count, plan.pool_offset(), d_err, tiles,
+                1u, 0ull, 0ull);
         } else if (geo.m == n) {
             const int rb = phase_reg_bits(plan.dtype);
             int threads = (int)(geo.m >= rb + kPhaseMinSlotBits ? size >> rb : size / EPT_WHOLE);
@@ -1016,13 +1058,14 @@ static int launch_plan_t(void* sv, const TilePlan& plan, const void* dev, cudaSt
 }
 
 int launch_tile_plan_multi(void* sv0, uint64_t reg_stride, int members, const TilePlan& plan, const void* dev0,
-                           uint64_t dev_stride, cudaStream_t stream, uint64_t* launches) {
-    if (plan.dtype != AQSG_C64 || plan.any_tc)
-        return set_error(AQSG_ERR_RUNTIME, "Grouped tile passes take plain complex64 plans");
+                           uint64_t dev_stride, cudaStream_t stream, int* d_err, uint64_t* launches) {
+    if (plan.dtype != AQSG_C64) return set_error(AQSG_ERR_RUNTIME, "Grouped tile passes take complex64 plans");
     const int n = plan.n;
     constexpr int EPT = (1 << 12) / 256;
     auto kplain = k_tile_stream_multi<float, EPT, false>;
     auto kplain_k = k_tile_stream_multi<float, EPT, true>;
+    StreamShape tshape;
+    bool have_t = false;
     for (const TilePass& p : plan.passes) {
         if (p.m != 12 || p.m == n) return set_error(AQSG_ERR_RUNTIME, "Grouped tile passes take streaming plans");
         TileGeom geo;
@@ -1031,14 +1074,28 @@ int launch_tile_plan_multi(void* sv0, uint64_t reg_stride, int members, const Ti
         geo.m = p.m;
         geo.L = p.L;
         for (int i = 0; i < p.m; ++i) geo.tbits[i] = p.tbits[i];
+        geo.tc_blob = p.tc_blob;
+        geo.tc_bytes = p.tc_bytes;
         const uint32_t size = 1u << geo.m;
-        const size_t shm = sizeof(float2) * size + (size_t(1) << (geo.m - geo.L)) * sizeof(uint64_t);
         const uint32_t tiles = 1u << (n - geo.m);
         const uint64_t blocks = (uint64_t)tiles * (uint64_t)members;
         if (blocks > 0x7fffffffull) return set_error(AQSG_ERR_RUNTIME, "Too many tiles in one grouped pass");
-        (p.matk ? kplain_k : kplain)<<<(unsigned)blocks, 256, shm, stream>>>(
-            (float2*)sv0, reg_stride, geo, (const unsigned char*)dev0, dev_stride, p.first, (int)p.count,
-            plan.pool_offset(), tiles);
+        if (p.tc) {
+            if (!have_t) {
+                if (int rc = stream_shape(k_stream_tc<true>, kTcCta, (int)TcStreamSmem::kBytes, &tshape)) return rc;
+                have_t = true;
+            }
+            if (p.tc_bytes > kTcBlobMax) return set_error(AQSG_ERR_RUNTIME, "Tensor-core operands exceed the blob");
+            const uint32_t grid = (uint32_t)std::min<uint64_t>(blocks, (uint64_t)tshape.sms * tshape.per_sm);
+            k_stream_tc<true><<<grid, kTcCta, TcStreamSmem::kBytes, stream>>>(
+                (float2*)sv0, geo, (const unsigned char*)dev0, p.first, (int)p.count, plan.pool_offset(), d_err,
+                tiles, (uint32_t)members, reg_stride, dev_stride);
+        } else {
+            const size_t shm = sizeof(float2) * size + (size_t(1) << (geo.m - geo.L)) * sizeof(uint64_t);
+            (p.matk ? kplain_k : kplain)<<<(unsigned)blocks, 256, shm, stream>>>(
+                (float2*)sv0, reg_stride, geo, (const unsigned char*)dev0, dev_stride, p.first, (int)p.count,
+                plan.pool_offset(), tiles);
+        }
         if (launches) ++*launches;
         AQSG_CUDA_TRY(cudaGetLastError());
     }

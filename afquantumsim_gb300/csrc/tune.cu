@@ -164,11 +164,13 @@ int autotune_impl(aqsg_ctx ctx, int n, int dtype, const aqsg_op* ops, int count,
 
 namespace aqsg {
 
-// Fusion width for a large register of the batched engine, timed the way the
-// batch runs it: the plain (CUDA-core) tile plan over a group of replicas
-// whose size depends only on n (so the choice does not depend on the rest of
-// the batch), one launch per pass.  Cached per context and structure.
-int autotune_grouped(aqsg_ctx ctx, int n, const aqsg_op* ops, int count, int* fuse_out) {
+// Fusion width and tensor-core use for a large register of the batched
+// engine, timed the way the batch runs it: the tile plan over a group of
+// replicas whose size depends only on n (so the choice does not depend on
+// the rest of the batch), one launch per pass.  Cached per context and
+// structure.  A run that trips the device error flag (a bounded wait gave
+// up) fails the tuning with AQSG_ERR_TIMEOUT.
+int autotune_grouped(aqsg_ctx ctx, int n, const aqsg_op* ops, int count, int* fuse_out, int* tc_out) {
     if (int rc = aqsg_check_ops(n, ops, count)) return rc;
     const uint64_t key = structure_hash(n, AQSG_C64, ops, count) ^ 0xC2B2AE3D27D4EB4Full;
     TuneCache& cache = tune_cache();
@@ -177,6 +179,7 @@ int autotune_grouped(aqsg_ctx ctx, int n, const aqsg_op* ops, int count, int* fu
         auto it = cache.best.find({(const void*)ctx, key});
         if (it != cache.best.end()) {
             *fuse_out = it->second.fuse_qubits;
+            *tc_out = it->second.tensor_cores;
             return AQSG_OK;
         }
     }
@@ -194,9 +197,11 @@ int autotune_grouped(aqsg_ctx ctx, int n, const aqsg_op* ops, int count, int* fu
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
     if (e != cudaSuccess) rc = cuda_error(e, "autotune_grouped");
     double best_ms = 1e300;
-    int best_fuse = 0;
+    int best_fuse = 0, best_tc = 0;
     size_t table_cap = 0;
-    for (int fuse : {0, 1, 2, 3, 4, 5}) {
+    const int cand[][2] = {{0, 0}, {1, 0}, {2, 0}, {3, 0}, {4, 0}, {5, 0}, {3, 1}, {4, 1}, {5, 1}};
+    for (const auto& fc : cand) {
+        const int fuse = fc[0], tc = fc[1];
         if (rc != AQSG_OK) break;
         std::vector<LOp> low;
         if (fuse > 0) {
@@ -213,7 +218,8 @@ int autotune_grouped(aqsg_ctx ctx, int n, const aqsg_op* ops, int count, int* fu
             if (rc) break;
         }
         TilePlan plan;
-        if ((rc = encode_tiled(n, AQSG_C64, low, false, &plan, false))) break;
+        if ((rc = encode_tiled(n, AQSG_C64, low, tc != 0, &plan, false))) break;
+        if (tc && !plan.any_tc) continue;  // nothing for the tensor cores: same as the plain plan
         const size_t stride = (plan.pool_offset() + plan.pool.size() + 255) & ~size_t(255);
         if (stride * replicas > table_cap) {
             if (tables) cudaFree(tables);
@@ -236,19 +242,36 @@ int autotune_grouped(aqsg_ctx ctx, int n, const aqsg_op* ops, int count, int* fu
             break;
         }
         uint64_t launches = 0;
-        if ((rc = launch_tile_plan_multi(regs, amps, replicas, plan, tables, stride, ctx->stream, &launches))) break;
+        if ((rc = launch_tile_plan_multi(regs, amps, replicas, plan, tables, stride, ctx->stream, ctx->d_err,
+                                         &launches)))
+            break;
         cudaEventRecord(e0, ctx->stream);
-        if ((rc = launch_tile_plan_multi(regs, amps, replicas, plan, tables, stride, ctx->stream, &launches))) break;
+        if ((rc = launch_tile_plan_multi(regs, amps, replicas, plan, tables, stride, ctx->stream, ctx->d_err,
+                                         &launches)))
+            break;
         cudaEventRecord(e1, ctx->stream);
         if ((e = cudaEventSynchronize(e1)) != cudaSuccess) {
             rc = cuda_error(e, "autotune_grouped");
             break;
+        }
+        if (plan.any_tc) {
+            int flag = 0;
+            if ((e = cudaMemcpy(&flag, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost)) != cudaSuccess) {
+                rc = cuda_error(e, "autotune_grouped");
+                break;
+            }
+            if (flag) {
+                cudaMemset(ctx->d_err, 0, sizeof(int));
+                rc = set_error(AQSG_ERR_TIMEOUT, "A bounded device wait gave up while tuning");
+                break;
+            }
         }
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
         if (ms < best_ms) {
             best_ms = ms;
             best_fuse = fuse;
+            best_tc = tc;
         }
     }
     cudaStreamSynchronize(ctx->stream);
@@ -261,12 +284,14 @@ int autotune_grouped(aqsg_ctx ctx, int n, const aqsg_op* ops, int count, int* fu
     std::memset(&en, 0, sizeof(en));
     en.exec_mode = AQSG_EXEC_TILED;
     en.fuse_qubits = best_fuse;
+    en.tensor_cores = best_tc;
     en.ms = best_ms / replicas;
     {
         std::lock_guard<std::mutex> g(cache.mu);
         cache.best[{(const void*)ctx, key}] = en;
     }
     *fuse_out = best_fuse;
+    *tc_out = best_tc;
     return AQSG_OK;
 }
 
