@@ -10,10 +10,11 @@
 // later group touches any of the gate's qubits — then moving the gate up to
 // the group only crosses gates it commutes with — and (2) the union of the
 // qubits stays within K.  Afterwards each group may merge whole into the
-// previous or next group it shares a qubit with, under the same two rules.  Each group's unitary is built on the host in FP64
-// by applying its gates to the 2^k basis vectors.
+// previous or next group it shares a qubit with, under the same two rules.
+// Each group's unitary is built on the host in FP64 by applying its gates as
+// row operations to the 2^k x 2^k identity.
 #include <algorithm>
-#include <complex>
+
 #include <cstring>
 
 #include "aqsg_internal.h"
@@ -31,7 +32,6 @@ struct aqsg_program_s {
 
 namespace aqsg {
 
-using cd = std::complex<double>;
 
 const std::vector<LOp>& program_ops(aqsg_program p) { return p->ops; }
 
@@ -43,39 +43,68 @@ static uint64_t support(const LOp& o) {
     return s;
 }
 
-// Apply one lowered op to a small host vector of 2^k amplitudes whose index
-// bits are the op's bits already remapped to local positions.
-static void host_apply(std::vector<cd>& v, const LOp& o) {
-    const uint64_t N = v.size();
-    auto coef = [&](int i) { return cd(o.m[2 * i], o.m[2 * i + 1]); };
+// Apply one lowered op to the rows of a D x D matrix U (row-major, real and
+// imaginary parts apart) whose row index bits are the op's bits remapped to
+// local positions: U <- O U.  Every column sees the same arithmetic as the op
+// applied to that column alone; the inner loops run along the contiguous
+// columns.
+struct RowMat {
+    int D = 0;
+    std::vector<double> re, im;
+    double* r(uint64_t i) { return re.data() + i * (uint64_t)D; }
+    double* q(uint64_t i) { return im.data() + i * (uint64_t)D; }
+};
+
+static void swap_rows(RowMat& u, uint64_t i, uint64_t j) {
+    std::swap_ranges(u.r(i), u.r(i) + u.D, u.r(j));
+    std::swap_ranges(u.q(i), u.q(i) + u.D, u.q(j));
+}
+
+static void scale_row(RowMat& u, uint64_t i, double cr, double ci) {
+    double *xr = u.r(i), *xi = u.q(i);
+    for (int c = 0; c < u.D; ++c) {
+        const double a = xr[c], b = xi[c];
+        xr[c] = cr * a - ci * b;
+        xi[c] = cr * b + ci * a;
+    }
+}
+
+static void host_apply_rows(RowMat& u, const LOp& o) {
+    const uint64_t N = (uint64_t)u.D;
     auto ok = [&](uint64_t i) { return (i & o.cmask) == o.cval; };
     switch (o.cls) {
         case L_PERM_X: case L_PERM_OR: case L_MAT2: case L_DIAG2: {
             const uint64_t t = 1ull << o.t0;
             for (uint64_t i = 0; i < N; ++i) {
                 if ((i & t) || !ok(i)) continue;
-                const cd a = v[i], b = v[i | t];
                 if (o.cls == L_PERM_X || (o.cls == L_PERM_OR && (i & o.amask))) {
-                    v[i] = b;
-                    v[i | t] = a;
+                    swap_rows(u, i, i | t);
                 } else if (o.cls == L_MAT2) {
-                    v[i] = coef(0) * a + coef(1) * b;
-                    v[i | t] = coef(2) * a + coef(3) * b;
+                    double *ar = u.r(i), *ai = u.q(i), *br = u.r(i | t), *bi = u.q(i | t);
+                    const double m0r = o.m[0], m0i = o.m[1], m1r = o.m[2], m1i = o.m[3];
+                    const double m2r = o.m[4], m2i = o.m[5], m3r = o.m[6], m3i = o.m[7];
+                    for (int c = 0; c < u.D; ++c) {
+                        const double xr = ar[c], xi = ai[c], yr = br[c], yi = bi[c];
+                        ar[c] = (m0r * xr - m0i * xi) + (m1r * yr - m1i * yi);
+                        ai[c] = (m0r * xi + m0i * xr) + (m1r * yi + m1i * yr);
+                        br[c] = (m2r * xr - m2i * xi) + (m3r * yr - m3i * yi);
+                        bi[c] = (m2r * xi + m2i * xr) + (m3r * yi + m3i * yr);
+                    }
                 } else if (o.cls == L_DIAG2) {
-                    v[i] = coef(0) * a;
-                    v[i | t] = coef(1) * b;
+                    scale_row(u, i, o.m[0], o.m[1]);
+                    scale_row(u, i | t, o.m[2], o.m[3]);
                 }
             }
             break;
         }
         case L_DIAG1:
             for (uint64_t i = 0; i < N; ++i)
-                if (ok(i)) v[i] *= coef(0);
+                if (ok(i)) scale_row(u, i, o.m[0], o.m[1]);
             break;
         case L_PERM_SWAP: {
             const uint64_t a = 1ull << o.t0, b = 1ull << o.t1;
             for (uint64_t i = 0; i < N; ++i)
-                if (!(i & a) && (i & b) && ok(i)) std::swap(v[i], v[i ^ (a | b)]);
+                if (!(i & a) && (i & b) && ok(i)) swap_rows(u, i, i ^ (a | b));
             break;
         }
         case L_MATK: {
@@ -87,15 +116,26 @@ static void host_apply(std::vector<cd>& v, const LOp& o) {
                 for (int j = 0; j < o.k; ++j)
                     if ((r >> (o.k - 1 - j)) & 1) off[r] |= 1ull << o.tb[j];
             }
-            std::vector<cd> in(D);
+            std::vector<double> inr((size_t)D * u.D), ini((size_t)D * u.D);
             for (uint64_t i = 0; i < N; ++i) {
                 if ((i & tm) || !ok(i)) continue;
-                for (int c = 0; c < D; ++c) in[c] = v[i | off[c]];
+                for (int c = 0; c < D; ++c) {
+                    std::copy(u.r(i | off[c]), u.r(i | off[c]) + u.D, inr.begin() + (size_t)c * u.D);
+                    std::copy(u.q(i | off[c]), u.q(i | off[c]) + u.D, ini.begin() + (size_t)c * u.D);
+                }
                 for (int r = 0; r < D; ++r) {
-                    cd acc = 0;
-                    for (int c = 0; c < D; ++c)
-                        acc += cd(o.mk[2 * (r * D + c)], o.mk[2 * (r * D + c) + 1]) * in[c];
-                    v[i | off[r]] = acc;
+                    double *yr = u.r(i | off[r]), *yi = u.q(i | off[r]);
+                    std::fill(yr, yr + u.D, 0.0);
+                    std::fill(yi, yi + u.D, 0.0);
+                    for (int c = 0; c < D; ++c) {
+                        const double mr = o.mk[2 * (r * D + c)], mi = o.mk[2 * (r * D + c) + 1];
+                        const double* xr = inr.data() + (size_t)c * u.D;
+                        const double* xi = ini.data() + (size_t)c * u.D;
+                        for (int col = 0; col < u.D; ++col) {
+                            yr[col] += mr * xr[col] - mi * xi[col];
+                            yi[col] += mr * xi[col] + mi * xr[col];
+                        }
+                    }
                 }
             }
             break;
@@ -106,8 +146,7 @@ static void host_apply(std::vector<cd>& v, const LOp& o) {
 
 static uint64_t remap_mask(uint64_t m, const int* local) {
     uint64_t r = 0;
-    for (int b = 0; b < 64; ++b)
-        if ((m >> b) & 1ull) r |= 1ull << local[b];
+    for (; m; m &= m - 1) r |= 1ull << local[__builtin_ctzll(m)];
     return r;
 }
 
@@ -140,8 +179,7 @@ static int fuse(int n, const std::vector<LOp>& in, const std::vector<aqsg_op>& s
         if (o.cls == L_NOP) continue;
         const uint64_t s = support(o);
         int cand = -1;
-        for (int b = 0; b < 64; ++b)
-            if ((s >> b) & 1ull) cand = std::max(cand, last[b]);
+        for (uint64_t x = s; x; x &= x - 1) cand = std::max(cand, last[__builtin_ctzll(x)]);
         int g;
         if (cand >= 0 && __builtin_popcountll(groups[cand].bits | s) <= K) {
             g = cand;
@@ -151,8 +189,7 @@ static int fuse(int n, const std::vector<LOp>& in, const std::vector<aqsg_op>& s
         }
         groups[g].bits |= s;
         groups[g].ops.push_back(oi);
-        for (int b = 0; b < 64; ++b)
-            if ((s >> b) & 1ull) last[b] = g;
+        for (uint64_t x = s; x; x &= x - 1) last[__builtin_ctzll(x)] = g;
     }
     // Merge groups into the previous (else the next) group that shares a
     // qubit with them when the union stays within K qubits.  The groups in
@@ -232,17 +269,19 @@ static int fuse(int n, const std::vector<LOp>& in, const std::vector<aqsg_op>& s
         // matrix index MSB = highest global bit
         for (int j = 0; j < k; ++j) f.tb[j] = bits[k - 1 - j];
         f.mk.assign(2 * D * D, 0.0);
-        for (int c = 0; c < D; ++c) {
-            std::vector<cd> v(D, 0.0);
-            v[c] = 1.0;
-            for (const LOp& o : lops) host_apply(v, o);
-            // local index i has bit j <-> bits[j]; the matrix index r has
-            // bit (k-1-j') <-> tb[j'] = bits[k-1-j'], i.e. r == i
-            for (int r = 0; r < D; ++r) {
-                f.mk[2 * (r * D + c)] = v[r].real();
-                f.mk[2 * (r * D + c) + 1] = v[r].imag();
+        RowMat u;
+        u.D = D;
+        u.re.assign((size_t)D * D, 0.0);
+        u.im.assign((size_t)D * D, 0.0);
+        for (int c = 0; c < D; ++c) u.re[(size_t)c * D + c] = 1.0;
+        for (const LOp& o : lops) host_apply_rows(u, o);
+        // local index i has bit j <-> bits[j]; the matrix index r has
+        // bit (k-1-j') <-> tb[j'] = bits[k-1-j'], i.e. r == i
+        for (int r = 0; r < D; ++r)
+            for (int c = 0; c < D; ++c) {
+                f.mk[2 * (r * D + c)] = u.re[(size_t)r * D + c];
+                f.mk[2 * (r * D + c) + 1] = u.im[(size_t)r * D + c];
             }
-        }
         prog->mats.push_back(f.mk);
         aqsg_op ex;
         std::memset(&ex, 0, sizeof(ex));

@@ -503,19 +503,30 @@ static void tc_operand(const std::vector<double>& mk, int k, std::vector<unsigne
     const size_t split = 2ull * N * K;
     const size_t at = out.size();
     out.resize(at + 2 * split, 0);
-    for (uint32_t n = 0; n < N; ++n)
-        for (uint32_t kk = 0; kk < K; ++kk) {
-            const uint32_t r = n >> 1, c = kk >> 1;
-            const double re = mk[2 * (r * D + c)], im = mk[2 * (r * D + c) + 1];
-            double v;
-            if ((n & 1u) == 0) v = (kk & 1u) == 0 ? re : -im;
-            else v = (kk & 1u) == 0 ? im : re;
-            const uint16_t hi = host_bf16((float)v);
-            const uint16_t lo = host_bf16((float)(v - (double)host_bf16_val(hi)));
-            const uint32_t off = kmajor_off(n, kk, K);
-            std::memcpy(&out[at + off], &hi, 2);
-            std::memcpy(&out[at + split + off], &lo, 2);
+    // each complex entry is split once; -Ui is the sign-flipped split of Ui
+    // (rounding to nearest even is symmetric)
+    std::vector<uint16_t> hi(N * K), lo(N * K);
+    auto split16 = [](double v, uint16_t& h, uint16_t& l) {
+        h = host_bf16((float)v);
+        l = host_bf16((float)(v - (double)host_bf16_val(h)));
+    };
+    auto put = [&](uint32_t n, uint32_t kk, uint16_t h, uint16_t l) {
+        const uint32_t off = kmajor_off(n, kk, K) / 2u;
+        hi[off] = h;
+        lo[off] = l;
+    };
+    for (uint32_t r = 0; r < D; ++r)
+        for (uint32_t c = 0; c < D; ++c) {
+            uint16_t rh, rl, ih, il;
+            split16(mk[2 * (r * D + c)], rh, rl);
+            split16(mk[2 * (r * D + c) + 1], ih, il);
+            put(2 * r, 2 * c, rh, rl);
+            put(2 * r, 2 * c + 1, (uint16_t)(ih ^ 0x8000u), (uint16_t)(il ^ 0x8000u));
+            put(2 * r + 1, 2 * c, ih, il);
+            put(2 * r + 1, 2 * c + 1, rh, rl);
         }
+    std::memcpy(&out[at], hi.data(), split);
+    std::memcpy(&out[at + split], lo.data(), split);
 }
 
 static void pad_to(std::vector<unsigned char>& v, size_t align) {
