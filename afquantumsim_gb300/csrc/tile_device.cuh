@@ -59,6 +59,19 @@ struct CtaSync {
 struct ComputeSync512 {
     static __device__ __forceinline__ void sync() { asm volatile("bar.sync 1, 512;" ::: "memory"); }
 };
+// Barrier among the N threads of this thread's compute group (aligned
+// blocks of N threads; group q uses named barrier 1 + q), for warp-
+// specialised kernels whose groups each run their own tile.
+template <int N>
+struct GroupSync {
+    static __device__ __forceinline__ void sync() {
+        asm volatile("bar.sync %0, %1;" ::"r"(1u + threadIdx.x / (uint32_t)N), "n"(N) : "memory");
+    }
+};
+
+// Index of this thread among the nthr threads (a power of two) that run a
+// tile's ops: compute groups are aligned blocks of nthr threads.
+__device__ __forceinline__ uint32_t tile_tid(uint32_t nthr) { return threadIdx.x & (nthr - 1u); }
 
 // ---- asynchronous copies and barriers (sm_90+ bulk copies, mbarriers) -----------
 
@@ -167,8 +180,9 @@ constexpr int kTcThreads = 512;                    // 16 warps: 4 per TMEM lane 
 constexpr uint32_t kTcTmemCols = 64;               // 2^(12+1) / 128
 constexpr uint32_t kTcABytes = 4u << kTcTileBits;  // one split of A: 16 KiB
 // A pass's tensor-core operands (per op: B hi and lo splits, then the index
-// tables) are loaded into shared memory once per CTA; at most this many bytes.
-constexpr uint32_t kTcBlobMax = 76u * 1024u;
+// tables) are loaded into shared memory once per CTA; at most this many bytes
+// (three 5-qubit unitaries: 3 x 17 KiB).
+constexpr uint32_t kTcBlobMax = 52u * 1024u;
 
 __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
     uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
@@ -229,29 +243,33 @@ struct TcPhase {
 
 // One fused unitary on the tile through the tensor cores, for a unitary on KQ
 // tile bits whose operand gather puts CB lane bits on data columns (and
-// 5 - CB on matrix rows; op.lt1, chosen on the host).  All kTcThreads threads
-// call it.  A bounded wait that gives up sets the error flag (the caller
-// checks it once per tile).
+// 5 - CB on matrix rows; op.lt1, chosen on the host).  All WARPS x 32 threads
+// of the compute group call it (an aligned block of threads; t.a, t.tmem and
+// t.mma_bar are the group's own).  A bounded wait that gives up sets the
+// error flag (the caller checks it once per tile).
 //
 // The op's blob entry holds B hi, B lo (2 N K bytes each), then colbase[c]
 // (tile index of data column c; 512 x u16) and offr[r] (tile-index bits of
 // matrix row r; 32 x u16).
 //
-// Operand gather: item it (0..7) of thread (warp w, lane l) is data column
-// c = c0 + it * 2^(9-KQ) and matrix row r (both fixed by w and l), so a
+// Operand gather: item it of thread (warp w, lane l) is data column
+// c = c0 + it * CSTEP and matrix row r (both fixed by w and l), so a
 // thread's row bits and its column's low bits stay in registers; the column
 // table is linear over disjoint bits, colbase[c] = colbase[c0] |
-// colbase[it * 2^(9-KQ)], and the operand offset advances by a constant.
-template <class LAY, class SYNC, int KQ, int CB>
+// colbase[it * CSTEP], and the operand offset advances by a constant.
+template <class LAY, class SYNC, int KQ, int CB, int WARPS>
 __device__ __forceinline__ void tc_apply_k(float2* s, const TileOp& op, const TcSmem& t, TcPhase& ph) {
     constexpr uint32_t D = 1u << KQ, K = 2u * D, N = 2u * D;
     constexpr uint32_t blocks = 1u << (kTcTileBits - KQ - 7);
     constexpr uint32_t bsplit = 2u * N * K;
+    constexpr int WB = WARPS == 16 ? 4 : 3;
+    static_assert(WARPS == 16 || WARPS == 8, "compute group of 8 or 16 warps");
     constexpr int RB = 5 - CB, KD = KQ - RB;
-    static_assert(RB >= 1 && KD >= 0 && KD <= 4, "lane split");
-    constexpr uint32_t CSTEP = 1u << (9 - KQ);          // column step per item
+    static_assert(RB >= 1 && KD >= 0 && KD <= WB, "lane split");
+    constexpr int ITEMS = 1 << (7 - WB);                 // gathered amplitudes per thread
+    constexpr uint32_t CSTEP = 1u << (5 + WB - KQ);      // column step per item
     constexpr uint32_t OSTEP = (CSTEP / 8u) * 16u * K;   // operand offset step per item
-    const uint32_t tid = threadIdx.x, w = tid >> 5, lane = tid & 31u;
+    const uint32_t tid = threadIdx.x & (WARPS * 32u - 1u), w = tid >> 5, lane = tid & 31u;
     const unsigned char* bsm = t.blob + op.mat;
     const uint16_t* colbase = reinterpret_cast<const uint16_t*>(bsm + 2u * bsplit);
     const uint16_t* offr = colbase + 512;
@@ -262,8 +280,8 @@ __device__ __forceinline__ void tc_apply_k(float2* s, const TileOp& op, const Tc
         const uint32_t j0 = (uint32_t)colbase[c0] | (uint32_t)offr[r];
         const uint32_t off0 = (c0 >> 3) * 16u * K + (r >> 2) * 128u + (c0 & 7u) * 16u + (r & 3u) * 4u;
         unsigned char* ahi = t.a + off0;
-#pragma unroll
-        for (int it = 0; it < 8; ++it) {
+#pragma unroll 8
+        for (int it = 0; it < ITEMS; ++it) {
             const uint32_t j = j0 | (uint32_t)colbase[CSTEP * it];
             const float2 x = s[LAY::at(j)];
             const __nv_bfloat162 hi = __float22bfloat162_rn(x);
@@ -302,35 +320,45 @@ __device__ __forceinline__ void tc_apply_k(float2* s, const TileOp& op, const Tc
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
     // D straight to the tile: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its
-    // data columns) and the 16 columns 16 (w / 4) .. + 15 (8 output rows)
-    const uint32_t g = w & 3u, h = w >> 2;
-    uint32_t v[16];
-    tc_ld16(t.tmem + ((g * 32u) << 16) + h * 16u, v);
-    tc_ld_wait();
-    const uint32_t tcol = h * 16u;
-    const uint32_t c = ((tcol >> (KQ + 1)) << 7) + g * 32u + lane;
-    const uint32_t r0 = (tcol & (N - 1u)) >> 1;
-    const uint32_t cbase = colbase[c];
+    // data columns) and the 16-column chunks w / 4, w / 4 + WARPS / 4, ...
+    // of the 64 (8 output rows each)
+    const uint32_t g = w & 3u;
+#pragma unroll 1
+    for (uint32_t h = w >> 2; h < 4u; h += WARPS / 4u) {
+        uint32_t v[16];
+        tc_ld16(t.tmem + ((g * 32u) << 16) + h * 16u, v);
+        tc_ld_wait();
+        const uint32_t tcol = h * 16u;
+        const uint32_t c = ((tcol >> (KQ + 1)) << 7) + g * 32u + lane;
+        const uint32_t r0 = (tcol & (N - 1u)) >> 1;
+        const uint32_t cbase = colbase[c];
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
-        s[LAY::at(cbase | (uint32_t)offr[r0 + i])] =
-            make_float2(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1]));
+        for (int i = 0; i < 8; ++i)
+            s[LAY::at(cbase | (uint32_t)offr[r0 + i])] =
+                make_float2(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1]));
+    }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     SYNC::sync();
 }
 
-template <class LAY, class SYNC>
+template <class LAY, class SYNC, int WARPS>
 __device__ __forceinline__ void tc_apply(float2* s, const TileOp& op, const TcSmem& t, TcPhase& ph) {
     switch (op.k * 8 + op.lt1) {
-        case 3 * 8 + 2: tc_apply_k<LAY, SYNC, 3, 2>(s, op, t, ph); break;
-        case 3 * 8 + 3: tc_apply_k<LAY, SYNC, 3, 3>(s, op, t, ph); break;
-        case 3 * 8 + 4: tc_apply_k<LAY, SYNC, 3, 4>(s, op, t, ph); break;
-        case 4 * 8 + 2: tc_apply_k<LAY, SYNC, 4, 2>(s, op, t, ph); break;
-        case 4 * 8 + 3: tc_apply_k<LAY, SYNC, 4, 3>(s, op, t, ph); break;
-        case 4 * 8 + 4: tc_apply_k<LAY, SYNC, 4, 4>(s, op, t, ph); break;
-        case 5 * 8 + 2: tc_apply_k<LAY, SYNC, 5, 2>(s, op, t, ph); break;
-        case 5 * 8 + 3: tc_apply_k<LAY, SYNC, 5, 3>(s, op, t, ph); break;
-        default: tc_apply_k<LAY, SYNC, 5, 4>(s, op, t, ph); break;
+        case 3 * 8 + 2: tc_apply_k<LAY, SYNC, 3, 2, WARPS>(s, op, t, ph); break;
+        case 3 * 8 + 3: tc_apply_k<LAY, SYNC, 3, 3, WARPS>(s, op, t, ph); break;
+        case 3 * 8 + 4: tc_apply_k<LAY, SYNC, 3, 4, WARPS>(s, op, t, ph); break;
+        case 4 * 8 + 2: tc_apply_k<LAY, SYNC, 4, 2, WARPS>(s, op, t, ph); break;
+        case 4 * 8 + 3: tc_apply_k<LAY, SYNC, 4, 3, WARPS>(s, op, t, ph); break;
+        case 4 * 8 + 4: tc_apply_k<LAY, SYNC, 4, 4, WARPS>(s, op, t, ph); break;
+        case 5 * 8 + 2: tc_apply_k<LAY, SYNC, 5, 2, WARPS>(s, op, t, ph); break;
+        default:
+            if constexpr (WARPS == 16) {
+                if (op.lt1 == 4) tc_apply_k<LAY, SYNC, 5, 4, WARPS>(s, op, t, ph);
+                else tc_apply_k<LAY, SYNC, 5, 3, WARPS>(s, op, t, ph);
+            } else {
+                tc_apply_k<LAY, SYNC, 5, 3, WARPS>(s, op, t, ph);  // the host keeps 5 - lt1 >= 2 here
+            }
+            break;
     }
 }
 
@@ -366,7 +394,7 @@ __device__ __noinline__ void matk_apply(T* s, uint32_t size, uint32_t nthr, cons
     // G groups per thread and step share each matrix element load (small K)
     constexpr int G = K <= 3 ? 2 : 1;
     const uint32_t groups = size >> K;
-    for (uint32_t p0 = threadIdx.x; p0 < groups; p0 += G * nthr) {
+    for (uint32_t p0 = tile_tid(nthr); p0 < groups; p0 += G * nthr) {
         uint32_t jg[G];
         bool on[G];
         T v[G][D];
@@ -626,7 +654,7 @@ __device__ __forceinline__ void rphase_run(T* s, uint32_t size, uint32_t nthr, u
             if ((e >> i) & 1) o ^= bo[i];
         return o;
     };
-    for (uint32_t slot = threadIdx.x; slot < (size >> RB); slot += nthr) {
+    for (uint32_t slot = tile_tid(nthr); slot < (size >> RB); slot += nthr) {
         uint32_t jt = 0;
         for (int i = 0; i < tbits; ++i) jt |= ((slot >> i) & 1u) << ((tpos >> (4 * i)) & 15u);
         const uint32_t ajt = LAY::at(jt) * (uint32_t)sizeof(T);
@@ -748,7 +776,8 @@ __device__ __forceinline__ void rphase_run(T* s, uint32_t size, uint32_t nthr, u
 // consecutive diagonal
 // ops runs from registers: each thread keeps the same EPT elements for the
 // whole run, so the run costs one shared-memory round trip and one barrier.
-template <typename R, int EPT, bool TC, class LAY, class SYNC = CtaSync, bool MATK = true, bool RPH = !TC>
+template <typename R, int EPT, bool TC, class LAY, class SYNC = CtaSync, bool MATK = true, bool RPH = !TC,
+          int TCW = 16>
 __device__ __forceinline__ void tile_run_ops(typename Cx<R>::T* s, uint32_t size, uint32_t nthr, uint64_t base,
                                              const TileOp* __restrict__ ops, int nops,
                                              const unsigned char* __restrict__ pool, const TcSmem* tcs,
@@ -769,7 +798,7 @@ __device__ __forceinline__ void tile_run_ops(typename Cx<R>::T* s, uint32_t size
             T reg[EPT];
 #pragma unroll
             for (int e = 0; e < EPT; ++e) {
-                const uint32_t j = threadIdx.x + e * nthr;
+                const uint32_t j = tile_tid(nthr) + e * nthr;
                 if (j < size) reg[e] = s[LAY::at(j)];
             }
             int q = oi;
@@ -786,13 +815,13 @@ __device__ __forceinline__ void tile_run_ops(typename Cx<R>::T* s, uint32_t size
                 const uint32_t cm = (uint32_t)d.cm_loc, cv = (uint32_t)d.cv_loc;
 #pragma unroll
                 for (int e = 0; e < EPT; ++e) {
-                    const uint32_t j = threadIdx.x + e * nthr;
+                    const uint32_t j = tile_tid(nthr) + e * nthr;
                     if (j < size && (j & cm) == cv) reg[e] = cmul((two && ((j >> lt) & 1u)) ? ph1 : ph0, reg[e]);
                 }
             }
 #pragma unroll
             for (int e = 0; e < EPT; ++e) {
-                const uint32_t j = threadIdx.x + e * nthr;
+                const uint32_t j = tile_tid(nthr) + e * nthr;
                 if (j < size) s[LAY::at(j)] = reg[e];
             }
             SYNC::sync();
@@ -803,7 +832,7 @@ __device__ __forceinline__ void tile_run_ops(typename Cx<R>::T* s, uint32_t size
         if ((base & op.cm_ext) != op.cv_ext) continue;
         if constexpr (TC) {
             if (cls == L_MATK && op.pad) {  // tensor-core op (host marks it)
-                tc_apply<LAY, SYNC>(reinterpret_cast<float2*>(s), op, *tcs, *ph);
+                tc_apply<LAY, SYNC, TCW>(reinterpret_cast<float2*>(s), op, *tcs, *ph);
                 continue;
             }
         }
@@ -815,7 +844,7 @@ __device__ __forceinline__ void tile_run_ops(typename Cx<R>::T* s, uint32_t size
             const T m10 = ld_coef<T>(op.m, 2), m11 = ld_coef<T>(op.m, 3);
             const bool or_all = (base & op.am_ext) != 0;
             const uint32_t am = (uint32_t)op.am_loc;
-            for (uint32_t p = threadIdx.x; p < (size >> 1); p += nthr) {
+            for (uint32_t p = tile_tid(nthr); p < (size >> 1); p += nthr) {
                 const uint32_t j0 = ins0(p, lt);
                 if ((j0 & cm) != cv) continue;
                 const uint32_t a0 = LAY::at(j0), a1 = LAY::at(j0 | tb);
@@ -831,7 +860,7 @@ __device__ __forceinline__ void tile_run_ops(typename Cx<R>::T* s, uint32_t size
         } else if (cls == L_PERM_SWAP) {
             const int lo = min(op.lt0, op.lt1), hi = max(op.lt0, op.lt1);
             const uint32_t ma = 1u << op.lt0, mb = 1u << op.lt1;
-            for (uint32_t p = threadIdx.x; p < (size >> 2); p += nthr) {
+            for (uint32_t p = tile_tid(nthr); p < (size >> 2); p += nthr) {
                 const uint32_t j = ins0(ins0(p, lo), hi) | mb;  // a = 0, b = 1
                 if ((j & cm) != cv) continue;
                 const uint32_t a0 = LAY::at(j), a1 = LAY::at(j ^ (ma | mb));

@@ -147,37 +147,43 @@ k_tile_stream_multi(typename Cx<R>::T* __restrict__ sv0, uint64_t reg_stride, co
 constexpr uint32_t kRowBytes = 256;
 constexpr uint32_t kRows = 128;                     // rows of a 2^12-amplitude c64 tile
 constexpr int kTcCta = kTcThreads + 32;             // 16 compute warps + 1 producer warp
-constexpr int kTcMaxOps = 96;                       // op tables up to this size go to shared memory
+constexpr int kTcGroups = 2;                        // compute groups (tiles in flight) per CTA
+constexpr int kTcMaxOps = 48;                       // op tables up to this size go to shared memory
 constexpr uint32_t kTcRowStride = 272u;             // padded tile row in the tensor-core kernel
 static_assert(sizeof(TileOp) % 16 == 0, "op tables are bulk-copied: 16-byte multiples");
 
-// Shared memory of the tensor-core streaming kernel: three tile buffers (one
-// computing, the next loaded, the previous storing).  Rows are padded by 16
-// bytes (a 272-byte stride) so the operand gathers of rows that share their
-// low index bits spread over the banks.
-struct TcStreamSmem {
+// Shared memory of the tensor-core streaming kernel: three tile buffers (the
+// compute groups' tiles, the next loaded, the previous storing), then per
+// compute group an A operand (hi and lo splits), then the pass's operand blob.
+// Rows are padded by 16 bytes (a 272-byte stride) so the operand gathers of
+// rows that share their low index bits spread over the banks.
+template <int GROUPS>
+struct TcStreamSmemT {
     static constexpr int kBufs = 3;
     static constexpr uint32_t kRowStride = kTcRowStride;
     static constexpr uint32_t kBufBytes = kRows * kRowStride;          // 34 KiB
     static constexpr uint32_t kRowOff = kBufs * kBufBytes;              // kRows x u64
-    static constexpr uint32_t kBars = kRowOff + kRows * 8u;             // full[3] done[3] mma blob
+    static constexpr uint32_t kBars = kRowOff + kRows * 8u;             // full[3] done[3] mma[2] blob
     static constexpr uint32_t kTmemSlot = kBars + 16u * 8u;
     static constexpr uint32_t kOps = (kTmemSlot + 16u + 127u) & ~127u;  // kTcMaxOps TileOps
     static constexpr uint32_t kA = (kOps + kTcMaxOps * (uint32_t)sizeof(TileOp) + 1023u) & ~1023u;
-    static constexpr uint32_t kBlob = kA + 2u * kTcABytes;
+    static constexpr uint32_t kBlob = kA + GROUPS * 2u * kTcABytes;
     static constexpr uint32_t kBytes = kBlob + kTcBlobMax;
     static_assert(kBytes <= 232448u, "more shared memory than a CTA may have");
 };
+using TcStreamSmem = TcStreamSmemT<kTcGroups>;
 
-// any(v) over the 512 compute threads (named barrier 1)
-__device__ __forceinline__ bool compute_any(bool v) {
+// any(v) over the N threads of this thread's compute group (named barrier
+// 1 + group, as GroupSync)
+template <int N>
+__device__ __forceinline__ bool group_any(bool v) {
     uint32_t r;
     asm volatile(
         "{\n\t.reg .pred p, q;\n\t"
         "setp.ne.u32 p, %1, 0;\n\t"
-        "bar.red.or.pred q, 1, 512, p;\n\t"
+        "bar.red.or.pred q, %2, %3, p;\n\t"
         "selp.u32 %0, 1, 0, q;\n\t}"
-        : "=r"(r) : "r"((uint32_t)v) : "memory");
+        : "=r"(r) : "r"((uint32_t)v), "r"(1u + threadIdx.x / (uint32_t)N), "n"(N) : "memory");
     return r != 0;
 }
 
@@ -187,12 +193,14 @@ __device__ __forceinline__ bool compute_any(bool v) {
 // Warp 16 is the producer: it copies tiles in 16-byte cp.async chunks into
 // three shared-memory buffers (full[b] completes when all 32 lanes' chunks
 // have landed; many small requests stay in flight without the per-request
-// cost of bulk copies) and writes them back with 128-bit stores once the 16
-// compute warps have released them (done[b]); so the next tiles load and the
-// previous one stores while the compute warps run the pass's ops on the
-// current one.  The pass's operand blob and op table are bulk-loaded into
-// shared memory.  Every wait is bounded: one that gives up sets the error
-// flag and the CTA winds down.
+// cost of bulk copies) and writes them back with 128-bit stores once the
+// compute warps have released them (done[b]).  The 16 compute warps form
+// GROUPS groups; group g runs the pass's ops on the CTA's tiles g, g + GROUPS,
+// ... with its own named barrier, A operand, tensor-memory columns and MMA
+// barrier, so one group's operand gathers and write-backs overlap the other
+// group's MMAs and waits.  The pass's operand blob and op table are
+// bulk-loaded into shared memory.  Every wait is bounded: one that gives up
+// sets the error flag and the CTA winds down.
 //
 // One register (MULTI false): CTA b takes tiles b, b + grid, ...  A group of
 // `members` registers of equal plan geometry (MULTI true; the batched
@@ -201,6 +209,76 @@ __device__ __forceinline__ bool compute_any(bool v) {
 // run of the members' tiles, and where the run crosses into the next
 // register the producer reloads the blob and op table once the compute warps
 // have released the last tile of the previous one.
+// The CTA's tiles as the compute groups see them: the i-th is tile
+// local(i) of register member(i) (MULTI: a contiguous run from `first`;
+// otherwise blockIdx.x + i * gridDim.x of register 0).
+struct TcTiles {
+    uint32_t count, first, ntiles;
+    __device__ __forceinline__ uint32_t tile(uint32_t i, bool multi) const {
+        return multi ? first + i : blockIdx.x + i * gridDim.x;
+    }
+};
+
+// Compute group G = threadIdx.x / NT (named barrier 1 + G) of the
+// tensor-core streaming kernel: runs the pass's ops on the CTA's tiles G,
+// G + GROUPS, ...
+template <int NT, int GROUPS, bool MULTI, class LAY>
+__device__ __forceinline__ void tc_compute_group(unsigned char* smem_raw, const TileGeom& g, const TcTiles& tl,
+                                                 const unsigned char* __restrict__ dev0, uint64_t dev_stride,
+                                                 uint32_t op_first, int nops, uint64_t pool_off, const TileOp* sops,
+                                                 bool ops_in_smem, uint64_t* full, uint64_t* done,
+                                                 uint64_t* blob_bar, const TcSmem& tcs_in, int* err) {
+    constexpr int NB = TcStreamSmem::kBufs, M = kTcTileBits;
+    constexpr uint32_t kBufBytes = TcStreamSmem::kBufBytes;
+    using SYNC = GroupSync<NT>;
+    const uint32_t G = threadIdx.x / NT;
+    const uint32_t lane = threadIdx.x & 31u;
+    const bool gtid0 = (threadIdx.x & (NT - 1)) == 0;
+    TcSmem tcs = tcs_in;
+    TcPhase tph;
+    uint32_t blob_par = 0;
+    uint32_t cur = (MULTI && tl.count) ? tl.tile(0, true) / tl.ntiles : 0u;
+    bool ok = !group_any<NT>(!mbar_wait_bounded(blob_bar, 0, err));
+    for (uint32_t i = G; ok && i < tl.count; i += GROUPS) {
+        const uint32_t buf = i % NB;
+        const uint32_t t = tl.tile(i, MULTI);
+        const uint32_t m = MULTI ? t / tl.ntiles : 0u;
+        const uint32_t local = MULTI ? t % tl.ntiles : t;
+        if (MULTI && m != cur) {  // the producer reloads the blob after the previous register's tiles
+            blob_par ^= 1u;
+            if (group_any<NT>(!mbar_wait_bounded(blob_bar, blob_par, err))) break;
+            cur = m;
+        }
+        if (group_any<NT>(!mbar_wait_bounded(full + buf, (i / NB) & 1u, err))) break;
+        float2* s = reinterpret_cast<float2*>(smem_raw + buf * kBufBytes);
+        uint64_t base = local;  // spread over the non-tile bits
+        for (int q = 0; q < M; ++q) {
+            const int b = g.tbits[q];
+            const uint64_t lo = base & ((1ull << b) - 1ull);
+            base = ((base - lo) << 1) | lo;
+        }
+        const unsigned char* dev = dev0 + (uint64_t)m * dev_stride;
+        const TileOp* optab = ops_in_smem ? sops : reinterpret_cast<const TileOp*>(dev) + op_first;
+        tile_run_ops<float, (1 << M) / NT, true, LAY, SYNC, true, false, NT / 32>(s, 1u << M, NT, base, optab, nops,
+                                                                               dev + pool_off, &tcs, &tph);
+        fence_async_smem();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(done + buf);
+        if (group_any<NT>(gtid0 && *(volatile int*)err != 0)) break;
+    }
+    if (!ok || *(volatile int*)err != 0) {
+        if (gtid0) {
+            atomicExch(err, 1);
+            // the MMAs this group issued finish before the shared and tensor
+            // memory go (the producer waits for its own copies): the last
+            // issued commit is the phase of parity tph.mma ^ 1 (already
+            // complete, or never started on a fresh barrier, when nothing is
+            // outstanding)
+            mbar_wait_timeout(tcs.mma_bar, tph.mma ^ 1u);
+        }
+    }
+}
+
 template <bool MULTI>
 __global__ void __launch_bounds__(kTcCta, 1)
 k_stream_tc(float2* __restrict__ sv0, const TileGeom g, const unsigned char* __restrict__ dev0, uint32_t op_first,
@@ -208,31 +286,32 @@ k_stream_tc(float2* __restrict__ sv0, const TileGeom g, const unsigned char* __r
             uint64_t dev_stride) {
     using SM = TcStreamSmem;
     constexpr int NB = SM::kBufs;
+    constexpr int GROUPS = kTcGroups;
+    constexpr int NT = kTcThreads / GROUPS;  // threads per compute group
     constexpr int L = 5, M = 12;
     constexpr uint32_t kRowStride = SM::kRowStride, kBufBytes = SM::kBufBytes;
     using LAY = TileLay<L, (int)((kRowStride - kRowBytes) / sizeof(float2))>;
-    constexpr int EPT = (1 << M) / kTcThreads;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     uint64_t* rowoff = reinterpret_cast<uint64_t*>(smem_raw + SM::kRowOff);
     uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + SM::kBars);
     uint64_t* done = full + NB;
-    uint64_t* mma_bar = full + 2 * NB;
-    uint64_t* blob_bar = mma_bar + 1;
+    uint64_t* mma_bar = full + 2 * NB;  // one per compute group
+    uint64_t* blob_bar = mma_bar + GROUPS;
     TileOp* sops = reinterpret_cast<TileOp*>(smem_raw + SM::kOps);
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
     const bool ops_in_smem = nops <= kTcMaxOps;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                     ::"r"(smem_u32(smem_raw + SM::kTmemSlot)), "r"(kTcTmemCols));
+                     ::"r"(smem_u32(smem_raw + SM::kTmemSlot)), "r"(kTcTmemCols * GROUPS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
         for (int b = 0; b < NB; ++b) {
             mbar_init(full + b, 32);  // one cp.async arrival per producer lane
-            mbar_init(done + b, kTcThreads / 32);
+            mbar_init(done + b, NT / 32);
         }
-        mbar_init(mma_bar, 1);
+        for (int q = 0; q < GROUPS; ++q) mbar_init(mma_bar + q, 1);
         mbar_init(blob_bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -305,8 +384,8 @@ k_stream_tc(float2* __restrict__ sv0, const TileGeom g, const unsigned char* __r
                 if (lane == 0) atomicExch(err, 1);
                 break;
             }
-            // the compute warps have released tile i: at a change of register
-            // its blob and op table may be replaced
+            // tiles are released in order, so every tile up to i is done: at
+            // a change of register its blob and op table may be replaced
             if (MULTI && lane == 0 && i + 1 < count && member_of(i + 1) != member_of(i)) load_blob(member_of(i + 1));
             float2* dstg = sv_of(member_of(i)) + tile_base(local_of(i));
             const unsigned char* src = smem_raw + buf * kBufBytes;
@@ -324,46 +403,20 @@ k_stream_tc(float2* __restrict__ sv0, const TileGeom g, const unsigned char* __r
         asm volatile("cp.async.wait_all;" ::: "memory");
         if (lane == 0 && blob_loads > 0) mbar_wait_timeout(blob_bar, (blob_loads - 1u) & 1u);
     } else {
-        // ---- compute warps ----
+        // ---- compute groups ----
+        const uint32_t grp = warp / (NT / 32);
         TcSmem tcs;
-        TcPhase tph;
-        tcs.a = smem_raw + SM::kA;
+        tcs.a = smem_raw + SM::kA + grp * 2u * kTcABytes;
         tcs.blob = smem_raw + SM::kBlob;
-        tcs.mma_bar = mma_bar;
-        tcs.tmem = *reinterpret_cast<volatile uint32_t*>(smem_raw + SM::kTmemSlot);
+        tcs.mma_bar = mma_bar + grp;
+        tcs.tmem = *reinterpret_cast<volatile uint32_t*>(smem_raw + SM::kTmemSlot) + grp * kTcTmemCols;
         tcs.err = err;
-        uint32_t blob_par = 0, cur = count ? member_of(0) : 0u;
-        bool ok = !compute_any(!mbar_wait_bounded(blob_bar, 0, err));
-        for (uint32_t i = 0; ok && i < count; ++i) {
-            const uint32_t buf = i % NB;
-            const uint32_t m = member_of(i);
-            if (MULTI && m != cur) {  // the producer reloads the blob after tile i - 1
-                blob_par ^= 1u;
-                if (compute_any(!mbar_wait_bounded(blob_bar, blob_par, err))) break;
-                cur = m;
-            }
-            if (compute_any(!mbar_wait_bounded(full + buf, (i / NB) & 1u, err))) break;
-            float2* s = reinterpret_cast<float2*>(smem_raw + buf * kBufBytes);
-            const uint64_t base = tile_base(local_of(i));
-            const TileOp* optab = ops_in_smem ? sops : reinterpret_cast<const TileOp*>(dev_of(m)) + op_first;
-            tile_run_ops<float, EPT, true, LAY, ComputeSync512>(s, 1u << M, kTcThreads, base, optab, nops,
-                                                               dev_of(m) + pool_off, &tcs, &tph);
-            fence_async_smem();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(done + buf);
-            if (compute_any(tid == 0 && *(volatile int*)err != 0)) break;
-        }
-        if (!ok || *(volatile int*)err != 0) {
-            if (tid == 0) {
-                atomicExch(err, 1);
-                // the MMAs this CTA issued finish before the shared and
-                // tensor memory go (the producer waits for its own copies):
-                // the last issued commit is the phase of parity tph.mma ^ 1
-                // (already complete, or never started on a fresh barrier,
-                // when nothing is outstanding)
-                mbar_wait_timeout(mma_bar, tph.mma ^ 1u);
-            }
-        }
+        TcTiles tl;
+        tl.count = count;
+        tl.first = first;
+        tl.ntiles = ntiles;
+        tc_compute_group<NT, GROUPS, MULTI, LAY>(smem_raw, g, tl, dev0, dev_stride, op_first, nops, pool_off, sops,
+                                                  ops_in_smem, full, done, blob_bar, tcs, err);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -371,7 +424,7 @@ k_stream_tc(float2* __restrict__ sv0, const TileGeom g, const unsigned char* __r
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(
                          *reinterpret_cast<volatile uint32_t*>(smem_raw + SM::kTmemSlot)),
-                     "r"(kTcTmemCols));
+                     "r"(kTcTmemCols * GROUPS));
     }
 }
 
@@ -605,7 +658,9 @@ static void tc_tables(TileOp& t, std::vector<unsigned char>& blob) {
     int best_cb = 3, best_cost = 1 << 30;
     for (int cb = 2; cb <= 4; ++cb) {
         const int rb = 5 - cb;
-        if (rb > k) continue;
+        // the row bits beyond the lane's come from the warp index within a
+        // compute group of 16 / kTcGroups warps
+        if (rb > k || k - rb > (kTcGroups == 1 ? 4 : 3)) continue;
         int cost = 0;
         for (uint32_t w = 0; w < 4; ++w) {
             int rd[16] = {0}, wr[32] = {0};
