@@ -596,6 +596,16 @@ def run_ours(args, rank, world, local_rank):
         r.apply(ops, mode)
         r.download_async_ptr(ho.data_ptr())
         c.synchronize()
+    # the host link's copy rate on this run (the pipeline hides the copies
+    # only while each takes less than a step's gates)
+    t_c = time.perf_counter()
+    st.upload_ptr(host_in.data_ptr())
+    ctx.synchronize()
+    h2d_s = time.perf_counter() - t_c
+    t_c = time.perf_counter()
+    st.download_async_ptr(host_out.data_ptr())
+    ctx.synchronize()
+    d2h_s = time.perf_counter() - t_c
     if world > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
@@ -624,6 +634,7 @@ def run_ours(args, rank, world, local_rank):
     e2e = {"value": round(world * gates * e2e_steps / e2e_s, 3), "unit": "gate-apps/s",
            "h2d_bytes_per_step": N * amp_b, "d2h_bytes_per_step": N * amp_b,
            "ms_per_step": round(e2e_s / e2e_steps * 1e3, 3), "steps": e2e_steps,
+           "h2d_gbs": round(N * amp_b / h2d_s / 1e9, 1), "d2h_gbs": round(N * amp_b / d2h_s / 1e9, 1),
            "pipeline": "two registers on two streams, gates of consecutive steps ordered (aqsg_ctx_after); "
                        "each step uploads its input and reads its result under the other register's gates"}
 
