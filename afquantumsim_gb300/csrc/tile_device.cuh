@@ -52,12 +52,9 @@ struct TileLay {
 using FlatLay = TileLay<0, 0>;
 
 // Barrier among the threads that run a tile's ops: the whole CTA, or (in a
-// warp-specialised kernel) the first 512 threads on named barrier 1.
+// warp-specialised kernel) one compute group (GroupSync below).
 struct CtaSync {
     static __device__ __forceinline__ void sync() { __syncthreads(); }
-};
-struct ComputeSync512 {
-    static __device__ __forceinline__ void sync() { asm volatile("bar.sync 1, 512;" ::: "memory"); }
 };
 // Barrier among the N threads of this thread's compute group (aligned
 // blocks of N threads; group q uses named barrier 1 + q), for warp-
@@ -176,8 +173,8 @@ __device__ __forceinline__ void fence_async_smem() {
 // amplitude into one 4-byte operand word.
 
 constexpr int kTcTileBits = 12;
-constexpr int kTcThreads = 512;                    // 16 warps: 4 per TMEM lane quarter
-constexpr uint32_t kTcTmemCols = 64;               // 2^(12+1) / 128
+constexpr int kTcThreads = 512;                    // compute threads: 16 warps in 1 or 2 groups
+constexpr uint32_t kTcTmemCols = 64;               // per compute group: 2^(12+1) / 128
 constexpr uint32_t kTcABytes = 4u << kTcTileBits;  // one split of A: 16 KiB
 // A pass's tensor-core operands (per op: B hi and lo splits, then the index
 // tables) are loaded into shared memory once per CTA; at most this many bytes

@@ -147,6 +147,7 @@ k_tile_stream_multi(typename Cx<R>::T* __restrict__ sv0, uint64_t reg_stride, co
 constexpr uint32_t kRowBytes = 256;
 constexpr uint32_t kRows = 128;                     // rows of a 2^12-amplitude c64 tile
 constexpr int kTcCta = kTcThreads + 32;             // 16 compute warps + 1 producer warp
+                                                    // (17 warps: at most 96 registers per thread)
 constexpr int kTcGroups = 2;                        // compute groups (tiles in flight) per CTA
 constexpr int kTcMaxOps = 48;                       // op tables up to this size go to shared memory
 constexpr uint32_t kTcRowStride = 272u;             // padded tile row in the tensor-core kernel
