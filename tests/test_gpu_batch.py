@@ -100,3 +100,29 @@ def test_batch_groups_of_equal_structure(gpu_ctx):
         assert np.max(np.abs(za[0] - z[k])) < 1e-12
         alone.free()
     b.free()
+
+
+def test_batch_groups_on_tensor_cores(gpu_ctx):
+    """VQE registers of 17 qubits tune to fused unitaries on the tensor
+    cores; a group of them runs one persistent tensor-core launch per pass
+    whose CTAs cross from one register's tiles into the next (reloading the
+    operands): every register matches the oracle and equals the same circuit
+    run alone."""
+    rng = np.random.default_rng(7)
+    shapes = [(17, 4)] * 6
+    items = [(n, circuits.vqe_ops_array(n, L, rng.uniform(-np.pi, np.pi, size=(L, n, 2)))) for n, L in shapes]
+    b = aq.Batch(gpu_ctx, items)
+    info = b.info()
+    assert info["large"] == 6 and all(info["tensor_cores"]), info
+    z, zz = b.run()
+    for (n, ops), zi, zzi in zip(items, z, zz):
+        wz, wzz = oracle_z(n, ops)
+        assert np.max(np.abs(zi - wz)) < 1e-5
+        assert np.max(np.abs(zzi - wzz)) < 1e-5
+    n, ops = items[3]
+    alone = aq.Batch(gpu_ctx, [(n, ops)])
+    za, zza = alone.run()
+    np.testing.assert_array_equal(za[0], z[3])
+    np.testing.assert_array_equal(zza[0], zz[3])
+    alone.free()
+    b.free()
