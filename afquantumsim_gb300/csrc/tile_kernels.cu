@@ -922,7 +922,7 @@ bool relocate_tile_matrices(unsigned char* table, size_t count, int32_t delta) {
                 }
             }
             q += (size_t)t.k;
-        } else if (t.cls == L_MATK) {
+        } else if (t.cls == L_MATK && !t.pad) {  // (a tensor-core op's offset is into its pass's blob)
             t.mat += delta;
             any = true;
             std::memcpy(table + q * sizeof(TileOp), &t, sizeof(TileOp));
