@@ -86,6 +86,14 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def measured_bf16_tflops():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["bf16_tflops"]), "measured (burst)"
+    return 1900.0, "fallback (burst)"
+
+
 # ---- clocks -------------------------------------------------------------------------
 
 class ClockSampler:
@@ -223,6 +231,22 @@ def bench_fused_brickwork(ctx, st, stream, n, depth):
     prog.run(st, aq.EXEC_TILED)
     res["fused_tensor_core_ms"] = round(_time_ms(stream, lambda: prog.run(st, aq.EXEC_TILED), 3), 2)
     res["speedup_fused_vs_tiled"] = round(res["tiled_ms"] / res["fused_tensor_core_ms"], 2)
+    # tensor-pipe work of the fused run: a k-qubit unitary on the tensor
+    # cores is three bf16 products of (2^n / 2^k) x 2^(k+1) x 2^(k+1) per
+    # register = 24 x 2^n x 2^k flops (k >= 3, not a permutation)
+    flops = 0.0
+    for o in prog.export():
+        k = o.num_qubits
+        if o.kind == aq.kinds.UNITARY and k >= 3:
+            m = np.ctypeslib.as_array(o.matrix, shape=(2 * (1 << k) * (1 << k),))
+            mat = m[0::2] + 1j * m[1::2]
+            if not np.all((mat == 0) | (mat == 1)):
+                flops += 24.0 * N * (1 << k)
+    bf16_peak = measured_bf16_tflops()
+    tflops = flops / (res["fused_tensor_core_ms"] / 1e3) / 1e12
+    res["tensor"] = {"flops_per_run": flops, "tflops": round(tflops, 1), "peak_tflops": bf16_peak[0],
+                     "peak_source": bf16_peak[1], "frac": round(tflops / bf16_peak[0], 4),
+                     "note": "3-term split-bf16 products of the fused unitaries of >= 3 qubits"}
     # what the autotuner picks for this circuit (all choices timed once)
     best, every = aq.autotune(ctx, n, ops, aq.C64, reps=1)
     res["autotune_best"] = {k: best[k] for k in ("exec_mode", "fuse_qubits", "tensor_cores", "ms")}
