@@ -203,6 +203,9 @@ __device__ __forceinline__ bool group_any(bool v) {
 // bulk-loaded into shared memory.  Every wait is bounded: one that gives up
 // sets the error flag and the CTA winds down.
 //
+// MATK: the pass also has dense k-qubit ops on the CUDA cores (the variant
+// without that path keeps its registers: the path is a call).
+//
 // One register (MULTI false): CTA b takes tiles b, b + grid, ...  A group of
 // `members` registers of equal plan geometry (MULTI true; the batched
 // engine): register m starts reg_stride amplitudes after register m-1, its
@@ -223,7 +226,7 @@ struct TcTiles {
 // Compute group G = threadIdx.x / NT (named barrier 1 + G) of the
 // tensor-core streaming kernel: runs the pass's ops on the CTA's tiles G,
 // G + GROUPS, ...
-template <int NT, int GROUPS, bool MULTI, class LAY>
+template <int NT, int GROUPS, bool MULTI, bool MATK, class LAY>
 __device__ __forceinline__ void tc_compute_group(unsigned char* smem_raw, const TileGeom& g, const TcTiles& tl,
                                                  const unsigned char* __restrict__ dev0, uint64_t dev_stride,
                                                  uint32_t op_first, int nops, uint64_t pool_off, const TileOp* sops,
@@ -260,8 +263,8 @@ __device__ __forceinline__ void tc_compute_group(unsigned char* smem_raw, const 
         }
         const unsigned char* dev = dev0 + (uint64_t)m * dev_stride;
         const TileOp* optab = ops_in_smem ? sops : reinterpret_cast<const TileOp*>(dev) + op_first;
-        tile_run_ops<float, (1 << M) / NT, true, LAY, SYNC, true, false, NT / 32>(s, 1u << M, NT, base, optab, nops,
-                                                                               dev + pool_off, &tcs, &tph);
+        tile_run_ops<float, (1 << M) / NT, true, LAY, SYNC, MATK, false, NT / 32>(s, 1u << M, NT, base, optab, nops,
+                                                                                dev + pool_off, &tcs, &tph);
         fence_async_smem();
         __syncwarp();
         if (lane == 0) mbar_arrive(done + buf);
@@ -280,7 +283,7 @@ __device__ __forceinline__ void tc_compute_group(unsigned char* smem_raw, const 
     }
 }
 
-template <bool MULTI>
+template <bool MULTI, bool MATK>
 __global__ void __launch_bounds__(kTcCta, 1)
 k_stream_tc(float2* __restrict__ sv0, const TileGeom g, const unsigned char* __restrict__ dev0, uint32_t op_first,
             int nops, uint64_t pool_off, int* err, uint32_t ntiles, uint32_t members, uint64_t reg_stride,
@@ -416,8 +419,8 @@ k_stream_tc(float2* __restrict__ sv0, const TileGeom g, const unsigned char* __r
         tl.count = count;
         tl.first = first;
         tl.ntiles = ntiles;
-        tc_compute_group<NT, GROUPS, MULTI, LAY>(smem_raw, g, tl, dev0, dev_stride, op_first, nops, pool_off, sops,
-                                                  ops_in_smem, full, done, blob_bar, tcs, err);
+        tc_compute_group<NT, GROUPS, MULTI, MATK, LAY>(smem_raw, g, tl, dev0, dev_stride, op_first, nops, pool_off,
+                                                        sops, ops_in_smem, full, done, blob_bar, tcs, err);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -1096,14 +1099,18 @@ static int launch_plan_t(void* sv, const TilePlan& plan, const void* dev, cudaSt
         if (p.tc) {  // c64, 12 tile bits (streaming, or the whole 12-qubit register)
             if (geo.m != kTcTileBits || sizeof(R) != 4)
                 return set_error(AQSG_ERR_RUNTIME, "Tensor-core pass with an unexpected tile shape");
-            if (!have_t) {
-                if (int rc = stream_shape(k_stream_tc<false>, kTcCta, (int)TcStreamSmem::kBytes, &tshape)) return rc;
+            auto ktc = p.matk ? k_stream_tc<false, true> : k_stream_tc<false, false>;
+            if (!have_t) {  // both variants have the same shape
+                if (int rc = stream_shape(k_stream_tc<false, true>, kTcCta, (int)TcStreamSmem::kBytes, &tshape))
+                    return rc;
+                if (int rc = stream_shape(k_stream_tc<false, false>, kTcCta, (int)TcStreamSmem::kBytes, &tshape))
+                    return rc;
                 have_t = true;
             }
             if (p.tc_bytes > kTcBlobMax) return set_error(AQSG_ERR_RUNTIME, "Tensor-core operands exceed the blob");
             const uint32_t tiles = 1u << (n - geo.m);
             const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)(tshape.sms * tshape.per_sm));
-            k_stream_tc<false><<<grid, kTcCta, TcStreamSmem::kBytes, stream>>>(
+            ktc<<<grid, kTcCta, TcStreamSmem::kBytes, stream>>>(
                 (float2*)sv, geo, (const unsigned char*)dev, p.first, (int)p.count, plan.pool_offset(), d_err, tiles,
                 1u, 0ull, 0ull);
         } else if (geo.m == n) {
@@ -1148,13 +1155,17 @@ int launch_tile_plan_multi(void* sv0, uint64_t reg_stride, int members, const Ti
         const uint64_t blocks = (uint64_t)tiles * (uint64_t)members;
         if (blocks > 0x7fffffffull) return set_error(AQSG_ERR_RUNTIME, "Too many tiles in one grouped pass");
         if (p.tc) {
-            if (!have_t) {
-                if (int rc = stream_shape(k_stream_tc<true>, kTcCta, (int)TcStreamSmem::kBytes, &tshape)) return rc;
+            auto ktc = p.matk ? k_stream_tc<true, true> : k_stream_tc<true, false>;
+            if (!have_t) {  // both variants have the same shape
+                if (int rc = stream_shape(k_stream_tc<true, true>, kTcCta, (int)TcStreamSmem::kBytes, &tshape))
+                    return rc;
+                if (int rc = stream_shape(k_stream_tc<true, false>, kTcCta, (int)TcStreamSmem::kBytes, &tshape))
+                    return rc;
                 have_t = true;
             }
             if (p.tc_bytes > kTcBlobMax) return set_error(AQSG_ERR_RUNTIME, "Tensor-core operands exceed the blob");
             const uint32_t grid = (uint32_t)std::min<uint64_t>(blocks, (uint64_t)tshape.sms * tshape.per_sm);
-            k_stream_tc<true><<<grid, kTcCta, TcStreamSmem::kBytes, stream>>>(
+            ktc<<<grid, kTcCta, TcStreamSmem::kBytes, stream>>>(
                 (float2*)sv0, geo, (const unsigned char*)dev0, p.first, (int)p.count, plan.pool_offset(), d_err,
                 tiles, (uint32_t)members, reg_stride, dev_stride);
         } else {
