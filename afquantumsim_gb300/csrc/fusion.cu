@@ -274,7 +274,57 @@ static int fuse(int n, const std::vector<LOp>& in, const std::vector<aqsg_op>& s
         u.re.assign((size_t)D * D, 0.0);
         u.im.assign((size_t)D * D, 0.0);
         for (int c = 0; c < D; ++c) u.re[(size_t)c * D + c] = 1.0;
-        for (const LOp& o : lops) host_apply_rows(u, o);
+        // consecutive uncontrolled 2x2 gates on one qubit (RotY then RotZ, ...)
+        // act on the rows as their product: one row pass instead of several
+        for (size_t q = 0; q < lops.size();) {
+            const LOp& o = lops[q];
+            auto single = [](const LOp& x) {
+                return (x.cls == L_MAT2 || x.cls == L_DIAG2) && x.cmask == 0 && x.t0 >= 0;
+            };
+            if (!single(o)) {
+                host_apply_rows(u, o);
+                ++q;
+                continue;
+            }
+            // product m (row-major 2x2, complex as re/im pairs) of the run
+            auto mat_of = [](const LOp& x, double* m) {
+                if (x.cls == L_MAT2) {
+                    for (int e = 0; e < 8; ++e) m[e] = x.m[e];
+                } else {  // diag(m0, m1)
+                    m[0] = x.m[0]; m[1] = x.m[1]; m[2] = 0; m[3] = 0;
+                    m[4] = 0; m[5] = 0; m[6] = x.m[2]; m[7] = x.m[3];
+                }
+            };
+            double m[8];
+            mat_of(o, m);
+            size_t r = q + 1;
+            for (; r < lops.size() && single(lops[r]) && lops[r].t0 == o.t0; ++r) {
+                double b[8], c[8];
+                mat_of(lops[r], b);
+                for (int i = 0; i < 2; ++i)
+                    for (int j = 0; j < 2; ++j) {  // c = b m
+                        double re = 0, im = 0;
+                        for (int k = 0; k < 2; ++k) {
+                            const double br = b[2 * (2 * i + k)], bi = b[2 * (2 * i + k) + 1];
+                            const double mr = m[2 * (2 * k + j)], mi = m[2 * (2 * k + j) + 1];
+                            re += br * mr - bi * mi;
+                            im += br * mi + bi * mr;
+                        }
+                        c[2 * (2 * i + j)] = re;
+                        c[2 * (2 * i + j) + 1] = im;
+                    }
+                for (int e = 0; e < 8; ++e) m[e] = c[e];
+            }
+            if (r == q + 1) {
+                host_apply_rows(u, o);
+            } else {
+                LOp p2 = o;
+                p2.cls = L_MAT2;
+                for (int e = 0; e < 8; ++e) p2.m[e] = m[e];
+                host_apply_rows(u, p2);
+            }
+            q = r;
+        }
         // local index i has bit j <-> bits[j]; the matrix index r has
         // bit (k-1-j') <-> tb[j'] = bits[k-1-j'], i.e. r == i
         for (int r = 0; r < D; ++r)
