@@ -42,7 +42,7 @@ EXPORTS = [
     "aqsg_server_create", "aqsg_server_submit", "aqsg_server_start", "aqsg_server_poll",
     "aqsg_server_wait_idle", "aqsg_server_get_stats", "aqsg_server_destroy",
     "aqsg_expect_pauli", "aqsg_autotune", "aqsg_batch_tuning", "aqsg_selftest_bounded_wait",
-    "aqsg_state_download_async",
+    "aqsg_state_download_async", "aqsg_circuit_to_text", "aqsg_circuit_from_text",
 ]
 
 _lib = None
@@ -120,6 +120,9 @@ def load_library(path: os.PathLike | str | None = None) -> C.CDLL:
         "aqsg_selftest_bounded_wait": ([P, C.c_uint32, C.POINTER(I)], I),
         "aqsg_sample_noalloc": ([P, C.POINTER(D), U64, I, C.POINTER(U64)], I),
         "aqsg_state_compare": ([P, P] + [C.POINTER(D)] * 5, I),
+        "aqsg_circuit_to_text": ([I, C.POINTER(Op), I, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)], I),
+        "aqsg_circuit_from_text": ([C.c_char_p, C.POINTER(I), C.POINTER(Op), I, C.POINTER(I),
+                                    C.POINTER(D), C.c_size_t, C.POINTER(C.c_size_t)], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -452,6 +455,34 @@ class State:
         return out[0::2][: len(strings)] + 1j * out[1::2][: len(strings)]
 
 
+def circuit_to_text(n: int, ops) -> str:
+    """aqsg_circuit_to_text: the circuit as text (the reference's gate
+    representation with parameters, a "n;" header and "~q" zero-controls)."""
+    lib = load_library()
+    arr = op_array(list(ops)) if not isinstance(ops, C.Array) else ops
+    need = C.c_size_t()
+    _check(lib.aqsg_circuit_to_text(n, arr, len(arr), None, 0, C.byref(need)))
+    buf = C.create_string_buffer(need.value)
+    _check(lib.aqsg_circuit_to_text(n, arr, len(arr), buf, need.value, C.byref(need)))
+    return buf.value.decode("utf-8")
+
+
+def circuit_from_text(text: str):
+    """aqsg_circuit_from_text: (n, ops) with the ops as an aqsg_op array
+    (unitary matrices kept alive by the array)."""
+    lib = load_library()
+    raw = text.encode("utf-8")
+    n, cnt, nd = C.c_int(), C.c_int(), C.c_size_t()
+    _check(lib.aqsg_circuit_from_text(raw, C.byref(n), None, 0, C.byref(cnt), None, 0, C.byref(nd)))
+    arr = (Op * max(cnt.value, 1))()
+    mats = (C.c_double * max(nd.value, 1))()
+    _check(lib.aqsg_circuit_from_text(raw, C.byref(n), arr, cnt.value, C.byref(cnt), mats, nd.value,
+                                      C.byref(nd)))
+    out = (Op * cnt.value).from_buffer(arr)
+    out._keep = (arr, mats)
+    return n.value, out
+
+
 def check_ops(n: int, ops) -> None:
     lib = load_library()
     arr = op_array(list(ops))
@@ -666,6 +697,12 @@ class Server:
                                            out.ctypes.data_as(C.POINTER(C.c_uint64)), C.byref(t)))
         self._outs[t.value] = out[:shots]
         return t.value
+
+    def submit_text(self, text: str, shots: int = 1024, seed: int = 0, arrival_s: float = -1.0,
+                    fuse_qubits: int = 0) -> int:
+        """Submit a request written as circuit text (aqsg_circuit_from_text)."""
+        n, ops = circuit_from_text(text)
+        return self.submit(n, ops, shots, seed, arrival_s, fuse_qubits)
 
     def start(self) -> None:
         _check(self.lib.aqsg_server_start(self.h))

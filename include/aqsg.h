@@ -268,6 +268,38 @@ int aqsg_program_export(aqsg_program prog, aqsg_op* out, int capacity, int* coun
 
 int aqsg_program_free(aqsg_program prog);
 
+/* ---- circuit text ------------------------------------------------------------ */
+
+/* Circuits as text: the reference's gate representation ("Name,controls,
+ * targets:controls...,targets...;", QGate::to_string, src/quantum.cpp:
+ * 569-1662; the layout parse_circuit_representation reads, src/
+ * quantum_visuals.cpp:71-80) extended into a replayable wire format for
+ * request streams and golden files:
+ *   "n;"                      header: the qubit count
+ *   "RotX(0.25),0,1:3;"       parameters after the name: an angle (float,
+ *                             printed to round-trip exactly), or for "U" the
+ *                             2^k x 2^k matrix as (re, im) doubles, row-major
+ *   "X,1,1:0,2;" "X,2,1:0,1,2;"  base gate name with its controls first
+ *                             (CX, CCNot), as the reference writes them
+ *   "Z,1,1:~4,2;"             a control that fires on |0>
+ *   "Or,2,1:0,1,2;"  "B;"     Or; a barrier ("P;" reads as one too)
+ * Reference names that fix an angle read as their gates: S, S†, T, T†.
+ * Written text is canonical (parse, then write, gives the same text). */
+
+/* Write ops as text into buf (len bytes, NUL-terminated); *needed receives
+ * the size including the NUL.  buf may be NULL to query the size.  The ops
+ * are validated first (aqsg_check_ops). */
+int aqsg_circuit_to_text(int n, const aqsg_op* ops, int count, char* buf, size_t len, size_t* needed);
+
+/* Parse text into *n and ops[0 .. *count).  Unitary matrices are copied into
+ * matrices (matrix_capacity doubles) and the ops point there; with ops ==
+ * NULL only *n, *count and *matrix_count (doubles needed) are set.  Syntax
+ * errors return AQSG_ERR_INVALID_ARGUMENT with the offending token in
+ * aqsg_last_error; the parsed ops are validated like aqsg_check_ops (the
+ * reference's exception classes and messages). */
+int aqsg_circuit_from_text(const char* text, int* n, aqsg_op* ops, int capacity, int* count,
+                           double* matrices, size_t matrix_capacity, size_t* matrix_count);
+
 /* ---- autotuner ------------------------------------------------------------- */
 
 /* One way of running a circuit and its measured time. */

@@ -131,3 +131,20 @@ def test_server_close_with_queued_requests():
     t0 = time.perf_counter()
     srv.close()
     assert time.perf_counter() - t0 < 5.0
+
+
+def test_server_requests_as_text(gpu_ctx):
+    """A request submitted as circuit text gives the outcomes of the same ops
+    submitted directly."""
+    reqs = requests(3, seed=44, n_range=(8, 14), depth_range=(2, 4))
+    srv = aq.Server(0, aq.C64, 1 << 22, 2, 14, SHOTS)
+    t_ops = [srv.submit(r["n"], r["ops"], SHOTS, r["seed"], -1.0, r["fuse"]) for r in reqs]
+    t_txt = [srv.submit_text(aq.circuit_to_text(r["n"], r["ops"]), SHOTS, r["seed"], -1.0, r["fuse"])
+             for r in reqs]
+    srv.start()
+    srv.wait_idle(120)
+    done = {d["ticket"]: d for d in srv.poll(16)}
+    srv.close()
+    for a, b in zip(t_ops, t_txt):
+        assert done[a]["status"] == 0 and done[b]["status"] == 0
+        np.testing.assert_array_equal(done[a]["outcomes"], done[b]["outcomes"])
