@@ -34,15 +34,25 @@ using TileSwz = SwzLay<sizeof(R) == 4 ? 4 : 3>;
 // Whole-register passes (n <= 14 c64 / 13 c128): one CTA holds the register.
 // EPT: elements per thread in register runs; MATK: the pass has dense
 // k-qubit ops on CUDA cores.
+// ops_smem: the op table is staged in shared memory after the register (one
+// CTA reads each op once, so from global memory every op would be a cold
+// load on the critical path).
 template <typename R, int EPT, bool MATK>
 __global__ void __launch_bounds__(512, 1)
 k_tile(typename Cx<R>::T* __restrict__ sv, const TileGeom g, const TileOp* __restrict__ ops, int nops,
-       const unsigned char* __restrict__ pool) {
+       const unsigned char* __restrict__ pool, int ops_smem) {
     using T = typename Cx<R>::T;
     using LAY = TileSwz<R>;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     const uint32_t size = 1u << g.m;
     T* s = reinterpret_cast<T*>(smem_raw);
+    if (ops_smem) {
+        uint4* dst = reinterpret_cast<uint4*>(smem_raw + sizeof(T) * size);
+        const uint4* src = reinterpret_cast<const uint4*>(ops);
+        const uint32_t words = (uint32_t)nops * (uint32_t)(sizeof(TileOp) / 16);
+        for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) dst[i] = __ldg(src + i);
+        ops = reinterpret_cast<const TileOp*>(dst);
+    }
     if constexpr (sizeof(R) == 4) {
         for (uint32_t i = threadIdx.x; i < (size >> 1); i += blockDim.x) {
             const float4 x = __ldcs(reinterpret_cast<const float4*>(sv) + i);
@@ -1081,9 +1091,9 @@ static int launch_plan_t(void* sv, const TilePlan& plan, const void* dev, cudaSt
     auto kwhole_k = k_tile<R, EPT_WHOLE, true>;
     auto kplain = k_tile_stream<R, (1 << M_STREAM) / 256, false>;
     auto kplain_k = k_tile_stream<R, (1 << M_STREAM) / 256, true>;
-    const int whole_shm = (int)(sizeof(T) << tile_max_bits(plan.dtype));
-    AQSG_CUDA_TRY(cudaFuncSetAttribute(kwhole, cudaFuncAttributeMaxDynamicSharedMemorySize, whole_shm));
-    AQSG_CUDA_TRY(cudaFuncSetAttribute(kwhole_k, cudaFuncAttributeMaxDynamicSharedMemorySize, whole_shm));
+    constexpr int kWholeShmMax = 232448;  // the register plus, where it fits, its op table
+    AQSG_CUDA_TRY(cudaFuncSetAttribute(kwhole, cudaFuncAttributeMaxDynamicSharedMemorySize, kWholeShmMax));
+    AQSG_CUDA_TRY(cudaFuncSetAttribute(kwhole_k, cudaFuncAttributeMaxDynamicSharedMemorySize, kWholeShmMax));
     StreamShape tshape;
     bool have_t = false;
     for (const TilePass& p : plan.passes) {
@@ -1117,8 +1127,10 @@ static int launch_plan_t(void* sv, const TilePlan& plan, const void* dev, cudaSt
             const int rb = phase_reg_bits(plan.dtype);
             int threads = (int)(geo.m >= rb + kPhaseMinSlotBits ? size >> rb : size / EPT_WHOLE);
             threads = threads < 32 ? 32 : (threads > 512 ? 512 : threads);
-            (p.matk ? kwhole_k : kwhole)<<<1, threads, sizeof(T) * size, stream>>>((T*)sv, geo, dops + p.first,
-                                                                               (int)p.count, dpool);
+            const size_t reg_bytes = sizeof(T) * size, ops_bytes = sizeof(TileOp) * p.count;
+            const int ops_smem = reg_bytes + ops_bytes <= (size_t)kWholeShmMax ? 1 : 0;
+            (p.matk ? kwhole_k : kwhole)<<<1, threads, reg_bytes + (ops_smem ? ops_bytes : 0), stream>>>(
+                (T*)sv, geo, dops + p.first, (int)p.count, dpool, ops_smem);
         } else {
             if (geo.m != M_STREAM) return set_error(AQSG_ERR_RUNTIME, "Streaming pass with an unexpected tile size");
             const size_t shm = sizeof(T) * size + (size_t(1) << (geo.m - geo.L)) * sizeof(uint64_t);
