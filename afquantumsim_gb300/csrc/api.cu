@@ -327,6 +327,7 @@ int aqsg_shutdown(aqsg_ctx ctx) {
     if (ctx->host_result) cudaFreeHost(ctx->host_result);
     if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->order) cudaEventDestroy(ctx->order);
+    plan_cache_free(ctx);
     cudaStreamDestroy(ctx->stream);
     autotune_forget(ctx);
     delete ctx;
@@ -491,12 +492,49 @@ int aqsg_check_ops(int n, const aqsg_op* ops, int count) {
     return AQSG_OK;
 }
 
+// Bytes that determine the tile plan of ops on a register of st's shape:
+// the ops (matrix pointers replaced by the matrices' contents) and the
+// settings the encoding depends on.
+static std::vector<unsigned char> plan_key(const aqsg_state_s* st, const aqsg_op* ops, int count) {
+    std::vector<unsigned char> k;
+    const int32_t head[4] = {'A', st->n, st->dtype, st->ctx->tensor_cores};
+    k.insert(k.end(), (const unsigned char*)head, (const unsigned char*)head + sizeof(head));
+    for (int i = 0; i < count; ++i) {
+        aqsg_op o = ops[i];
+        o.matrix = nullptr;
+        k.insert(k.end(), (const unsigned char*)&o, (const unsigned char*)&o + sizeof(o));
+        if (ops[i].kind == AQSG_OP_UNITARY && ops[i].matrix) {
+            const size_t d = (size_t)1 << ops[i].num_qubits;
+            k.insert(k.end(), (const unsigned char*)ops[i].matrix,
+                     (const unsigned char*)(ops[i].matrix + 2 * d * d));
+        }
+    }
+    return k;
+}
+
 int aqsg_apply_ops(aqsg_state st, const aqsg_op* ops, int count, int mode) {
     if (int rc = check_state(st)) return rc;
-    if (int rc = aqsg_check_ops(st->n, ops, count)) return rc;
     if (mode < 0) mode = st->ctx->exec_mode;
     if (mode < AQSG_EXEC_AUTO || mode > AQSG_EXEC_TILED)
         return set_error(AQSG_ERR_INVALID_ARGUMENT, "Unknown execution mode");
+    if (mode != AQSG_EXEC_PER_GATE) {
+        if (count > 0 && !ops) return set_error(AQSG_ERR_NULL, "NULL op list");
+        if (count < 0) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Negative op count");
+        AQSG_CUDA_TRY(cudaSetDevice(st->ctx->device));
+        // a circuit run before on this context reuses its checked, lowered,
+        // encoded and uploaded plan
+        return run_tiled_cached(st, plan_key(st, ops, count), [&](std::vector<LOp>* low) {
+            if (int rc = aqsg_check_ops(st->n, ops, count)) return rc;
+            low->reserve(count);
+            for (int i = 0; i < count; ++i) {
+                LOp o;
+                if (int rc = lower_op(st->n, st->dtype, ops[i], &o)) return rc;
+                if (o.cls != L_NOP) low->push_back(std::move(o));
+            }
+            return (int)AQSG_OK;
+        });
+    }
+    if (int rc = aqsg_check_ops(st->n, ops, count)) return rc;
     std::vector<LOp> low;
     low.reserve(count);
     for (int i = 0; i < count; ++i) {
@@ -505,12 +543,9 @@ int aqsg_apply_ops(aqsg_state st, const aqsg_op* ops, int count, int mode) {
         if (o.cls != L_NOP) low.push_back(std::move(o));
     }
     AQSG_CUDA_TRY(cudaSetDevice(st->ctx->device));
-    if (mode == AQSG_EXEC_PER_GATE) {
-        for (const LOp& o : low)
-            if (int rc = launch_lop(st, o)) return rc;
-        return AQSG_OK;
-    }
-    return run_tiled(st, low);
+    for (const LOp& o : low)
+        if (int rc = launch_lop(st, o)) return rc;
+    return AQSG_OK;
 }
 
 int aqsg_qubit_prob(aqsg_state st, int qubit, double* out) {

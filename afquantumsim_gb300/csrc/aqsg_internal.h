@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <functional>
 #include <vector>
 
 #include "../../include/aqsg.h"
@@ -65,6 +66,10 @@ struct Scratch {
 
 }  // namespace aqsg
 
+namespace aqsg {
+struct PlanCache;
+}
+
 struct aqsg_ctx_s {
     int device = 0;
     int sm_count = 0;
@@ -82,6 +87,7 @@ struct aqsg_ctx_s {
     int* d_err = nullptr;           // device flag: a bounded kernel wait gave up
     int tensor_cores = 1;           // fused unitaries on tcgen05 (c64 tiles)
     cudaEvent_t order = nullptr;    // marks this stream's queue for aqsg_ctx_after
+    aqsg::PlanCache* plans = nullptr;  // recently run tile plans (host + device copies)
 };
 
 struct aqsg_state_s {
@@ -138,6 +144,13 @@ int launch_tile_plan_multi(void* sv0, uint64_t reg_stride, int members, const Ti
                            uint64_t dev_stride, cudaStream_t stream, int* d_err, uint64_t* launches);
 // Runs ops through shared-memory tile passes; returns AQSG_OK.
 int run_tiled(aqsg_state_s* st, const std::vector<LOp>& ops);
+// The same, with the encoded plan and its device table cached per context
+// under `key` (bytes that determine the plan: the caller's ops, or a
+// program's identity).  On a hit, lower() is not called.  lower() fills
+// the ops to encode on a miss.
+int run_tiled_cached(aqsg_state_s* st, const std::vector<unsigned char>& key,
+                     const std::function<int(std::vector<LOp>*)>& lower);
+void plan_cache_free(aqsg_ctx_s* c);
 // Largest tile (log2 amplitudes) the tile kernel holds for a dtype.
 int tile_max_bits(int dtype);
 

@@ -14,12 +14,14 @@
 // Each group's unitary is built on the host in FP64 by applying its gates as
 // row operations to the 2^k x 2^k identity.
 #include <algorithm>
+#include <atomic>
 
 #include <cstring>
 
 #include "aqsg_internal.h"
 
 struct aqsg_program_s {
+    uint64_t id = 0;  // unique per compiled program (keys the plan cache)
     int n = 0;
     int dtype = AQSG_C64;
     int source_ops = 0;
@@ -380,7 +382,9 @@ int aqsg_compile(int n, int dtype, const aqsg_op* ops, int count, int max_qubits
         src.push_back(ops[i]);
         src.back().matrix = nullptr;  // the caller's buffer need not outlive the program
     }
+    static std::atomic<uint64_t> next_id{1};
     auto* p = new aqsg_program_s();
+    p->id = next_id++;
     p->n = n;
     p->dtype = dtype;
     p->source_ops = count;
@@ -415,7 +419,14 @@ int aqsg_run_program(aqsg_state st, aqsg_program p, int mode) {
             if (int rc = launch_lop(st, o)) return rc;
         return AQSG_OK;
     }
-    return run_tiled(st, p->ops);
+    // the program's plan stays cached on the context while it is in use
+    std::vector<unsigned char> key;
+    const uint64_t head[4] = {'P', p->id, (uint64_t)st->dtype, (uint64_t)st->ctx->tensor_cores};
+    key.insert(key.end(), (const unsigned char*)head, (const unsigned char*)head + sizeof(head));
+    return run_tiled_cached(st, key, [&](std::vector<LOp>* low) {
+        *low = p->ops;
+        return (int)AQSG_OK;
+    });
 }
 
 int aqsg_program_export(aqsg_program p, aqsg_op* out, int capacity, int* count) {

@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <functional>
 #include <mutex>
 
 #include "tile_device.cuh"
@@ -1234,6 +1235,124 @@ int run_tiled(aqsg_state_s* st, const std::vector<LOp>& ops) {
             if (int rc = launch_scale(st, std::sqrt(norm_before / norm_after))) return rc;
     }
     return AQSG_OK;
+}
+
+// ---- plan cache ----------------------------------------------------------------------
+//
+// Re-running a circuit (a simulator that simulates the same QCircuit again,
+// a parameter-free sweep of shots) would lower, plan and encode it and copy
+// its table to the device each time; the cache keeps the last few encoded
+// plans with their device tables.  Entries are matched on the exact key
+// bytes, so a hit runs exactly what a miss would.
+constexpr size_t kPlanCacheEntries = 8;
+
+struct PlanCache {
+    struct Entry {
+        std::vector<unsigned char> key;
+        TilePlan plan;
+        void* dev = nullptr;
+        size_t dev_bytes = 0;
+        uint64_t last = 0;
+    };
+    std::vector<Entry> e;
+    uint64_t tick = 0;
+};
+
+void plan_cache_free(aqsg_ctx_s* c) {
+    if (!c->plans) return;
+    for (auto& en : c->plans->e)
+        if (en.dev) cudaFree(en.dev);
+    delete c->plans;
+    c->plans = nullptr;
+}
+
+// Run an encoded plan whose table is on the device (dev_table): the tile
+// passes, the error-flag check, and for tensor-core passes the
+// renormalisation to the input's FP64 norm.
+static int run_encoded(aqsg_state_s* st, const TilePlan& plan, const void* dev_table) {
+    aqsg_ctx_s* c = st->ctx;
+    // The tensor-core products lose a little norm in a biased way (~1e-7 per
+    // fused op); a run that uses them restores the input's FP64 norm at the
+    // end (one read pass before, one read and one scale pass after).
+    double norm_before = 0;
+    if (plan.any_tc)
+        if (int rc = reduce_prob(st, 0, 0, &norm_before)) return rc;
+    if (int rc = launch_tile_plan(st->d, plan, dev_table, c->stream, c->d_err, &c->launches)) return rc;
+    if (plan.any_stream) {  // a bounded wait that gave up leaves a flag
+        AQSG_CUDA_TRY(cudaMemcpyAsync(c->host_result, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        AQSG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        int flag = 0;
+        std::memcpy(&flag, c->host_result, sizeof(int));
+        if (flag) {
+            AQSG_CUDA_TRY(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
+            return set_error(AQSG_ERR_TIMEOUT, "Tile pass timed out waiting for its copies or MMAs");
+        }
+    }
+    if (plan.any_tc) {
+        double norm_after = 0;
+        if (int rc = reduce_prob(st, 0, 0, &norm_after)) return rc;
+        if (norm_after > 0 && norm_before > 0)
+            if (int rc = launch_scale(st, std::sqrt(norm_before / norm_after))) return rc;
+    }
+    return AQSG_OK;
+}
+
+int run_tiled_cached(aqsg_state_s* st, const std::vector<unsigned char>& key,
+                     const std::function<int(std::vector<LOp>*)>& lower) {
+    aqsg_ctx_s* c = st->ctx;
+    if (!c->plans) c->plans = new PlanCache();
+    PlanCache& pc = *c->plans;
+    for (auto& en : pc.e)
+        if (en.key == key) {
+            en.last = ++pc.tick;
+            if (en.plan.passes.empty()) return AQSG_OK;
+            return run_encoded(st, en.plan, en.dev);
+        }
+    std::vector<LOp> ops;
+    if (int rc = lower(&ops)) return rc;
+    PlanCache::Entry fresh;
+    fresh.key = key;
+    if (int rc = encode_tiled(st->n, st->dtype, ops, c->tensor_cores != 0, &fresh.plan)) return rc;
+    // the slot: a free one, else the least recently used (its device table
+    // is reused when large enough)
+    PlanCache::Entry* slot = nullptr;
+    if (pc.e.size() < kPlanCacheEntries) {
+        pc.e.emplace_back();
+        slot = &pc.e.back();
+    } else {
+        slot = &pc.e[0];
+        for (auto& en : pc.e)
+            if (en.last < slot->last) slot = &en;
+    }
+    const size_t poff = fresh.plan.pool_offset();
+    const size_t bytes = poff + fresh.plan.pool.size() + 16;
+    void* dev = slot->dev;
+    size_t dev_bytes = slot->dev_bytes;
+    slot->key.clear();  // the slot is invalid until the new table is in place
+    if (dev_bytes < bytes) {
+        if (dev) {
+            AQSG_CUDA_TRY(cudaStreamSynchronize(c->stream));  // the old table may still be in use
+            AQSG_CUDA_TRY(cudaFree(dev));
+            dev = nullptr;
+            dev_bytes = 0;
+        }
+        AQSG_CUDA_TRY(cudaMalloc(&dev, bytes));
+        dev_bytes = bytes;
+    }
+    slot->dev = dev;
+    slot->dev_bytes = dev_bytes;
+    if (!fresh.plan.passes.empty()) {
+        AQSG_CUDA_TRY(cudaMemcpyAsync(dev, fresh.plan.table.data(), fresh.plan.table.size(), cudaMemcpyHostToDevice,
+                                      c->stream));
+        if (!fresh.plan.pool.empty())
+            AQSG_CUDA_TRY(cudaMemcpyAsync((char*)dev + poff, fresh.plan.pool.data(), fresh.plan.pool.size(),
+                                          cudaMemcpyHostToDevice, c->stream));
+    }
+    slot->plan = std::move(fresh.plan);
+    slot->key = key;
+    slot->last = ++pc.tick;
+    if (slot->plan.passes.empty()) return AQSG_OK;
+    return run_encoded(st, slot->plan, slot->dev);
 }
 
 int run_plan_async(aqsg_state_s* st, const TilePlan& plan, const void* dev_table, double* d_norms) {
