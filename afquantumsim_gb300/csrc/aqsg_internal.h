@@ -142,10 +142,8 @@ int launch_tile_plan(void* sv, const TilePlan& plan, const void* dev, cudaStream
 // their own ops) sit dev_stride bytes apart from dev0: one launch per pass.
 int launch_tile_plan_multi(void* sv0, uint64_t reg_stride, int members, const TilePlan& plan, const void* dev0,
                            uint64_t dev_stride, cudaStream_t stream, int* d_err, uint64_t* launches);
-// Runs ops through shared-memory tile passes; returns AQSG_OK.
-int run_tiled(aqsg_state_s* st, const std::vector<LOp>& ops);
-// The same, with the encoded plan and its device table cached per context
-// under `key` (bytes that determine the plan: the caller's ops, or a
+// Runs ops through shared-memory tile passes, with the encoded plan and its
+// device table cached per context under `key` (bytes that determine the plan: the caller's ops, or a
 // program's identity).  On a hit, lower() is not called.  lower() fills
 // the ops to encode on a miss.
 int run_tiled_cached(aqsg_state_s* st, const std::vector<unsigned char>& key,

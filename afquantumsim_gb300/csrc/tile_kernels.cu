@@ -1199,44 +1199,6 @@ int launch_tile_plan(void* sv, const TilePlan& plan, const void* dev, cudaStream
                                   : launch_plan_t<double>(sv, plan, dev, stream, d_err, launches);
 }
 
-int run_tiled(aqsg_state_s* st, const std::vector<LOp>& ops) {
-    aqsg_ctx_s* c = st->ctx;
-    TilePlan plan;
-    if (int rc = encode_tiled(st->n, st->dtype, ops, c->tensor_cores != 0, &plan)) return rc;
-    if (plan.passes.empty()) return AQSG_OK;
-    const size_t poff = plan.pool_offset();
-    if (int rc = ensure_scratch(c->ops, poff + plan.pool.size() + 16)) return rc;
-    AQSG_CUDA_TRY(cudaMemcpyAsync(c->ops.ptr, plan.table.data(), plan.table.size(), cudaMemcpyHostToDevice,
-                                  c->stream));
-    if (!plan.pool.empty())
-        AQSG_CUDA_TRY(cudaMemcpyAsync((char*)c->ops.ptr + poff, plan.pool.data(), plan.pool.size(),
-                                      cudaMemcpyHostToDevice, c->stream));
-    // The tensor-core products lose a little norm in a biased way (~1e-7 per
-    // fused op); a run that uses them restores the input's FP64 norm at the
-    // end (one read pass before, one read and one scale pass after).
-    double norm_before = 0;
-    if (plan.any_tc)
-        if (int rc = reduce_prob(st, 0, 0, &norm_before)) return rc;
-    if (int rc = launch_tile_plan(st->d, plan, c->ops.ptr, c->stream, c->d_err, &c->launches)) return rc;
-    if (plan.any_stream) {  // a bounded wait that gave up leaves a flag
-        AQSG_CUDA_TRY(cudaMemcpyAsync(c->host_result, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-        AQSG_CUDA_TRY(cudaStreamSynchronize(c->stream));
-        int flag = 0;
-        std::memcpy(&flag, c->host_result, sizeof(int));
-        if (flag) {
-            AQSG_CUDA_TRY(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
-            return set_error(AQSG_ERR_TIMEOUT, "Tile pass timed out waiting for its copies or MMAs");
-        }
-    }
-    if (plan.any_tc) {
-        double norm_after = 0;
-        if (int rc = reduce_prob(st, 0, 0, &norm_after)) return rc;
-        if (norm_after > 0 && norm_before > 0)
-            if (int rc = launch_scale(st, std::sqrt(norm_before / norm_after))) return rc;
-    }
-    return AQSG_OK;
-}
-
 // ---- plan cache ----------------------------------------------------------------------
 //
 // Re-running a circuit (a simulator that simulates the same QCircuit again,
