@@ -143,9 +143,9 @@ int launch_tile_plan(void* sv, const TilePlan& plan, const void* dev, cudaStream
 int launch_tile_plan_multi(void* sv0, uint64_t reg_stride, int members, const TilePlan& plan, const void* dev0,
                            uint64_t dev_stride, cudaStream_t stream, int* d_err, uint64_t* launches);
 // Runs ops through shared-memory tile passes, with the encoded plan and its
-// device table cached per context under `key` (bytes that determine the plan: the caller's ops, or a
-// program's identity).  On a hit, lower() is not called.  lower() fills
-// the ops to encode on a miss.
+// device table cached per context under `key` (bytes that determine the
+// plan: the caller's ops, or a program's identity).  On a hit, lower() is
+// not called; on a miss it fills the ops to encode.
 int run_tiled_cached(aqsg_state_s* st, const std::vector<unsigned char>& key,
                      const std::function<int(std::vector<LOp>*)>& lower);
 void plan_cache_free(aqsg_ctx_s* c);
