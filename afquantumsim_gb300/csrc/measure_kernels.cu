@@ -601,6 +601,7 @@ int launch_collapse_qubit(aqsg_state_s* st, uint64_t mask, int outcome, double s
 // bits and sums blocks in a fixed order.
 
 constexpr int kZMaxS = 12;
+constexpr int kZMaxRB2 = 40;  // 2 x amplitude bits per block, at most (rb <= 20)
 
 size_t expz_partial_doubles(int n);
 int launch_expz_raw(const void* sv, int n, int dtype, double* partial, double* out_raw, cudaStream_t stream);
@@ -658,6 +659,54 @@ k_expz_partial(const T* __restrict__ sv, int tb, int rb, double* partial, uint64
     }
     const int stride = 2 * rb;
     double* out = partial + (uint64_t)blockIdx.x * stride;
+    if constexpr (sizeof(a_t<T>) == 4) {
+        // c64: every block sum in float-float on the FP32 pipe (warp
+        // butterflies, then across the <= 8 warps); FP64 only for the
+        // block's results
+        __shared__ float ffh[8][kZMaxRB2], ffl[8][kZMaxRB2];
+        const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        const FAcc ftot = [&] { FAcc t; t.hi = (float)tot; t.lo = (float)(tot - (double)(float)tot); return t; }();
+        for (int v = 0; v < stride; ++v) {
+            FAcc c;  // this thread's share of value v
+            if (v == 0) {
+                c = ftot;
+            } else if (v <= rb) {  // S1[q]
+                const int q = v - 1;
+                if (q < tb) {
+                    if ((threadIdx.x >> q) & 1) c = ftot;
+                } else {
+                    const double d = S[q - tb < kZMaxS ? q - tb : 0];
+                    c.hi = (float)d;
+                    c.lo = (float)(d - (double)c.hi);
+                }
+            } else {  // X[q], pair (q, q+1)
+                const int q = v - 1 - rb;
+                double d = 0;
+                if (q + 1 < tb) d = (((threadIdx.x >> q) ^ (threadIdx.x >> (q + 1))) & 1) ? tot : 0.0;
+                else if (q + 1 == tb) d = ((threadIdx.x >> q) & 1) ? tot - S[0] : S[0];
+                else d = X[q - tb < kZMaxS ? q - tb : 0];
+                c.hi = (float)d;
+                c.lo = (float)(d - (double)c.hi);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float h = __shfl_xor_sync(0xffffffffu, c.hi, o);
+                const float l = __shfl_xor_sync(0xffffffffu, c.lo, o);
+                c.add(h, l);
+            }
+            if (lane == 0) {
+                ffh[w][v] = c.hi;
+                ffl[w][v] = c.lo;
+            }
+        }
+        __syncthreads();
+        if ((int)threadIdx.x < stride) {
+            FAcc r;
+            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) r.add(ffh[q][threadIdx.x], ffl[q][threadIdx.x]);
+            out[threadIdx.x] = r.value();
+        }
+        return;
+    }
     const double btot = block_sum(tot, sh);
     if (threadIdx.x == 0) out[0] = btot;
     // S1[q] for q < rb
