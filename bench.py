@@ -385,6 +385,12 @@ def bench_vqe_batch(ctx, count=4096, seed=5):
     for _ in range(reps):
         z, zz = b.run()
     sweep_s = (_t.perf_counter() - t0) / reps
+    # one more replay inside an NVTX range "vqe_sweep", untimed: the range an
+    # ncu launch list of one sweep filters on
+    import torch
+    torch.cuda.nvtx.range_push("vqe_sweep")
+    b.run()
+    torch.cuda.nvtx.range_pop()
     rng = np.random.default_rng(seed + 1)
     new = []
     for n, ops in items:  # same shapes (n >= 8: 3n ops per layer), new angles
