@@ -658,9 +658,12 @@ __device__ __forceinline__ void rphase_run(T* s, uint32_t size, uint32_t nthr, u
         T v[E];
 #pragma unroll
         for (int e = 0; e < E; ++e) v[e] = *reinterpret_cast<const T*>(sb + off_of(ajt, e));
+        // the next op's header is loaded while this one runs
+        uint4 hd_next = nops > 0 ? *reinterpret_cast<const uint4*>(rops) : make_uint4(0u, 0u, 0u, 0u);
         for (int q = 0; q < nops; ++q) {
             const ROp* op = rops + q;
-            const uint4 hd = *reinterpret_cast<const uint4*>(op);
+            const uint4 hd = hd_next;
+            if (q + 1 < nops) hd_next = *reinterpret_cast<const uint4*>(rops + q + 1);
             const uint32_t code = hd.x;
             if (code & RF_EXT) {
                 if ((base & op->cm_ext) != op->cv_ext) continue;
