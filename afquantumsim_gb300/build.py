@@ -5,7 +5,7 @@ git-ignored):
 
 * ``afquantumsim_gb300/_build/libaqsg.so`` - the C-ABI engine (CUDA, sm_103a)
 * ``afquantumsim_gb300/_build/libaqs.so``  - the ``aqs::`` C++ layer over it
-* ``oracle/_build/libaqs_oracle.so``       - the CPU oracle (test checker)
+* ``oracle/_build/libaqs_oracle.so``       - the CPU oracle (test infrastructure)
 
 Only nvcc / g++ / gcc are used, translation units compile in parallel.
 """
