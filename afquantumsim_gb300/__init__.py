@@ -43,6 +43,7 @@ EXPORTS = [
     "aqsg_server_wait_idle", "aqsg_server_get_stats", "aqsg_server_destroy",
     "aqsg_expect_pauli", "aqsg_autotune", "aqsg_batch_tuning", "aqsg_selftest_bounded_wait",
     "aqsg_state_download_async", "aqsg_circuit_to_text", "aqsg_circuit_from_text",
+    "aqsg_debug_tile_plan",
 ]
 
 _lib = None
@@ -481,6 +482,33 @@ def circuit_from_text(text: str):
     out = (Op * cnt.value).from_buffer(arr)
     out._keep = (arr, mats)
     return n.value, out
+
+
+class TilePass(C.Structure):
+    """struct aqsg_tile_pass (aqsg_debug.h)"""
+    _fields_ = [("m", C.c_int32), ("L", C.c_int32), ("first", C.c_int32), ("count", C.c_int32),
+                ("tbits", C.c_int32 * 16)]
+
+
+def debug_tile_plan(n: int, ops, dtype: int = C64, fuse_qubits: int = 0):
+    """aqsg_debug_tile_plan: (passes, table bytes, pool bytes) of the CUDA-core
+    tile plan the engine would run for ops (a testing aid)."""
+    lib = load_library()
+    f = lib.aqsg_debug_tile_plan
+    f.argtypes = [C.c_int, C.c_int, C.POINTER(Op), C.c_int, C.c_int, C.POINTER(TilePass), C.c_int,
+                  C.POINTER(C.c_int), C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t), C.c_void_p, C.c_size_t,
+                  C.POINTER(C.c_size_t)]
+    f.restype = C.c_int
+    arr = op_array(list(ops)) if not isinstance(ops, C.Array) else ops
+    npass, tb, pb = C.c_int(), C.c_size_t(), C.c_size_t()
+    _check(f(n, dtype, arr, len(arr), fuse_qubits, None, 0, C.byref(npass), None, 0, C.byref(tb), None, 0,
+             C.byref(pb)))
+    passes = (TilePass * max(npass.value, 1))()
+    table = C.create_string_buffer(max(tb.value, 1))
+    pool = C.create_string_buffer(max(pb.value, 1))
+    _check(f(n, dtype, arr, len(arr), fuse_qubits, passes, npass.value, C.byref(npass), table, tb.value,
+             C.byref(tb), pool, pb.value, C.byref(pb)))
+    return list(passes[:npass.value]), table.raw[:tb.value], pool.raw[:pb.value]
 
 
 def check_ops(n: int, ops) -> None:

@@ -1331,3 +1331,57 @@ int run_plan_async(aqsg_state_s* st, const TilePlan& plan, const void* dev_table
 }
 
 }  // namespace aqsg
+
+// ---- testing aid ----------------------------------------------------------------------
+
+#include "../../include/aqsg_debug.h"
+
+extern "C" int aqsg_debug_tile_plan(int n, int dtype, const aqsg_op* ops, int count, int fuse_qubits,
+                                    aqsg_tile_pass* passes, int pass_capacity, int* pass_count,
+                                    void* table, size_t table_capacity, size_t* table_bytes, void* pool,
+                                    size_t pool_capacity, size_t* pool_bytes) {
+    using namespace aqsg;
+    if (n < 1 || n > AQSG_MAX_QUBITS) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Invalid qubit count");
+    if (dtype != AQSG_C64 && dtype != AQSG_C128) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Unknown dtype");
+    std::vector<LOp> low;
+    if (fuse_qubits > 0) {
+        aqsg_program p = nullptr;
+        if (int rc = aqsg_compile(n, dtype, ops, count, fuse_qubits, &p)) return rc;
+        low = program_ops(p);
+        aqsg_program_free(p);
+    } else {
+        if (int rc = aqsg_check_ops(n, ops, count)) return rc;
+        for (int i = 0; i < count; ++i) {
+            LOp o;
+            if (int rc = lower_op(n, dtype, ops[i], &o)) return rc;
+            if (o.cls != L_NOP) low.push_back(std::move(o));
+        }
+    }
+    TilePlan plan;
+    if (int rc = encode_tiled(n, dtype, low, false, &plan)) return rc;
+    if (pass_count) *pass_count = (int)plan.passes.size();
+    if (table_bytes) *table_bytes = plan.table.size();
+    if (pool_bytes) *pool_bytes = plan.pool.size();
+    if (passes) {
+        if (pass_capacity < (int)plan.passes.size()) return set_error(AQSG_ERR_OUT_OF_RANGE, "Pass buffer too small");
+        for (size_t i = 0; i < plan.passes.size(); ++i) {
+            const TilePass& p = plan.passes[i];
+            aqsg_tile_pass& o = passes[i];
+            std::memset(&o, 0, sizeof(o));
+            o.m = p.m;
+            o.L = p.L;
+            o.first = (int32_t)p.first;
+            o.count = (int32_t)p.count;
+            for (int b = 0; b < p.m && b < 16; ++b) o.tbits[b] = p.tbits[b];
+        }
+    }
+    if (table) {
+        if (table_capacity < plan.table.size()) return set_error(AQSG_ERR_OUT_OF_RANGE, "Table buffer too small");
+        std::memcpy(table, plan.table.data(), plan.table.size());
+    }
+    if (pool && !plan.pool.empty()) {
+        if (pool_capacity < plan.pool.size()) return set_error(AQSG_ERR_OUT_OF_RANGE, "Pool buffer too small");
+        std::memcpy(pool, plan.pool.data(), plan.pool.size());
+    }
+    return AQSG_OK;
+}

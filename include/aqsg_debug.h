@@ -1,0 +1,39 @@
+/* Testing aids of libaqsg: inspection of what the engine would run, for
+ * host-side tests on machines without a GPU.  Not needed to use the engine.
+ * Plain C, same conventions as aqsg.h (status codes, caller-owned buffers). */
+#ifndef AQSG_DEBUG_H
+#define AQSG_DEBUG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "aqsg.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* One tile pass of an encoded plan: tiles of 2^m amplitudes whose local
+ * index bit i is global index bit tbits[i] (ascending; the L lowest are the
+ * contiguous row bits), running table records [first, first + count). */
+typedef struct aqsg_tile_pass {
+    int32_t m, L, first, count;
+    int32_t tbits[16];
+} aqsg_tile_pass;
+
+/* The tile-pass plan aqsg_apply_ops would run for ops in AQSG_EXEC_TILED mode
+ * on an n-qubit register of dtype, the CUDA-core form (no tensor cores),
+ * after fusing at fuse_qubits (0: the gates as they are): the passes, the
+ * op table (160-byte records: the engine's tile ops and register-phase ops)
+ * and the operand pool, byte for byte as they are uploaded.  Call with NULL
+ * buffers to get the counts and sizes. */
+int aqsg_debug_tile_plan(int n, int dtype, const aqsg_op* ops, int count, int fuse_qubits,
+                         aqsg_tile_pass* passes, int pass_capacity, int* pass_count,
+                         void* table, size_t table_capacity, size_t* table_bytes,
+                         void* pool, size_t pool_capacity, size_t* pool_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AQSG_DEBUG_H */

@@ -15,7 +15,7 @@ ROOT = Path(__file__).resolve().parent.parent
 
 
 def declared_symbols():
-    text = (ROOT / "include" / "aqsg.h").read_text()
+    text = "".join(h.read_text() for h in sorted((ROOT / "include").glob("*.h")))
     return sorted(set(re.findall(r"^\s*(?:int|size_t)\s+(aqsg_\w+)\s*\(", text, re.M)))
 
 

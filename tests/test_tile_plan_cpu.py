@@ -1,0 +1,40 @@
+"""The host tile encoder checked on the CPU: the plan the engine would run
+(aqsg_debug_tile_plan: passes, op table with register phases, operand pool),
+interpreted by a numpy restatement of the tile kernels' record semantics
+(tests/tile_emulator.py), gives the FP64 oracle's state — for whole-register
+and streaming passes, complex64 and complex128 encodings, fused and unfused
+programs, every gate kind with extra controls.  The device code itself is
+covered by the GPU parity tests."""
+import numpy as np
+import pytest
+
+import afquantumsim_gb300 as aq
+from afquantumsim_gb300 import circuits
+from oracle import oracle
+from tests import _kat
+from tests.tile_emulator import run_plan
+
+
+@pytest.mark.parametrize("dtype", [aq.C64, aq.C128])
+@pytest.mark.parametrize("n,fuse,seed", [(6, 0, 1), (9, 0, 2), (10, 2, 3), (12, 0, 4), (12, 3, 5),
+                                         (13, 4, 6), (15, 0, 7), (15, 2, 8), (16, 3, 9)])
+def test_encoded_plan_equals_oracle(dtype, n, fuse, seed):
+    ops = _kat.random_circuit(n, 120, seed)
+    passes, table, pool = aq.debug_tile_plan(n, ops, dtype, fuse)
+    v = _kat.random_state(n, seed)
+    want = oracle.apply_f64(v.copy(), ops)
+    got = run_plan(v, n, passes, table, pool, c64=(dtype == aq.C64))
+    tol = 1e-5 if dtype == aq.C64 else 1e-12
+    assert np.max(np.abs(got - want)) < tol
+
+
+def test_vqe_plan_uses_register_phases():
+    n = 16
+    ops = circuits.vqe_ops_array(n, 3, np.random.default_rng(2).uniform(-np.pi, np.pi, size=(3, n, 2)))
+    ops = list((aq.Op * len(ops)).from_buffer_copy(ops.tobytes()))
+    passes, table, pool = aq.debug_tile_plan(n, ops, aq.C64, 0)
+    recs = np.frombuffer(table, dtype=np.int32).reshape(-1, 40)
+    assert (recs[:, 0] == 8).any()  # register-phase headers
+    v = _kat.random_state(n, 3)
+    got = run_plan(v, n, passes, table, pool, c64=True)
+    assert np.max(np.abs(got - oracle.apply_f64(v.copy(), ops))) < 1e-5
