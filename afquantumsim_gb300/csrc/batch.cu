@@ -221,10 +221,13 @@ size_t expz_partial_doubles(int n);
 static int encode_circuit(const aqsg_circuit& ci, int fuse, bool tc, TilePlan* plan) {
     std::vector<LOp> low;
     if (fuse > 0) {
+        // encode straight from the program's ops (fused matrices are 16 KiB
+        // each: no copy)
         aqsg_program p = nullptr;
         if (int rc = aqsg_compile(ci.n, AQSG_C64, ci.ops, ci.count, fuse, &p)) return rc;
-        low = program_ops(p);
+        const int rc = encode_tiled(ci.n, AQSG_C64, program_ops(p), tc, plan, false);
         aqsg_program_free(p);
+        return rc;
     } else {
         low.reserve(ci.count);
         for (int k = 0; k < ci.count; ++k) {

@@ -334,24 +334,28 @@ static int fuse(int n, const std::vector<LOp>& in, const std::vector<aqsg_op>& s
                 f.mk[2 * (r * D + c)] = u.re[(size_t)r * D + c];
                 f.mk[2 * (r * D + c) + 1] = u.im[(size_t)r * D + c];
             }
-        prog->mats.push_back(f.mk);
         aqsg_op ex;
         std::memset(&ex, 0, sizeof(ex));
         ex.kind = AQSG_OP_UNITARY;
         ex.num_qubits = k;
         for (int j = 0; j < k; ++j) ex.qubits[j] = n - 1 - f.tb[j];
-        ex.matrix = prog->mats.back().data();
-        prog->exported.push_back(ex);
         if (k == 1) {
+            prog->mats.push_back(f.mk);
+            ex.matrix = prog->mats.back().data();
             f.cls = L_MAT2;
             f.t0 = bits[0];
             f.k = 0;
             for (int e = 0; e < 8; ++e) f.m[e] = f.mk[e];
             f.mk.clear();
+            out->push_back(std::move(f));
         } else {
+            // the exported op reads the matrix the lowered op holds (its heap
+            // buffer stays put when the op vector grows)
             f.cls = L_MATK;
+            out->push_back(std::move(f));
+            ex.matrix = out->back().mk.data();
         }
-        out->push_back(std::move(f));
+        prog->exported.push_back(ex);
     }
     return AQSG_OK;
 }
