@@ -43,7 +43,7 @@ EXPORTS = [
     "aqsg_server_wait_idle", "aqsg_server_get_stats", "aqsg_server_destroy",
     "aqsg_expect_pauli", "aqsg_autotune", "aqsg_batch_tuning", "aqsg_selftest_bounded_wait",
     "aqsg_state_download_async", "aqsg_circuit_to_text", "aqsg_circuit_from_text",
-    "aqsg_debug_tile_plan",
+    "aqsg_debug_tile_plan", "aqsg_debug_batch_image",
 ]
 
 _lib = None
@@ -509,6 +509,27 @@ def debug_tile_plan(n: int, ops, dtype: int = C64, fuse_qubits: int = 0):
     _check(f(n, dtype, arr, len(arr), fuse_qubits, passes, npass.value, C.byref(npass), table, tb.value,
              C.byref(tb), pool, pb.value, C.byref(pb)))
     return list(passes[:npass.value]), table.raw[:tb.value], pool.raw[:pb.value]
+
+
+def debug_batch_image(circuits, fuse=None, tc=None, update=None) -> bytes:
+    """aqsg_debug_batch_image: the plan image a batch of [(n, ops), ...]
+    uploads, with the fusion width and tensor-core choice of each register
+    of more than 14 qubits given (fuse, tc: one entry per such register), or
+    the image after an update with the circuits `update` (a testing aid)."""
+    lib = load_library()
+    f = lib.aqsg_debug_batch_image
+    f.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+                  C.POINTER(C.c_size_t)]
+    f.restype = C.c_int
+    arr, _ = Batch._encode(circuits)
+    upd = Batch._encode(update)[0] if update is not None else None
+    fz = (C.c_int * max(len(fuse), 1))(*fuse) if fuse is not None else None
+    tz = (C.c_int * max(len(tc), 1))(*tc) if tc is not None else None
+    size = C.c_size_t()
+    _check(f(arr, len(arr), fz, tz, upd, None, 0, C.byref(size)))
+    buf = C.create_string_buffer(max(size.value, 1))
+    _check(f(arr, len(arr), fz, tz, upd, buf, size.value, C.byref(size)))
+    return buf.raw[:size.value]
 
 
 def check_ops(n: int, ops) -> None:

@@ -19,6 +19,7 @@
 #include <thread>
 #include <vector>
 
+#include "../../include/aqsg_debug.h"
 #include "tile_device.cuh"
 
 namespace aqsg {
@@ -167,6 +168,17 @@ static int class_of(int n) {
     return -1;
 }
 
+// Where one circuit's encoded ops sit in the batch's plan image: its op
+// table, its operand pool, and (small registers) the shift applied to its
+// pool offsets, which are relative to the class pool there.
+struct PlanSlot {
+    uint64_t table_at = 0, pool_at = 0;
+    uint64_t table_bytes = 0, pool_bytes = 0;
+    int32_t reloc = 0;
+    int cls = -1;    // size class, or -1 for a large register
+    int large = -1;  // index into the large plans
+};
+
 }  // namespace aqsg
 
 using namespace aqsg;
@@ -194,6 +206,20 @@ struct aqsg_batch_s {
     std::vector<LargeGroup> groups;
     std::vector<char> grouped;     // per large circuit: runs in a group
     void* d_large = nullptr;
+    // every plan area in one host image (pinned) and its device copy,
+    // uploaded with one copy: the three class tables (pool after each),
+    // then the large plans.  d_small_ops and d_large point into d_plans.
+    std::vector<PlanSlot> slots;  // per circuit
+    size_t small_base[3] = {0, 0, 0};
+    size_t large_base = 0;
+    size_t plans_bytes = 0;
+    unsigned char* h_plans = nullptr;
+    void* d_plans = nullptr;
+    // host-only batches (the plan-image check): no device, the fusion width
+    // and tensor-core choice of each large register given, not tuned
+    bool host_only = false;
+    const int* preset_fuse = nullptr;
+    const int* preset_tc = nullptr;
     // parallel branches of the graph: large circuits go round-robin to
     // branch streams, each with its own register and reduction scratch
     std::vector<cudaStream_t> streams;
@@ -262,47 +288,33 @@ static void parallel_for(int count, F body) {
     for (auto& t : pool) t.join();
 }
 
-// Lower and encode every circuit; fills the host-side tables of b.  The
-// first call also tunes each large structure (on the GPU, serially); the
+// Lower and encode every circuit at creation; fills the host-side tables
+// of b.  Each large register first gets its fusion width: the width the
+// grouped tuner finds fastest for its structure (timed as the batch runs
+// it, over a replica count that depends on n only, and cached per
+// structure, so a circuit runs the same way alone and in any batch).  The
 // per-circuit lowering and encoding then run on all host threads, and the
 // tables are assembled in circuit order, so the result does not depend on
 // the thread count.
-static int encode_batch(aqsg_batch_s* b, const aqsg_circuit* cs, bool first_time) {
-    for (int c = 0; c < 3; ++c) {
-        b->small_table[c].clear();
-        b->small_pool[c].clear();
-        if (first_time) {
-            b->items[c].clear();
-            b->class_circuits[c].clear();
-        }
-    }
-    if (first_time) {
-        b->large.clear();
-        b->plans.clear();
-        b->fuse.clear();
-        b->tc.clear();
-    }
-    // validation, and (first call) the tuned fusion width of each large
-    // register: the width the grouped tuner finds fastest for its structure
-    // (timed as the batch runs it, over a replica count that depends on n
-    // only, and cached per structure, so a circuit runs the same way alone
-    // and in any batch)
+static int encode_batch(aqsg_batch_s* b, const aqsg_circuit* cs) {
     std::vector<int> large_index(b->count, -1);
     int nlarge = 0;
     for (int i = 0; i < b->count; ++i) {
         const aqsg_circuit& ci = cs[i];
-        if (ci.n != b->n[i]) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Batch structure changed (qubit count)");
         if (int rc = aqsg_check_ops(ci.n, ci.ops, ci.count)) return rc;
         if (class_of(ci.n) >= 0) continue;
         large_index[i] = nlarge++;
-        if (first_time) {
-            int best_fuse = 0, best_tc = 0;
-            if (int rc = autotune_grouped(b->ctx, ci.n, ci.ops, ci.count, &best_fuse, &best_tc)) return rc;
-            b->fuse.push_back(best_fuse);
-            b->tc.push_back(best_tc);
+        int best_fuse = 0, best_tc = 0;
+        if (b->preset_fuse) {
+            best_fuse = b->preset_fuse[nlarge - 1];
+            best_tc = b->preset_tc ? b->preset_tc[nlarge - 1] : 0;
+            if (best_fuse < 0) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Negative fusion width");
+        } else if (int rc = autotune_grouped(b->ctx, ci.n, ci.ops, ci.count, &best_fuse, &best_tc)) {
+            return rc;
         }
+        b->fuse.push_back(best_fuse);
+        b->tc.push_back(best_tc);
     }
-    // per-circuit lowering and encoding on all host threads
     std::vector<TilePlan> plans(b->count);
     std::vector<int> rcs(b->count, AQSG_OK);
     std::vector<std::string> msgs(b->count);
@@ -315,13 +327,17 @@ static int encode_batch(aqsg_batch_s* b, const aqsg_circuit* cs, bool first_time
     });
     for (int i = 0; i < b->count; ++i)
         if (rcs[i]) return set_error(rcs[i], msgs[i]);
-    // assemble the tables in circuit order
-    std::vector<size_t> seen(3, 0);
+    // assemble the class tables in circuit order
+    b->slots.assign(b->count, PlanSlot());
     for (int i = 0; i < b->count; ++i) {
         const int cls = class_of(cs[i].n);
         TilePlan& plan = plans[i];
+        PlanSlot& sl = b->slots[i];
+        sl.cls = cls;
+        sl.table_bytes = plan.table.size();
+        sl.pool_bytes = plan.pool.size();
         if (cls >= 0) {
-            // one whole-register pass; append its ops to the class table with
+            // one whole-register pass; its ops go to the class table with
             // their pool offsets shifted to the class pool
             const size_t tsz = sizeof(TileOp);
             const uint32_t first = (uint32_t)(b->small_table[cls].size() / tsz);
@@ -330,61 +346,183 @@ static int encode_batch(aqsg_batch_s* b, const aqsg_circuit* cs, bool first_time
             b->small_pool[cls].insert(b->small_pool[cls].end(), plan.pool.begin(), plan.pool.end());
             const size_t w = b->small_table[cls].size();
             b->small_table[cls].insert(b->small_table[cls].end(), plan.table.begin(), plan.table.end());
-            if (relocate_tile_matrices(&b->small_table[cls][w], plan.table.size() / tsz, (int32_t)pbase) &&
-                first_time)
+            if (relocate_tile_matrices(&b->small_table[cls][w], plan.table.size() / tsz, (int32_t)pbase))
                 b->class_matk[cls] = true;
-            const int nops = (int)(plan.table.size() / tsz);
-            if (first_time) {
-                SmallItem it;
-                it.n = cs[i].n;
-                it.nops = nops;
-                it.op_first = first;
-                it.out = (uint32_t)b->out_off[i];
-                b->items[cls].push_back(it);
-                b->class_circuits[cls].push_back(i);
-            } else {
-                SmallItem& it = b->items[cls][seen[cls]];
-                if (it.nops != nops || it.op_first != first)
-                    return set_error(AQSG_ERR_INVALID_ARGUMENT, "Batch structure changed (ops)");
-            }
-            seen[cls]++;
+            sl.table_at = w;     // within the class table, until laid out
+            sl.pool_at = pbase;  // within the class pool
+            sl.reloc = (int32_t)pbase;
+            SmallItem it;
+            it.n = cs[i].n;
+            it.nops = (int)(plan.table.size() / tsz);
+            it.op_first = first;
+            it.out = (uint32_t)b->out_off[i];
+            b->items[cls].push_back(it);
+            b->class_circuits[cls].push_back(i);
         } else {
-            const int li = large_index[i];
-            if (first_time) {
-                b->large.push_back(i);
-                b->plans.push_back(std::move(plan));
-            } else {
-                TilePlan& old = b->plans[li];
-                if (old.table.size() != plan.table.size() || old.pool.size() != plan.pool.size() ||
-                    old.passes.size() != plan.passes.size())
-                    return set_error(AQSG_ERR_INVALID_ARGUMENT, "Batch structure changed (ops)");
-                old.table = std::move(plan.table);
-                old.pool = std::move(plan.pool);
-            }
+            sl.large = (int)b->large.size();
+            b->large.push_back(i);
+            b->plans.push_back(std::move(plan));
         }
     }
     return AQSG_OK;
 }
 
-static int upload_batch(aqsg_batch_s* b, cudaStream_t s) {
+// Group the large registers with equal plan geometry, and lay out the plan
+// image: each size class's table then pool, then the large plans (each
+// group's members at a fixed stride, then the rest).  Host only.
+static void layout_batch(aqsg_batch_s* b) {
+    b->grouped.assign(b->large.size(), 0);
+    {
+        std::map<std::vector<uint64_t>, std::vector<size_t>> by_key;
+        for (size_t k = 0; k < b->large.size(); ++k) {
+            const TilePlan& p = b->plans[k];
+            std::vector<uint64_t> key = {(uint64_t)p.n, p.table.size(), p.pool.size(), p.passes.size()};
+            for (const TilePass& ps : p.passes) {
+                key.push_back(((uint64_t)ps.m << 48) | ((uint64_t)ps.L << 40) | ((uint64_t)ps.tc << 36) |
+                              ((uint64_t)ps.matk << 32) | ps.first);
+                key.push_back(ps.count);
+                key.push_back(((uint64_t)ps.tc_blob << 32) | ps.tc_bytes);
+                uint64_t bits = 0;
+                for (int i = 0; i < ps.m; ++i) bits |= 1ull << ps.tbits[i];
+                key.push_back(bits);
+            }
+            by_key[key].push_back(k);
+        }
+        for (auto& kv : by_key) {
+            const int n = b->plans[kv.second[0]].n;
+            const size_t per_chunk = std::max<size_t>(1, std::min<size_t>(kGroupBytes >> (n + 3), 65535));
+            for (size_t at = 0; at < kv.second.size(); at += per_chunk) {
+                LargeGroup gr;
+                gr.n = n;
+                gr.members.assign(kv.second.begin() + (long)at,
+                                  kv.second.begin() + (long)std::min(kv.second.size(), at + per_chunk));
+                for (size_t k : gr.members) b->grouped[k] = 1;
+                b->groups.push_back(std::move(gr));
+            }
+        }
+    }
+    size_t at = 0;
+    for (int c = 0; c < 3; ++c) {
+        b->small_base[c] = at;
+        if (b->items[c].empty()) continue;
+        const size_t poff = (b->small_table[c].size() + 255) & ~size_t(255);
+        at += (poff + b->small_pool[c].size() + 16 + 255) & ~size_t(255);
+    }
+    b->large_base = at;
+    b->plan_off.assign(b->plans.size(), 0);
+    size_t large_bytes = 0;
+    for (LargeGroup& gr : b->groups) {
+        const TilePlan& p = b->plans[gr.members[0]];
+        gr.stride = (p.pool_offset() + p.pool.size() + 255) & ~size_t(255);
+        gr.dev_off = large_bytes;
+        for (size_t j = 0; j < gr.members.size(); ++j) b->plan_off[gr.members[j]] = large_bytes + j * gr.stride;
+        large_bytes += gr.members.size() * gr.stride;
+    }
+    for (size_t k = 0; k < b->plans.size(); ++k) {
+        if (b->grouped[k]) continue;
+        const TilePlan& p = b->plans[k];
+        b->plan_off[k] = large_bytes;
+        large_bytes += (p.pool_offset() + p.pool.size() + 255) & ~size_t(255);
+    }
+    b->plans_bytes = at + large_bytes;
+    // slots as image offsets
+    for (PlanSlot& sl : b->slots) {
+        if (sl.cls >= 0) {
+            const size_t poff = (b->small_table[sl.cls].size() + 255) & ~size_t(255);
+            sl.table_at += b->small_base[sl.cls];
+            sl.pool_at += b->small_base[sl.cls] + poff;
+        } else {
+            sl.table_at = b->large_base + b->plan_off[sl.large];
+            sl.pool_at = sl.table_at + b->plans[sl.large].pool_offset();
+        }
+    }
+}
+
+// Write the tables assembled at creation into the (zeroed) plan image.
+static void fill_image(aqsg_batch_s* b) {
+    std::memset(b->h_plans, 0, b->plans_bytes);
     for (int c = 0; c < 3; ++c) {
         if (b->items[c].empty()) continue;
-        const size_t tb = b->small_table[c].size();
-        const size_t poff = (tb + 255) & ~size_t(255);
-        AQSG_CUDA_TRY(cudaMemcpyAsync(b->d_small_ops[c], b->small_table[c].data(), tb, cudaMemcpyHostToDevice, s));
-        if (!b->small_pool[c].empty())
-            AQSG_CUDA_TRY(cudaMemcpyAsync((char*)b->d_small_ops[c] + poff, b->small_pool[c].data(),
-                                          b->small_pool[c].size(), cudaMemcpyHostToDevice, s));
+        unsigned char* dst = b->h_plans + b->small_base[c];
+        const size_t poff = (b->small_table[c].size() + 255) & ~size_t(255);
+        if (!b->small_table[c].empty()) std::memcpy(dst, b->small_table[c].data(), b->small_table[c].size());
+        if (!b->small_pool[c].empty()) std::memcpy(dst + poff, b->small_pool[c].data(), b->small_pool[c].size());
     }
     for (size_t k = 0; k < b->plans.size(); ++k) {
         const TilePlan& p = b->plans[k];
-        char* dst = (char*)b->d_large + b->plan_off[k];
-        AQSG_CUDA_TRY(cudaMemcpyAsync(dst, p.table.data(), p.table.size(), cudaMemcpyHostToDevice, s));
-        if (!p.pool.empty())
-            AQSG_CUDA_TRY(cudaMemcpyAsync(dst + p.pool_offset(), p.pool.data(), p.pool.size(),
-                                          cudaMemcpyHostToDevice, s));
+        unsigned char* dst = b->h_plans + b->large_base + b->plan_off[k];
+        if (!p.table.empty()) std::memcpy(dst, p.table.data(), p.table.size());
+        if (!p.pool.empty()) std::memcpy(dst + p.pool_offset(), p.pool.data(), p.pool.size());
     }
+}
+
+// New parameter values: re-lower and re-encode every circuit on all host
+// threads, each straight into its slot of the plan image.  The structure
+// (qubit counts, op classes, table, pool and pass geometry) must be the
+// one the batch was created with, since the captured graph's launches
+// depend on it.  On an error the image may be partly rewritten; it is not
+// uploaded.
+static int update_image(aqsg_batch_s* b, const aqsg_circuit* cs) {
+    for (int i = 0; i < b->count; ++i) {
+        if (cs[i].n != b->n[i]) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Batch structure changed (qubit count)");
+        if (cs[i].count > 0 && !cs[i].ops) return set_error(AQSG_ERR_NULL, "NULL op list");
+        if (int rc = aqsg_check_ops(cs[i].n, cs[i].ops, cs[i].count)) return rc;
+    }
+    std::vector<int> rcs(b->count, AQSG_OK);
+    std::vector<std::string> msgs(b->count);
+    parallel_for(b->count, [&](int i) {
+        // one plan per host thread, reused: its buffers keep their capacity
+        thread_local TilePlan plan;
+        const PlanSlot& sl = b->slots[i];
+        const int fuse = sl.large >= 0 ? b->fuse[sl.large] : 0;
+        const bool tc = sl.large >= 0 && b->tc[sl.large] != 0;
+        int rc = encode_circuit(cs[i], fuse, tc, &plan);
+        if (!rc && (plan.table.size() != sl.table_bytes || plan.pool.size() != sl.pool_bytes))
+            rc = set_error(AQSG_ERR_INVALID_ARGUMENT, "Batch structure changed (ops)");
+        if (!rc && sl.large >= 0) {
+            const std::vector<TilePass>& was = b->plans[sl.large].passes;
+            if (plan.passes.size() != was.size() ||
+                (!was.empty() && std::memcmp(plan.passes.data(), was.data(), was.size() * sizeof(TilePass))))
+                rc = set_error(AQSG_ERR_INVALID_ARGUMENT, "Batch structure changed (passes)");
+        }
+        if (!rc) {
+            unsigned char* t = b->h_plans + sl.table_at;
+            if (sl.table_bytes) std::memcpy(t, plan.table.data(), sl.table_bytes);
+            if (sl.pool_bytes) std::memcpy(b->h_plans + sl.pool_at, plan.pool.data(), sl.pool_bytes);
+            if (sl.cls >= 0 && relocate_tile_matrices(t, sl.table_bytes / sizeof(TileOp), sl.reloc) &&
+                !b->class_matk[sl.cls])
+                rc = set_error(AQSG_ERR_INVALID_ARGUMENT, "Batch structure changed (dense ops)");
+        }
+        if (rc) {
+            rcs[i] = rc;
+            msgs[i] = last_error_message();
+        }
+    });
+    for (int i = 0; i < b->count; ++i)
+        if (rcs[i]) return set_error(rcs[i], msgs[i]);
+    return AQSG_OK;
+}
+
+static int upload_batch(aqsg_batch_s* b, cudaStream_t s) {
+    if (b->plans_bytes)
+        AQSG_CUDA_TRY(cudaMemcpyAsync(b->d_plans, b->h_plans, b->plans_bytes, cudaMemcpyHostToDevice, s));
     AQSG_CUDA_TRY(cudaStreamSynchronize(s));
+    return AQSG_OK;
+}
+
+// Qubit counts and result offsets of a new batch.
+static int init_shape(aqsg_batch_s* b, const aqsg_circuit* cs, int count) {
+    b->count = count;
+    b->n.resize(count);
+    b->out_off.resize(count);
+    for (int i = 0; i < count; ++i) {
+        const int n = cs[i].n;
+        if (n < 1 || n > 30) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Batch registers take 1 to 30 qubits");
+        if (cs[i].count > 0 && !cs[i].ops) return set_error(AQSG_ERR_NULL, "NULL op list");
+        b->n[i] = n;
+        b->out_off[i] = b->out_doubles;
+        b->out_doubles += 2 * (size_t)n;
+    }
     return AQSG_OK;
 }
 
@@ -459,11 +597,15 @@ static int record_batch(aqsg_batch_s* b, cudaStream_t s) {
 static void free_batch(aqsg_batch_s* b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
-    for (int c = 0; c < 3; ++c) {
-        if (b->d_small_items[c]) cudaFree(b->d_small_items[c]);
-        if (b->d_small_ops[c]) cudaFree(b->d_small_ops[c]);
+    if (b->host_only) {  // nothing on the device
+        delete[] b->h_plans;
+        delete b;
+        return;
     }
-    if (b->d_large) cudaFree(b->d_large);
+    for (int c = 0; c < 3; ++c)
+        if (b->d_small_items[c]) cudaFree(b->d_small_items[c]);
+    if (b->d_plans) cudaFree(b->d_plans);
+    if (b->h_plans) cudaFreeHost(b->h_plans);
     for (LargeGroup& gr : b->groups) {
         if (gr.regs) cudaFree(gr.regs);
         if (gr.partials) cudaFree(gr.partials);
@@ -494,88 +636,32 @@ int aqsg_batch_create(aqsg_ctx ctx, const aqsg_circuit* circuits, int count, aqs
     AQSG_CUDA_TRY(cudaSetDevice(ctx->device));
     auto* b = new aqsg_batch_s();
     b->ctx = ctx;
-    b->count = count;
-    b->n.resize(count);
-    b->out_off.resize(count);
-    for (int i = 0; i < count; ++i) {
-        const int n = circuits[i].n;
-        if (n < 1 || n > 30) {
-            delete b;
-            return set_error(AQSG_ERR_INVALID_ARGUMENT, "Batch registers take 1 to 30 qubits");
-        }
-        if (circuits[i].count > 0 && !circuits[i].ops) {
-            delete b;
-            return set_error(AQSG_ERR_NULL, "NULL op list");
-        }
-        b->n[i] = n;
-        b->out_off[i] = b->out_doubles;
-        b->out_doubles += 2 * (size_t)n;
+    if (int rc = init_shape(b, circuits, count)) {
+        delete b;
+        return rc;
     }
-    int rc = encode_batch(b, circuits, true);
+    int rc = encode_batch(b, circuits);
     auto fail = [&](int code) {
         free_batch(b);
         return code;
     };
     if (rc) return fail(rc);
-    cudaError_t e = cudaSuccess;
+    layout_batch(b);
+    cudaError_t e = cudaMallocHost((void**)&b->h_plans, std::max<size_t>(b->plans_bytes, 256));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_plans, std::max<size_t>(b->plans_bytes, 256));
+    if (e == cudaSuccess) {
+        fill_image(b);
+        for (int c = 0; c < 3; ++c)
+            if (!b->items[c].empty()) b->d_small_ops[c] = (char*)b->d_plans + b->small_base[c];
+        b->d_large = (char*)b->d_plans + b->large_base;
+    }
     for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
         if (b->items[c].empty()) continue;
-        const size_t tb = b->small_table[c].size();
-        const size_t poff = (tb + 255) & ~size_t(255);
-        e = cudaMalloc(&b->d_small_ops[c], poff + b->small_pool[c].size() + 16);
-        if (e == cudaSuccess) e = cudaMalloc(&b->d_small_items[c], sizeof(SmallItem) * b->items[c].size());
+        e = cudaMalloc(&b->d_small_items[c], sizeof(SmallItem) * b->items[c].size());
         if (e == cudaSuccess)
             e = cudaMemcpy(b->d_small_items[c], b->items[c].data(), sizeof(SmallItem) * b->items[c].size(),
                            cudaMemcpyHostToDevice);
     }
-    // group the large registers with equal plan geometry
-    b->grouped.assign(b->large.size(), 0);
-    {
-        std::map<std::vector<uint64_t>, std::vector<size_t>> by_key;
-        for (size_t k = 0; k < b->large.size(); ++k) {
-            const TilePlan& p = b->plans[k];
-            std::vector<uint64_t> key = {(uint64_t)p.n, p.table.size(), p.pool.size(), p.passes.size()};
-            for (const TilePass& ps : p.passes) {
-                key.push_back(((uint64_t)ps.m << 48) | ((uint64_t)ps.L << 40) | ((uint64_t)ps.tc << 36) |
-                              ((uint64_t)ps.matk << 32) | ps.first);
-                key.push_back(ps.count);
-                key.push_back(((uint64_t)ps.tc_blob << 32) | ps.tc_bytes);
-                uint64_t bits = 0;
-                for (int i = 0; i < ps.m; ++i) bits |= 1ull << ps.tbits[i];
-                key.push_back(bits);
-            }
-            by_key[key].push_back(k);
-        }
-        for (auto& kv : by_key) {
-            const int n = b->plans[kv.second[0]].n;
-            const size_t per_chunk = std::max<size_t>(1, std::min<size_t>(kGroupBytes >> (n + 3), 65535));
-            for (size_t at = 0; at < kv.second.size(); at += per_chunk) {
-                LargeGroup gr;
-                gr.n = n;
-                gr.members.assign(kv.second.begin() + (long)at,
-                                  kv.second.begin() + (long)std::min(kv.second.size(), at + per_chunk));
-                for (size_t k : gr.members) b->grouped[k] = 1;
-                b->groups.push_back(std::move(gr));
-            }
-        }
-    }
-    // device plan area: each group's members at a fixed stride, then the rest
-    b->plan_off.assign(b->plans.size(), 0);
-    size_t large_bytes = 0;
-    for (LargeGroup& gr : b->groups) {
-        const TilePlan& p = b->plans[gr.members[0]];
-        gr.stride = (p.pool_offset() + p.pool.size() + 255) & ~size_t(255);
-        gr.dev_off = large_bytes;
-        for (size_t j = 0; j < gr.members.size(); ++j) b->plan_off[gr.members[j]] = large_bytes + j * gr.stride;
-        large_bytes += gr.members.size() * gr.stride;
-    }
-    for (size_t k = 0; k < b->plans.size(); ++k) {
-        if (b->grouped[k]) continue;
-        const TilePlan& p = b->plans[k];
-        b->plan_off[k] = large_bytes;
-        large_bytes += (p.pool_offset() + p.pool.size() + 255) & ~size_t(255);
-    }
-    if (e == cudaSuccess && large_bytes) e = cudaMalloc(&b->d_large, large_bytes);
     for (LargeGroup& gr : b->groups) {
         if (e != cudaSuccess) break;
         const size_t members = gr.members.size();
@@ -650,7 +736,9 @@ int aqsg_batch_create(aqsg_ctx ctx, const aqsg_circuit* circuits, int count, aqs
 int aqsg_batch_update(aqsg_batch b, const aqsg_circuit* circuits) {
     if (!b || !circuits) return set_error(AQSG_ERR_NULL, "NULL argument");
     AQSG_CUDA_TRY(cudaSetDevice(b->ctx->device));
-    if (int rc = encode_batch(b, circuits, false)) return rc;
+    // the previous run has finished reading the device image (runs end
+    // with a synchronize), so the pinned image can be rewritten
+    if (int rc = update_image(b, circuits)) return rc;
     return upload_batch(b, b->ctx->stream);
 }
 
@@ -699,6 +787,36 @@ int aqsg_batch_tuning(aqsg_batch b, int* fuse_qubits, int* tensor_cores) {
         if (tensor_cores) tensor_cores[k] = b->tc[k];
     }
     return AQSG_OK;
+}
+
+int aqsg_debug_batch_image(const aqsg_circuit* circuits, int count, const int* fuse, const int* tc,
+                           const aqsg_circuit* update, void* image, size_t capacity, size_t* bytes) {
+    if (!circuits || !bytes) return set_error(AQSG_ERR_NULL, "NULL argument");
+    if (count < 1) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Empty batch");
+    auto* b = new aqsg_batch_s();
+    b->host_only = true;
+    std::vector<int> zeros(count, 0);  // at most one large register per circuit
+    b->preset_fuse = fuse ? fuse : zeros.data();
+    b->preset_tc = tc ? tc : zeros.data();
+    int rc = init_shape(b, circuits, count);
+    if (!rc) rc = encode_batch(b, circuits);
+    if (!rc) {
+        layout_batch(b);
+        b->h_plans = new unsigned char[std::max<size_t>(b->plans_bytes, 1)];
+        fill_image(b);
+        if (update) rc = update_image(b, update);
+    }
+    if (!rc) {
+        *bytes = b->plans_bytes;
+        if (image) {
+            if (capacity < b->plans_bytes)
+                rc = set_error(AQSG_ERR_OUT_OF_RANGE, "Image buffer too small");
+            else
+                std::memcpy(image, b->h_plans, b->plans_bytes);
+        }
+    }
+    free_batch(b);
+    return rc;
 }
 
 int aqsg_batch_free(aqsg_batch b) {

@@ -32,6 +32,16 @@ int aqsg_debug_tile_plan(int n, int dtype, const aqsg_op* ops, int count, int fu
                          void* table, size_t table_capacity, size_t* table_bytes,
                          void* pool, size_t pool_capacity, size_t* pool_bytes);
 
+/* The plan image aqsg_batch_create uploads for a batch of circuits, byte
+ * for byte: each size class's op table and operand pool, then the plans of
+ * the registers of more than 14 qubits.  Built on the host, with the fusion
+ * width fuse[k] and tensor-core choice tc[k] of the k-th register of more
+ * than 14 qubits given instead of tuned (NULL: 0 for all).  With update
+ * non-NULL: the image after aqsg_batch_update(update) instead.  Call with
+ * image NULL to get the size. */
+int aqsg_debug_batch_image(const aqsg_circuit* circuits, int count, const int* fuse, const int* tc,
+                           const aqsg_circuit* update, void* image, size_t capacity, size_t* bytes);
+
 #ifdef __cplusplus
 }
 #endif
