@@ -30,7 +30,6 @@ struct SmallItem {
     uint32_t out;       // offset (doubles) of its 2n raw results
 };
 
-constexpr int kSmallMaxQubits = 14;
 constexpr int kZMaxBits = 14;
 
 __device__ __forceinline__ double warp_sum_b(double v) {

@@ -573,28 +573,30 @@ static void tc_operand(const std::vector<double>& mk, int k, std::vector<unsigne
     out.resize(at + 2 * split, 0);
     // each complex entry is split once; -Ui is the sign-flipped split of Ui
     // (rounding to nearest even is symmetric)
-    std::vector<uint16_t> hi(N * K), lo(N * K);
+    unsigned char* hi = &out[at];
+    unsigned char* lo = hi + split;
     auto split16 = [](double v, uint16_t& h, uint16_t& l) {
         h = host_bf16((float)v);
         l = host_bf16((float)(v - (double)host_bf16_val(h)));
     };
-    auto put = [&](uint32_t n, uint32_t kk, uint16_t h, uint16_t l) {
-        const uint32_t off = kmajor_off(n, kk, K) / 2u;
-        hi[off] = h;
-        lo[off] = l;
+    // the 2x2 real block of entry (r, c) sits in one 8x8 core matrix (2r
+    // and 2c are even): (2r, 2c) and (2r, 2c+1) are adjacent halves of a
+    // 32-bit word, rows 2r and 2r+1 are 16 bytes apart
+    auto put = [](unsigned char* p, uint16_t r, uint16_t i) {
+        const uint32_t w0 = (uint32_t)r | ((uint32_t)(i ^ 0x8000u) << 16);  // Ur, -Ui
+        const uint32_t w1 = (uint32_t)i | ((uint32_t)r << 16);              // Ui, Ur
+        std::memcpy(p, &w0, 4);
+        std::memcpy(p + 16, &w1, 4);
     };
     for (uint32_t r = 0; r < D; ++r)
         for (uint32_t c = 0; c < D; ++c) {
             uint16_t rh, rl, ih, il;
             split16(mk[2 * (r * D + c)], rh, rl);
             split16(mk[2 * (r * D + c) + 1], ih, il);
-            put(2 * r, 2 * c, rh, rl);
-            put(2 * r, 2 * c + 1, (uint16_t)(ih ^ 0x8000u), (uint16_t)(il ^ 0x8000u));
-            put(2 * r + 1, 2 * c, ih, il);
-            put(2 * r + 1, 2 * c + 1, rh, rl);
+            const uint32_t off = kmajor_off(2 * r, 2 * c, K);
+            put(hi + off, rh, ih);
+            put(lo + off, rl, il);
         }
-    std::memcpy(&out[at], hi.data(), split);
-    std::memcpy(&out[at + split], lo.data(), split);
 }
 
 static void pad_to(std::vector<unsigned char>& v, size_t align) {
@@ -732,7 +734,7 @@ static std::vector<TileOp> register_phases(const std::vector<TileOp>& ops, int m
                                            std::vector<unsigned char>& pool) {
     const int rb = phase_reg_bits(dtype);
     if (m < rb + kPhaseMinSlotBits || m > 15) return ops;
-    const uint32_t E = 1u << rb, ALL = (1u << E) - 1u;
+    const uint32_t E = 1u << rb;
     std::vector<TileOp> out;
     out.reserve(ops.size() + 8);
     size_t i = 0;
@@ -968,6 +970,7 @@ int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, Tile
         for (size_t i = 0; i < p.bits.size(); ++i) local[p.bits[i]] = (int)i;
         const bool tc_pass = tc_on && dtype == AQSG_C64 && tp.m == kTcTileBits;
         std::vector<unsigned char> blob;  // this pass's tensor-core operands
+        if (tc_pass) blob.reserve(kTcBlobMax);
         std::vector<TileOp> pops;         // this pass's table
         for (const LOp* o : p.ops) {
             TileOp t;
@@ -999,17 +1002,17 @@ int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, Tile
                     pad_to(plan->pool, 256);
                     t.mat = (int32_t)plan->pool.size();
                     tp.matk = 1;
-                    const int D = 1 << o->k;
-                    const size_t esz = dtype == AQSG_C64 ? 8 : 16;
-                    for (int e = 0; e < D * D; ++e) {
-                        const size_t at = plan->pool.size();
-                        plan->pool.resize(at + esz);
-                        if (dtype == AQSG_C64) {
-                            const float v[2] = {(float)o->mk[2 * e], (float)o->mk[2 * e + 1]};
-                            std::memcpy(&plan->pool[at], v, 8);
-                        } else {
-                            std::memcpy(&plan->pool[at], &o->mk[2 * e], 16);
+                    const size_t DD = (size_t)1 << (2 * o->k);
+                    const size_t at = plan->pool.size();
+                    if (dtype == AQSG_C64) {
+                        plan->pool.resize(at + 8 * DD);
+                        for (size_t e = 0; e < 2 * DD; ++e) {
+                            const float v = (float)o->mk[e];
+                            std::memcpy(&plan->pool[at + 4 * e], &v, 4);
                         }
+                    } else {
+                        plan->pool.resize(at + 16 * DD);
+                        std::memcpy(&plan->pool[at], o->mk.data(), 16 * DD);
                     }
                 }
             }
