@@ -18,6 +18,7 @@
 #include <map>
 #include <functional>
 #include <mutex>
+#include <unordered_map>
 
 #include "tile_device.cuh"
 
@@ -637,8 +638,33 @@ static size_t tc_op_bytes(int k) {
 // for the operand gather (t.lt1 = lane bits on data columns, the rest on
 // matrix rows): the split whose first warps touch the fewest shared-memory
 // wavefronts, reading the padded tile (row stride kTcRowStride bytes) and
-// writing the 4-byte operand words.
+// writing the 4-byte operand words.  Both depend only on the op's tile
+// bits, so they are computed once per host thread and bit set.
+constexpr size_t kTcTableBytes = 1024 + 64;
+static int tc_tables_compute(const TileOp& t, unsigned char* out);
+
 static void tc_tables(TileOp& t, std::vector<unsigned char>& blob) {
+    struct Entry {
+        unsigned char bytes[kTcTableBytes];
+        int cb;
+    };
+    thread_local std::unordered_map<uint64_t, Entry> memo;
+    uint64_t key = (uint64_t)t.k;
+    for (int i = 0; i < t.k; ++i) key |= (uint64_t)t.ltb[i] << (4 + 5 * i);
+    auto it = memo.find(key);
+    if (it == memo.end()) {
+        Entry e;
+        std::memset(e.bytes, 0, sizeof(e.bytes));
+        e.cb = tc_tables_compute(t, e.bytes);
+        it = memo.emplace(key, e).first;
+    }
+    blob.insert(blob.end(), it->second.bytes, it->second.bytes + kTcTableBytes);
+    t.lt1 = it->second.cb;
+}
+
+// The tables of tc_tables into out (kTcTableBytes, zeroed); returns the
+// lane split.
+static int tc_tables_compute(const TileOp& t, unsigned char* out) {
     const int k = t.k;
     uint32_t tmask = 0;
     for (int i = 0; i < k; ++i) tmask |= 1u << t.ltb[i];
@@ -660,15 +686,13 @@ static void tc_tables(TileOp& t, std::vector<unsigned char>& blob) {
             if ((r >> (k - 1 - i)) & 1u) off |= 1u << t.ltb[i];
         offr[r] = off;
     }
-    const size_t at = blob.size();
-    blob.resize(at + 1024 + 64, 0);
     for (uint32_t c = 0; c < cols; ++c) {
         const uint16_t v = (uint16_t)colbase[c];
-        std::memcpy(&blob[at + 2 * c], &v, 2);
+        std::memcpy(out + 2 * c, &v, 2);
     }
     for (uint32_t r = 0; r < (1u << k); ++r) {
         const uint16_t v = (uint16_t)offr[r];
-        std::memcpy(&blob[at + 1024 + 2 * r], &v, 2);
+        std::memcpy(out + 1024 + 2 * r, &v, 2);
     }
     // lane split: cb column bits, 5 - cb row bits (5 - cb <= k)
     const uint32_t pad = (kTcRowStride - 256u) / 8u;  // float2 elements of padding per row
@@ -696,7 +720,7 @@ static void tc_tables(TileOp& t, std::vector<unsigned char>& blob) {
             best_cb = cb;
         }
     }
-    t.lt1 = best_cb;
+    return best_cb;
 }
 
 // Encode the passes of `ops` into a table of TileOps and an operand pool.
