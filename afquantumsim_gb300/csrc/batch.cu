@@ -345,7 +345,7 @@ static int encode_batch(aqsg_batch_s* b, const aqsg_circuit* cs) {
             b->small_pool[cls].insert(b->small_pool[cls].end(), plan.pool.begin(), plan.pool.end());
             const size_t w = b->small_table[cls].size();
             b->small_table[cls].insert(b->small_table[cls].end(), plan.table.begin(), plan.table.end());
-            if (relocate_tile_matrices(&b->small_table[cls][w], plan.table.size() / tsz, (int32_t)pbase))
+            if (relocate_tile_matrices(b->small_table[cls].data() + w, plan.table.size() / tsz, (int32_t)pbase))
                 b->class_matk[cls] = true;
             sl.table_at = w;     // within the class table, until laid out
             sl.pool_at = pbase;  // within the class pool

@@ -326,6 +326,16 @@ int aqsg_circuit_from_text(const char* text, int* n_out, aqsg_op* ops, int capac
         if (int rc = parse_op(toks[i], &parsed[i - 1])) return rc;
         doubles += parsed[i - 1].mat.size();
     }
+    // validated before anything is returned, so a size query and the
+    // parse proper fail alike
+    {
+        std::vector<aqsg_op> check(parsed.size());
+        for (size_t i = 0; i < parsed.size(); ++i) {
+            check[i] = parsed[i].op;
+            if (!parsed[i].mat.empty()) check[i].matrix = parsed[i].mat.data();
+        }
+        if (int rc = aqsg_check_ops((int)n, check.data(), (int)check.size())) return rc;
+    }
     *n_out = (int)n;
     *count = (int)parsed.size();
     if (matrix_count) *matrix_count = doubles;
@@ -342,7 +352,7 @@ int aqsg_circuit_from_text(const char* text, int* n_out, aqsg_op* ops, int capac
             at += parsed[i].mat.size();
         }
     }
-    return aqsg_check_ops((int)n, ops, (int)parsed.size());
+    return AQSG_OK;
 }
 
 }  // extern "C"

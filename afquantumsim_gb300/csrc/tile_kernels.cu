@@ -1404,7 +1404,7 @@ extern "C" int aqsg_debug_tile_plan(int n, int dtype, const aqsg_op* ops, int co
     }
     if (table) {
         if (table_capacity < plan.table.size()) return set_error(AQSG_ERR_OUT_OF_RANGE, "Table buffer too small");
-        std::memcpy(table, plan.table.data(), plan.table.size());
+        if (!plan.table.empty()) std::memcpy(table, plan.table.data(), plan.table.size());
     }
     if (pool && !plan.pool.empty()) {
         if (pool_capacity < plan.pool.size()) return set_error(AQSG_ERR_OUT_OF_RANGE, "Pool buffer too small");

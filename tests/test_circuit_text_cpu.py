@@ -63,3 +63,53 @@ def test_malformed_text(text, exc, msg):
         aq.circuit_from_text(text)
     if msg:
         assert msg in str(e.value)
+
+
+def test_mutated_text_parses_or_fails_cleanly():
+    """Random edits of valid texts (deleted, inserted, repeated or cut
+    characters) either read as a circuit whose canonical text reads back to
+    itself and whose ops pass the gate checks, or fail with an engine
+    error; the parser never reads past its input."""
+    rng = np.random.default_rng(17)
+    bases = [aq.circuit_to_text(n, _kat.random_circuit(n, 12, s)) for n, s in [(3, 1), (5, 2), (7, 3)]]
+    bases.append("4;X,0,1:3;X,1,1:0,2;Swap,0,2:1,3;S†,0,1:2;B;P;U(1,0,0,0,0,0,1,0),0,1:2;")
+    alphabet = list("0123456789;:,.()~-+eE ") + ["RotX", "U(", "†", "\t", "\n", "1e308", "nan", "-0"]
+    errors = aq.AqsgError
+    parsed = failed = 0
+    for trial in range(3000):
+        t = bases[trial % len(bases)]
+        for _ in range(int(rng.integers(1, 4))):
+            i = int(rng.integers(0, len(t) + 1))
+            op = int(rng.integers(0, 4))
+            if op == 0 and t:
+                t = t[:i] + t[i + 1:]
+            elif op == 1:
+                t = t[:i] + alphabet[int(rng.integers(len(alphabet)))] + t[i:]
+            elif op == 2:
+                j = min(len(t), i + int(rng.integers(1, 8)))
+                t = t[:j] + t[i:j] + t[j:]
+            else:
+                t = t[:i]
+        try:
+            n, ops = aq.circuit_from_text(t)
+        except errors:
+            failed += 1
+            continue
+        parsed += 1
+        aq.check_ops(n, list(ops))
+        canon = aq.circuit_to_text(n, ops)
+        n2, back = aq.circuit_from_text(canon)
+        assert n2 == n and aq.circuit_to_text(n2, back) == canon
+    assert parsed > 100 and failed > 100
+
+
+def test_size_query_validates_like_the_parse():
+    """The size query (ops NULL) refuses what the parse proper refuses."""
+    import ctypes as C
+    lib = aq.load_library()
+    n, cnt, nd = C.c_int(), C.c_int(), C.c_size_t()
+    for text in ["4;X,1,1:0,22;", "3;Swap,0,2:1,1;", "2;U(1,0,0,0,0,0,1,0),0,1:2;"]:
+        rc = lib.aqsg_circuit_from_text(text.encode(), C.byref(n), None, 0, C.byref(cnt), None, 0, C.byref(nd))
+        assert rc != 0
+        with pytest.raises(aq.AqsgError):
+            aq.circuit_from_text(text)
