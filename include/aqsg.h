@@ -350,7 +350,9 @@ typedef struct aqsg_batch_s* aqsg_batch;
 int aqsg_batch_create(aqsg_ctx ctx, const aqsg_circuit* circuits, int count, aqsg_batch* out);
 
 /* Swap in new parameters (angles, matrices): the same count, qubit counts,
- * gate kinds and operands as at creation; the graph is kept. */
+ * gate kinds and operands as at creation; the graph is kept.  Circuits whose
+ * encoding changes shape (op records, operand sizes, passes) are refused
+ * with AQSG_ERR_INVALID_ARGUMENT and the device copy is left as it was. */
 int aqsg_batch_update(aqsg_batch b, const aqsg_circuit* circuits);
 
 /* Replay the graph.  z receives sum_i n_i values (<Z_q> of circuit i at
