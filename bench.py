@@ -392,12 +392,23 @@ def bench_vqe_batch(ctx, count=4096, seed=5):
     b.run()
     torch.cuda.nvtx.range_pop()
     rng = np.random.default_rng(seed + 1)
-    new = []
-    for n, ops in items:  # same shapes (n >= 8: 3n ops per layer), new angles
-        L = len(ops) // (3 * n)
-        new.append((n, circuits.vqe_ops_array(n, L, rng.uniform(-np.pi, np.pi, size=(L, n, 2)))))
+
+    def new_angles():
+        out = []
+        for n, ops in items:  # same shapes (n >= 8: 3n ops per layer), new angles
+            L = len(ops) // (3 * n)
+            out.append((n, circuits.vqe_ops_array(n, L, rng.uniform(-np.pi, np.pi, size=(L, n, 2)))))
+        return out
+
+    # the first update after creation, then one in steady state (what an
+    # optimiser loop pays per step), followed by its run
+    first, new = new_angles(), new_angles()
+    t0 = _t.perf_counter()
+    b.update(first)
+    first_update_s = _t.perf_counter() - t0
     t0 = _t.perf_counter()
     b.update(new)
+    update_s = _t.perf_counter() - t0
     z, zz = b.run()
     update_run_s = _t.perf_counter() - t0
     # accuracy on a sample against the FP64 oracle
@@ -429,6 +440,7 @@ def bench_vqe_batch(ctx, count=4096, seed=5):
             "large_circuit_tuning": dict(tuned),
             "create_s": round(create_s, 3), "sweep_ms": round(1e3 * sweep_s, 3),
             "circuits_per_s": round(count / sweep_s, 1), "gate_apps_per_s": round(gates / sweep_s, 1),
+            "first_update_ms": round(1e3 * first_update_s, 3), "update_ms": round(1e3 * update_s, 3),
             "update_and_run_ms": round(1e3 * update_run_s, 3),
             "max_abs_err_z_vs_fp64_sample": err,
             "cpu_baseline": {"kind": "port", "cores": threads, "sample": f"{len(sample)} circuits (every 64th)",
