@@ -346,7 +346,10 @@ typedef struct aqsg_batch_s* aqsg_batch;
  * run as a group, one launch per tile pass for all of them (the choice is
  * cached per structure and timed over a group size that depends on n only,
  * so a circuit runs the same way alone and in any batch).  The whole run is
- * captured once as a CUDA graph. */
+ * captured once as a CUDA graph.  Create and update lower and encode the
+ * circuits on all host threads; the encoded plans are kept in one pinned
+ * host image, uploaded with one copy, and the caller's circuits are not
+ * retained. */
 int aqsg_batch_create(aqsg_ctx ctx, const aqsg_circuit* circuits, int count, aqsg_batch* out);
 
 /* Swap in new parameters (angles, matrices): the same count, qubit counts,
