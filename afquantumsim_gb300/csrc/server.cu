@@ -339,24 +339,29 @@ int aqsg_server_submit(aqsg_server s, int n, const aqsg_op* ops, int count, int 
     r->shots = shots;
     r->seed = seed;
     r->outcomes = outcomes;
-    std::vector<LOp> low;
     int rc = AQSG_OK;
+    int fused_ops = 0;
     if (fuse_qubits > 0) {
+        // encoded straight from the program's ops (no copy of the fused
+        // matrices)
         aqsg_program p = nullptr;
         rc = aqsg_compile(n, s->dtype, ops, count, fuse_qubits, &p);
         if (rc == AQSG_OK) {
-            low = program_ops(p);
+            fused_ops = (int)program_ops(p).size();
+            rc = encode_tiled(n, s->dtype, program_ops(p), true, &r->plan);
             aqsg_program_free(p);
         }
     } else {
+        std::vector<LOp> low;
         low.reserve(count);
         for (int i = 0; i < count && rc == AQSG_OK; ++i) {
             LOp o;
             rc = lower_op(n, s->dtype, ops[i], &o);
             if (rc == AQSG_OK && o.cls != L_NOP) low.push_back(std::move(o));
         }
+        fused_ops = (int)low.size();
+        if (rc == AQSG_OK) rc = encode_tiled(n, s->dtype, low, true, &r->plan);
     }
-    if (rc == AQSG_OK) rc = encode_tiled(n, s->dtype, low, true, &r->plan);
     if (rc == AQSG_OK && !r->plan.passes.empty()) {
         r->table_bytes = r->plan.pool_offset() + r->plan.pool.size();
         if (r->table_bytes + 16 > kLaneTableBytes)
@@ -366,7 +371,7 @@ int aqsg_server_submit(aqsg_server s, int n, const aqsg_op* ops, int count, int 
         delete r;
         return rc;
     }
-    r->fused_ops = (int)low.size();
+    r->fused_ops = fused_ops;
     r->order = s->buddy.order_for((uint64_t)amp_bytes(s->dtype) << n);
     {
         std::lock_guard<std::mutex> g(s->mu);
