@@ -653,6 +653,10 @@ static void tc_tables(TileOp& t, std::vector<unsigned char>& blob) {
     for (int i = 0; i < t.k; ++i) key |= (uint64_t)t.ltb[i] << (4 + 5 * i);
     auto it = memo.find(key);
     if (it == memo.end()) {
+        // fused unitaries list their bits in one order (at most 1507 sets of
+        // 3..5 of the 12 tile bits); user unitaries may use any order, so
+        // the memo is bounded
+        if (memo.size() >= 4096) memo.clear();
         Entry e;
         std::memset(e.bytes, 0, sizeof(e.bytes));
         e.cb = tc_tables_compute(t, e.bytes);
