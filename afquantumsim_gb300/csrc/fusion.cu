@@ -15,8 +15,8 @@
 // row operations to the 2^k x 2^k identity.
 #include <algorithm>
 #include <atomic>
-
 #include <cstring>
+#include <type_traits>
 
 #include "aqsg_internal.h"
 
@@ -350,7 +350,8 @@ static int fuse(int n, const std::vector<LOp>& in, const std::vector<aqsg_op>& s
             out->push_back(std::move(f));
         } else {
             // the exported op reads the matrix the lowered op holds (its heap
-            // buffer stays put when the op vector grows)
+            // buffer stays put when the op vector grows: ops are moved)
+            static_assert(std::is_nothrow_move_constructible<LOp>::value, "fused ops must move on growth");
             f.cls = L_MATK;
             out->push_back(std::move(f));
             ex.matrix = out->back().mk.data();
