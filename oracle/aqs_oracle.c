@@ -2,7 +2,8 @@
  * aqs_oracle.c — CPU oracle for the GB300 state-vector engine.
  *
  * TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
- * CPU-baseline leg of bench.py as the checker.  The product never links it.
+ * CPU-baseline leg of bench.py (results are compared with it; the
+ * CPU-baseline leg times it as the CPU arm).  The product never links it.
  *
  * Built with -ffp-contract=off so x86-64 and aarch64 hosts round alike.
  * See aqs_oracle.h for what each family restates.

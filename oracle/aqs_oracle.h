@@ -2,8 +2,8 @@
  * aqs_oracle.h — CPU oracle for the GB300 state-vector engine.
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product links, loads or calls
- * this code: it is the checker used by tests/, __graft_entry__.smoke() and
- * bench.py's CPU-baseline leg.
+ * this code: tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+ * leg compare results with it (the last also times it as the CPU arm).
  *
  * Two restatements of arrayfire/afQuantumSim's QSimulator::simulate
  * (src/quantum.cpp:277-291):

@@ -1,8 +1,9 @@
 """ctypes binding of the CPU oracle (oracle/aqs_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
-CPU-baseline leg of bench.py, always as the checker, never as the thing
-measured or shipped.
+CPU-baseline leg of bench.py: GPU results are compared with it, and the
+CPU-baseline leg times it as the CPU arm; it is never the product measured
+or shipped.
 """
 from __future__ import annotations
 
