@@ -43,7 +43,7 @@ EXPORTS = [
     "aqsg_server_wait_idle", "aqsg_server_get_stats", "aqsg_server_destroy",
     "aqsg_expect_pauli", "aqsg_autotune", "aqsg_batch_tuning", "aqsg_selftest_bounded_wait",
     "aqsg_state_download_async", "aqsg_circuit_to_text", "aqsg_circuit_from_text",
-    "aqsg_debug_tile_plan", "aqsg_debug_batch_image",
+    "aqsg_debug_tile_plan", "aqsg_debug_batch_image", "aqsg_debug_ctx_scratch",
 ]
 
 _lib = None
@@ -291,6 +291,17 @@ class Context:
         v = C.c_void_p()
         _check(self.lib.aqsg_ctx_stream(self.h, C.byref(v)))
         return v.value or 0
+
+    def scratch_bytes(self) -> list:
+        """aqsg_debug_ctx_scratch: bytes held in each of the context's
+        grown-on-demand device scratch buffers (a testing aid)."""
+        lib = load_library()
+        f = lib.aqsg_debug_ctx_scratch
+        f.argtypes = [C.c_void_p, C.POINTER(C.c_size_t), C.c_int, C.POINTER(C.c_int)]
+        f.restype = C.c_int
+        buf, cnt = (C.c_size_t * 8)(), C.c_int()
+        _check(f(self.h, buf, 8, C.byref(cnt)))
+        return list(buf[:cnt.value])
 
     def launch_count(self) -> int:
         v = C.c_uint64()

@@ -8,6 +8,7 @@
 #include <string>
 
 #include "aqsg_internal.h"
+#include "../../include/aqsg_debug.h"
 
 namespace aqsg {
 
@@ -295,7 +296,7 @@ int aqsg_init(int device, aqsg_ctx* out) {
     AQSG_CUDA_TRY(cudaGetDeviceCount(&count));
     if (device < 0 || device >= count)
         return set_error(AQSG_ERR_OUT_OF_RANGE, "No CUDA device " + std::to_string(device));
-    AQSG_CUDA_TRY(cudaSetDevice(device));
+    AQSG_ON_DEVICE(device);
     auto* c = new aqsg_ctx_s();
     c->device = device;
     cudaError_t e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
@@ -306,9 +307,21 @@ int aqsg_init(int device, aqsg_ctx* out) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->order, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         if (c->order) cudaEventDestroy(c->order);
+        if (c->d_err) cudaFree(c->d_err);
+        if (c->host_result) cudaFreeHost(c->host_result);
         if (c->stream) cudaStreamDestroy(c->stream);
         delete c;
         return cuda_error(e, "aqsg_init");
+    }
+    // the allocation-free sampler's static scratch becomes resident on this
+    // device now, not inside a caller's loop (lazy module loading)
+    if (int rc = noalloc_prepare(device)) {
+        cudaEventDestroy(c->order);
+        cudaFree(c->d_err);
+        cudaFreeHost(c->host_result);
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return rc;
     }
     *out = c;
     return AQSG_OK;
@@ -318,7 +331,7 @@ int aqsg_shutdown(aqsg_ctx ctx) {
     if (!ctx) return set_error(AQSG_ERR_NULL, "NULL context");
     if (ctx->live_states != 0)
         return set_error(AQSG_ERR_RUNTIME, "Context still owns live states");
-    cudaSetDevice(ctx->device);
+    DeviceScope scope(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     Scratch* all[] = {&ctx->partial, &ctx->prefix, &ctx->sample_u, &ctx->sample_o,
                       &ctx->ops, &ctx->probs};
@@ -350,6 +363,7 @@ int aqsg_set_tensor_cores(aqsg_ctx ctx, int enable) {
 
 int aqsg_synchronize(aqsg_ctx ctx) {
     if (!ctx) return set_error(AQSG_ERR_NULL, "NULL context");
+    AQSG_ON_DEVICE(ctx->device);
     AQSG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     return AQSG_OK;
 }
@@ -359,9 +373,17 @@ int aqsg_ctx_after(aqsg_ctx ctx, aqsg_ctx other) {
     if (ctx == other) return AQSG_OK;  // a stream is already ordered with itself
     if (ctx->device != other->device)
         return set_error(AQSG_ERR_INVALID_ARGUMENT, "Contexts on different devices");
-    AQSG_CUDA_TRY(cudaSetDevice(ctx->device));
+    AQSG_ON_DEVICE(ctx->device);
     AQSG_CUDA_TRY(cudaEventRecord(other->order, other->stream));
     AQSG_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, other->order, 0));
+    return AQSG_OK;
+}
+
+int aqsg_debug_ctx_scratch(aqsg_ctx ctx, size_t* bytes, int capacity, int* count) {
+    if (!ctx || !count) return set_error(AQSG_ERR_NULL, "NULL argument");
+    const Scratch* all[] = {&ctx->partial, &ctx->prefix, &ctx->sample_u, &ctx->sample_o, &ctx->ops, &ctx->probs};
+    *count = 6;
+    for (int i = 0; i < 6 && i < capacity && bytes; ++i) bytes[i] = all[i]->ptr ? all[i]->bytes : 0;
     return AQSG_OK;
 }
 
@@ -386,7 +408,7 @@ int aqsg_state_alloc(aqsg_ctx ctx, int n, int dtype, aqsg_state* out) {
                          "Maximum qubit count supported is " + std::to_string(AQSG_MAX_QUBITS));
     if (dtype != AQSG_C64 && dtype != AQSG_C128)
         return set_error(AQSG_ERR_INVALID_ARGUMENT, "Unknown dtype");
-    AQSG_CUDA_TRY(cudaSetDevice(ctx->device));
+    AQSG_ON_DEVICE(ctx->device);
     auto* s = new aqsg_state_s();
     s->ctx = ctx;
     s->n = n;
@@ -404,6 +426,7 @@ int aqsg_state_alloc(aqsg_ctx ctx, int n, int dtype, aqsg_state* out) {
 
 int aqsg_state_free(aqsg_state st) {
     if (!st) return set_error(AQSG_ERR_NULL, "NULL state");
+    DeviceScope scope(st->ctx->device);
     cudaStreamSynchronize(st->ctx->stream);
     if (st->d) cudaFree(st->d);
     st->ctx->live_states--;
@@ -420,18 +443,21 @@ int aqsg_state_info(aqsg_state st, int* n, int* dtype) {
 
 int aqsg_state_set_basis_index(aqsg_state st, uint64_t k) {
     if (int rc = check_state(st)) return rc;
+    AQSG_ON_DEVICE(st->ctx->device);
     if (k >= st->amps) return set_error(AQSG_ERR_OUT_OF_RANGE, "Basis index out of range");
     return launch_set_basis(st, k);
 }
 
 int aqsg_state_set_product(aqsg_state st, const float* amps) {
     if (int rc = check_state(st)) return rc;
+    AQSG_ON_DEVICE(st->ctx->device);
     if (!amps) return set_error(AQSG_ERR_NULL, "NULL qubit amplitudes");
     return launch_set_product(st, amps);
 }
 
 int aqsg_state_upload(aqsg_state st, const void* host, int normalize) {
     if (int rc = check_state(st)) return rc;
+    AQSG_ON_DEVICE(st->ctx->device);
     if (!host) return set_error(AQSG_ERR_NULL, "NULL host buffer");
     AQSG_CUDA_TRY(cudaMemcpyAsync(st->d, host, st->amps * amp_bytes(st->dtype),
                                   cudaMemcpyHostToDevice, st->ctx->stream));
@@ -446,6 +472,7 @@ int aqsg_state_upload(aqsg_state st, const void* host, int normalize) {
 
 int aqsg_state_download(aqsg_state st, void* host) {
     if (int rc = check_state(st)) return rc;
+    AQSG_ON_DEVICE(st->ctx->device);
     if (!host) return set_error(AQSG_ERR_NULL, "NULL host buffer");
     AQSG_CUDA_TRY(cudaMemcpyAsync(host, st->d, st->amps * amp_bytes(st->dtype),
                                   cudaMemcpyDeviceToHost, st->ctx->stream));
@@ -455,6 +482,7 @@ int aqsg_state_download(aqsg_state st, void* host) {
 
 int aqsg_state_download_async(aqsg_state st, void* host) {
     if (int rc = check_state(st)) return rc;
+    AQSG_ON_DEVICE(st->ctx->device);
     if (!host) return set_error(AQSG_ERR_NULL, "NULL host buffer");
     AQSG_CUDA_TRY(cudaMemcpyAsync(host, st->d, st->amps * amp_bytes(st->dtype),
                                   cudaMemcpyDeviceToHost, st->ctx->stream));
@@ -463,6 +491,7 @@ int aqsg_state_download_async(aqsg_state st, void* host) {
 
 int aqsg_state_download_range(aqsg_state st, uint64_t begin, uint64_t count, void* host) {
     if (int rc = check_state(st)) return rc;
+    AQSG_ON_DEVICE(st->ctx->device);
     if (!host) return set_error(AQSG_ERR_NULL, "NULL host buffer");
     if (begin > st->amps || count > st->amps - begin)
         return set_error(AQSG_ERR_OUT_OF_RANGE, "Range outside the register");
@@ -478,6 +507,7 @@ int aqsg_state_copy(aqsg_state dst, aqsg_state src) {
     if (int rc = check_state(src)) return rc;
     if (dst->n != src->n || dst->dtype != src->dtype)
         return set_error(AQSG_ERR_INVALID_ARGUMENT, "Registers differ in size or dtype");
+    AQSG_ON_DEVICE(src->ctx->device);
     AQSG_CUDA_TRY(cudaMemcpyAsync(dst->d, src->d, src->amps * amp_bytes(src->dtype),
                                   cudaMemcpyDeviceToDevice, src->ctx->stream));
     if (dst->ctx != src->ctx) AQSG_CUDA_TRY(cudaStreamSynchronize(src->ctx->stream));
@@ -520,7 +550,7 @@ int aqsg_apply_ops(aqsg_state st, const aqsg_op* ops, int count, int mode) {
     if (mode != AQSG_EXEC_PER_GATE) {
         if (count > 0 && !ops) return set_error(AQSG_ERR_NULL, "NULL op list");
         if (count < 0) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Negative op count");
-        AQSG_CUDA_TRY(cudaSetDevice(st->ctx->device));
+        AQSG_ON_DEVICE(st->ctx->device);
         // a circuit run before on this context reuses its checked, lowered,
         // encoded and uploaded plan
         return run_tiled_cached(st, plan_key(st, ops, count), [&](std::vector<LOp>* low) {
@@ -542,7 +572,7 @@ int aqsg_apply_ops(aqsg_state st, const aqsg_op* ops, int count, int mode) {
         if (int rc = lower_op(st->n, st->dtype, ops[i], &o)) return rc;
         if (o.cls != L_NOP) low.push_back(std::move(o));
     }
-    AQSG_CUDA_TRY(cudaSetDevice(st->ctx->device));
+    AQSG_ON_DEVICE(st->ctx->device);
     for (const LOp& o : low)
         if (int rc = launch_lop(st, o)) return rc;
     return AQSG_OK;
@@ -550,6 +580,7 @@ int aqsg_apply_ops(aqsg_state st, const aqsg_op* ops, int count, int mode) {
 
 int aqsg_qubit_prob(aqsg_state st, int qubit, double* out) {
     if (int rc = check_state(st)) return rc;
+    AQSG_ON_DEVICE(st->ctx->device);
     if (!out) return set_error(AQSG_ERR_NULL, "NULL output");
     if (qubit < 0 || qubit >= st->n)
         return set_error(AQSG_ERR_OUT_OF_RANGE, "Cannot obtain probability of the given qubit");
@@ -575,6 +606,7 @@ int aqsg_state_prob(aqsg_state st, uint64_t k, double* out) {
 
 int aqsg_probs(aqsg_state st, void* host, int out_dtype) {
     if (int rc = check_state(st)) return rc;
+    AQSG_ON_DEVICE(st->ctx->device);
     if (!host) return set_error(AQSG_ERR_NULL, "NULL host buffer");
     if (out_dtype != 0 && out_dtype != 1)
         return set_error(AQSG_ERR_INVALID_ARGUMENT, "out_dtype must be 0 (float) or 1 (double)");
@@ -589,12 +621,14 @@ int aqsg_probs(aqsg_state st, void* host, int out_dtype) {
 
 int aqsg_norm2(aqsg_state st, double* out) {
     if (int rc = check_state(st)) return rc;
+    AQSG_ON_DEVICE(st->ctx->device);
     if (!out) return set_error(AQSG_ERR_NULL, "NULL output");
     return reduce_prob(st, 0, 0, out);
 }
 
 int aqsg_sample(aqsg_state st, const double* u, uint64_t count, int rule, uint64_t* out) {
     if (int rc = check_state(st)) return rc;
+    AQSG_ON_DEVICE(st->ctx->device);
     if (count == 0) return AQSG_OK;
     if (!u || !out) return set_error(AQSG_ERR_NULL, "NULL buffer");
     if (rule != AQSG_SAMPLE_REFERENCE && rule != AQSG_SAMPLE_CLAMP)
@@ -604,6 +638,7 @@ int aqsg_sample(aqsg_state st, const double* u, uint64_t count, int rule, uint64
 
 int aqsg_sample_seeded(aqsg_state st, uint64_t seed, uint64_t count, int rule, uint64_t* out) {
     if (int rc = check_state(st)) return rc;
+    AQSG_ON_DEVICE(st->ctx->device);
     if (count == 0) return AQSG_OK;
     if (!out) return set_error(AQSG_ERR_NULL, "NULL buffer");
     if (rule != AQSG_SAMPLE_REFERENCE && rule != AQSG_SAMPLE_CLAMP)
@@ -613,6 +648,7 @@ int aqsg_sample_seeded(aqsg_state st, uint64_t seed, uint64_t count, int rule, u
 
 int aqsg_collapse_qubit(aqsg_state st, int qubit, double u, int* outcome, double* prob) {
     if (int rc = check_state(st)) return rc;
+    AQSG_ON_DEVICE(st->ctx->device);
     if (qubit < 0 || qubit >= st->n)
         return set_error(AQSG_ERR_OUT_OF_RANGE, "Cannot measure the state of the given qubit");
     uint64_t m = 1ull << (st->n - 1 - qubit);
@@ -630,6 +666,7 @@ int aqsg_collapse_qubit(aqsg_state st, int qubit, double u, int* outcome, double
 
 int aqsg_collapse_all(aqsg_state st, double u, uint64_t* outcome) {
     if (int rc = check_state(st)) return rc;
+    AQSG_ON_DEVICE(st->ctx->device);
     uint64_t k = 0;
     if (int rc = sample(st, &u, 0, false, 1, AQSG_SAMPLE_REFERENCE, &k)) return rc;
     if (int rc = launch_set_basis(st, k)) return rc;
@@ -639,6 +676,7 @@ int aqsg_collapse_all(aqsg_state st, double u, uint64_t* outcome) {
 
 int aqsg_expect_z(aqsg_state st, double* z, double* zz) {
     if (int rc = check_state(st)) return rc;
+    AQSG_ON_DEVICE(st->ctx->device);
     return expect_z(st, z, zz);
 }
 

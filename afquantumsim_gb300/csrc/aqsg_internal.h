@@ -23,6 +23,35 @@ int cuda_error(cudaError_t e, const char* where);
         if (e__ != cudaSuccess) return ::aqsg::cuda_error(e__, #expr); \
     } while (0)
 
+// Makes a context's device current for the duration of an entry point and
+// gives the calling thread back the device it had current on the way out,
+// so that one host thread can drive contexts on several GPUs in any order.
+class DeviceScope {
+  public:
+    explicit DeviceScope(int device) {
+        if (cudaGetDevice(&prev_) != cudaSuccess) prev_ = -1;
+        if (prev_ != device) {
+            err_ = cudaSetDevice(device);
+            switched_ = err_ == cudaSuccess && prev_ >= 0;
+        }
+    }
+    ~DeviceScope() {
+        if (switched_) cudaSetDevice(prev_);
+    }
+    DeviceScope(const DeviceScope&) = delete;
+    DeviceScope& operator=(const DeviceScope&) = delete;
+    cudaError_t error() const { return err_; }
+
+  private:
+    int prev_ = -1;
+    bool switched_ = false;
+    cudaError_t err_ = cudaSuccess;
+};
+#define AQSG_ON_DEVICE(dev)                                                   \
+    ::aqsg::DeviceScope aqsg_device_scope__(dev);                             \
+    if (aqsg_device_scope__.error() != cudaSuccess)                           \
+        return ::aqsg::cuda_error(aqsg_device_scope__.error(), "cudaSetDevice")
+
 // ---- lowered gate form ------------------------------------------------------
 // Every reference gate lowers to one of these classes acting on index bits
 // (bit = n-1-qubit).  Coefficients for c64 are float values (computed with
@@ -164,6 +193,9 @@ int sample(aqsg_state_s* st, const double* host_u, uint64_t seed, bool seeded,
 int launch_collapse_qubit(aqsg_state_s* st, uint64_t mask, int outcome,
                           double scale);
 int expect_z(aqsg_state_s* st, double* z, double* zz);
+// Looks up (once per device, with that device current) the device address of
+// the allocation-free sampler's static scratch, which loads its module.
+int noalloc_prepare(int device);
 // asynchronous variants (no host read; scratch reserved beforehand)
 int reserve_scratch(aqsg_ctx_s* c, int n, uint64_t shots);
 int launch_norm_to_device(aqsg_state_s* st, double* d_out);

@@ -632,7 +632,7 @@ int aqsg_batch_create(aqsg_ctx ctx, const aqsg_circuit* circuits, int count, aqs
     *out = nullptr;
     if (count < 1) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Empty batch");
     if (!circuits) return set_error(AQSG_ERR_NULL, "NULL circuit list");
-    AQSG_CUDA_TRY(cudaSetDevice(ctx->device));
+    AQSG_ON_DEVICE(ctx->device);
     auto* b = new aqsg_batch_s();
     b->ctx = ctx;
     if (int rc = init_shape(b, circuits, count)) {
@@ -734,7 +734,7 @@ int aqsg_batch_create(aqsg_ctx ctx, const aqsg_circuit* circuits, int count, aqs
 
 int aqsg_batch_update(aqsg_batch b, const aqsg_circuit* circuits) {
     if (!b || !circuits) return set_error(AQSG_ERR_NULL, "NULL argument");
-    AQSG_CUDA_TRY(cudaSetDevice(b->ctx->device));
+    AQSG_ON_DEVICE(b->ctx->device);
     // the previous run has finished reading the device image (runs end
     // with a synchronize), so the pinned image can be rewritten
     if (int rc = update_image(b, circuits)) return rc;
@@ -744,7 +744,7 @@ int aqsg_batch_update(aqsg_batch b, const aqsg_circuit* circuits) {
 int aqsg_batch_run(aqsg_batch b, double* z, double* zz) {
     if (!b) return set_error(AQSG_ERR_NULL, "NULL batch");
     aqsg_ctx_s* c = b->ctx;
-    AQSG_CUDA_TRY(cudaSetDevice(c->device));
+    AQSG_ON_DEVICE(c->device);
     AQSG_CUDA_TRY(cudaGraphLaunch(b->exec, c->stream));
     c->launches += b->kernels;
     AQSG_CUDA_TRY(cudaMemcpyAsync(b->h_out, b->d_out, sizeof(double) * b->out_doubles, cudaMemcpyDeviceToHost,
@@ -820,6 +820,7 @@ int aqsg_debug_batch_image(const aqsg_circuit* circuits, int count, const int* f
 
 int aqsg_batch_free(aqsg_batch b) {
     if (!b) return set_error(AQSG_ERR_NULL, "NULL batch");
+    DeviceScope scope(b->ctx->device);
     cudaStreamSynchronize(b->ctx->stream);
     free_batch(b);
     return AQSG_OK;

@@ -418,7 +418,7 @@ int aqsg_run_program(aqsg_state st, aqsg_program p, int mode) {
     if (mode < 0) mode = st->ctx->exec_mode;
     if (mode < AQSG_EXEC_AUTO || mode > AQSG_EXEC_TILED)
         return set_error(AQSG_ERR_INVALID_ARGUMENT, "Unknown execution mode");
-    AQSG_CUDA_TRY(cudaSetDevice(st->ctx->device));
+    AQSG_ON_DEVICE(st->ctx->device);
     if (mode == AQSG_EXEC_PER_GATE) {
         for (const LOp& o : p->ops)
             if (int rc = launch_lop(st, o)) return rc;

@@ -486,12 +486,15 @@ static void* g_noalloc_addr[kNoallocMaxDevices];
 // Device address of the static scratch on `device`, looked up once per device
 // with that device current.  (In host code g_noalloc_scratch names a host-side
 // stand-in, not device memory, so only the looked-up address is passed on.)
+// aqsg_init calls this for its device, so the module that holds the array is
+// loaded, and the array resident, before any sampling call; a sampling call
+// then only reads the cached address.
 static int noalloc_scratch(int device, unsigned char** out) {
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
     if (device < 0 || device >= kNoallocMaxDevices)
         return set_error(AQSG_ERR_OUT_OF_RANGE, "Device index beyond the allocation-free table");
     if (!g_noalloc_addr[device]) {
-        AQSG_CUDA_TRY(cudaSetDevice(device));
+        AQSG_ON_DEVICE(device);
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(allocation-free scratch)");
@@ -499,6 +502,11 @@ static int noalloc_scratch(int device, unsigned char** out) {
     }
     *out = (unsigned char*)g_noalloc_addr[device];
     return AQSG_OK;
+}
+
+int noalloc_prepare(int device) {
+    unsigned char* p = nullptr;
+    return noalloc_scratch(device, &p);
 }
 
 template <typename T>
@@ -547,6 +555,7 @@ extern "C" int aqsg_sample_noalloc(aqsg_state st, const double* u, uint64_t coun
                          "Allocation-free sampling takes at most " +
                              std::to_string(AQSG_NOALLOC_MAX_SHOTS) + " shots per call, got " +
                              std::to_string(count));
+    AQSG_ON_DEVICE(st->ctx->device);
     return st->dtype == AQSG_C64 ? sample_noalloc_t<float2>(st, u, count, rule, out)
                                  : sample_noalloc_t<double2>(st, u, count, rule, out);
 }
@@ -835,6 +844,7 @@ extern "C" int aqsg_state_compare(aqsg_state a, aqsg_state b, double* max_abs_di
     if (a->n != b->n) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Registers differ in qubit count");
     if (a->ctx != b->ctx) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Registers belong to different contexts");
     aqsg_ctx_s* c = a->ctx;
+    AQSG_ON_DEVICE(c->device);
     const unsigned grid = stream_grid(a, a->amps, 256);
     if (int rc = ensure_scratch(c->partial, sizeof(double) * 5 * grid)) return rc;
     double* part = (double*)c->partial.ptr;
@@ -1198,7 +1208,7 @@ extern "C" int aqsg_expect_pauli(aqsg_state st, const char* paulis, int count, d
     if (count < 0) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Negative string count");
     if (count == 0) return AQSG_OK;
     if (!paulis || !out) return set_error(AQSG_ERR_NULL, "NULL argument");
-    AQSG_CUDA_TRY(cudaSetDevice(st->ctx->device));
+    AQSG_ON_DEVICE(st->ctx->device);
     return st->dtype == AQSG_C64 ? expect_pauli_t<float2>(st, paulis, count, out)
                                  : expect_pauli_t<double2>(st, paulis, count, out);
 }
@@ -1239,7 +1249,7 @@ extern "C" int aqsg_selftest_bounded_wait(aqsg_ctx ctx, uint32_t limit_us, int* 
     using namespace aqsg;
     if (!ctx || !timed_out) return set_error(AQSG_ERR_NULL, "NULL argument");
     if (limit_us < 1 || limit_us > 100000) return set_error(AQSG_ERR_OUT_OF_RANGE, "Limit must be 1 us to 0.1 s");
-    AQSG_CUDA_TRY(cudaSetDevice(ctx->device));
+    AQSG_ON_DEVICE(ctx->device);
     if (int rc = ensure_scratch(ctx->partial, 64)) return rc;
     int* d_flag = reinterpret_cast<int*>(ctx->partial.ptr);
     k_wait_selftest<<<1, 1, 0, ctx->stream>>>((uint64_t)limit_us * 1000ull, d_flag);

@@ -282,6 +282,7 @@ int aqsg_server_create(int device, int dtype, uint64_t hbm_budget_bytes, int lan
     const int top_order = max_qubits + amp_order;
     const uint64_t tops = hbm_budget_bytes >> top_order;
     if (tops < 1) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Budget holds no register of max_qubits qubits");
+    AQSG_ON_DEVICE(device);
     auto* s = new aqsg_server_s();
     s->device = device;
     s->dtype = dtype;
@@ -448,7 +449,7 @@ int aqsg_server_destroy(aqsg_server s) {
     }
     s->cv_work.notify_one();
     if (s->worker.joinable()) s->worker.join();
-    cudaSetDevice(s->device);
+    DeviceScope scope(s->device);
     for (auto& kv : s->pending) delete kv.second;
     destroy_lanes(s);
     if (s->slab) cudaFree(s->slab);

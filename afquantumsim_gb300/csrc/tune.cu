@@ -71,6 +71,7 @@ void autotune_forget(aqsg_ctx ctx) {
 int autotune_impl(aqsg_ctx ctx, int n, int dtype, const aqsg_op* ops, int count, int reps, bool tiled_only,
                   aqsg_tune_entry* best, aqsg_tune_entry* all, int capacity, int* count_out) {
     if (!ctx || !best) return set_error(AQSG_ERR_NULL, "NULL argument");
+    AQSG_ON_DEVICE(ctx->device);
     if (count_out) *count_out = 0;
     if (reps < 1) reps = 1;
     if (int rc = aqsg_check_ops(n, ops, count)) return rc;
@@ -190,7 +191,7 @@ int autotune_grouped(aqsg_ctx ctx, int n, const aqsg_op* ops, int count, int* fu
     void* regs = nullptr;
     void* tables = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    AQSG_CUDA_TRY(cudaSetDevice(ctx->device));
+    AQSG_ON_DEVICE(ctx->device);
     int rc = AQSG_OK;
     cudaError_t e = cudaMalloc(&regs, (size_t)replicas * amps * 8);
     if (e == cudaSuccess) e = cudaMemsetAsync(regs, 0, (size_t)replicas * amps * 8, ctx->stream);

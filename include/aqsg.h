@@ -496,11 +496,13 @@ int aqsg_sample_seeded(aqsg_state st, uint64_t seed, uint64_t count, int rule,
  * GPU that loads the library until the process exits) instead of buffers
  * grown on demand.  The register must have at most AQSG_NOALLOC_MAX_QUBITS
  * qubits and count must be at most AQSG_NOALLOC_MAX_SHOTS; larger requests
- * fail with AQSG_ERR_INVALID_ARGUMENT.  The first call on a device looks up
- * the array's device address; make that first call before any stream
- * capture.  All calls on a device share the array: calls whose GPU work
- * overlaps (other threads or streams) race and must be serialised by the
- * caller. */
+ * fail with AQSG_ERR_INVALID_ARGUMENT.  aqsg_init looks up the array's
+ * device address for its device (which also loads the code that holds the
+ * array, so the array is resident before any sampling call); create the
+ * context before any stream capture.  Every call makes the context's device
+ * current and gives the caller's device back.  All calls on a device share
+ * the array: calls whose GPU work overlaps (other threads or streams) race
+ * and must be serialised by the caller. */
 #define AQSG_NOALLOC_MAX_QUBITS 30
 #define AQSG_NOALLOC_MAX_SHOTS 16384
 #define AQSG_NOALLOC_SCRATCH_BYTES \

@@ -42,6 +42,13 @@ int aqsg_debug_tile_plan(int n, int dtype, const aqsg_op* ops, int count, int fu
 int aqsg_debug_batch_image(const aqsg_circuit* circuits, int count, const int* fuse, const int* tc,
                            const aqsg_circuit* update, void* image, size_t capacity, size_t* bytes);
 
+/* Bytes the context currently holds in each of its scratch buffers, which
+ * calls grow on demand with cudaMalloc: bytes[0..5] = FP64 partial sums,
+ * sampling chunk prefixes, sampling uniforms, sampling outcomes, tile-pass
+ * op tables, probability staging; *count = 6 (at most capacity written).
+ * Tests use it to show that an entry point leaves these buffers alone. */
+int aqsg_debug_ctx_scratch(aqsg_ctx ctx, size_t* bytes, int capacity, int* count);
+
 #ifdef __cplusplus
 }
 #endif

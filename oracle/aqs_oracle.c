@@ -626,3 +626,116 @@ float ref32_qubit_probability_true(const float* sv, int n, int qubit) {
     }
     return s;
 }
+
+/* ------------------------------------------------------------------------ */
+/* change of measurement basis, QSimulator::set_basis                      */
+/* ------------------------------------------------------------------------ */
+
+/* The 2x2 change of basis the reference applies to every qubit
+ * (src/quantum.cpp:416-465), in float.  z_to_x and z_to_y are read
+ * row-major (af::array(2, 2, vals).T(), :433-434); the matrix from the
+ * current basis to Z is the identity for Z and x_to_z = inverse(z_to_x) for
+ * X and -- through the missing break at :443 -- also for Y; the target
+ * basis then multiplies z_to_y or z_to_x on the left (:454-458).  The
+ * inverse is adj/det in float (af::inverse calls LAPACK; its rounding may
+ * differ in the last place). */
+static void ref32_basis_matrix(int from, int to, cf out[4]) {
+    const float h = REF_H_F32;
+    const cf z_to_x[4] = {{h, 0.f}, {h, 0.f}, {h, 0.f}, {-h, 0.f}};
+    const cf z_to_y[4] = {{h, 0.f}, {h, 0.f}, {0.f, -h}, {0.f, h}};
+    cf m[4] = {{1.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {1.f, 0.f}};
+    switch (from) {
+        case ORC_BASIS_Z: break;
+        case ORC_BASIS_Y: /* falls through, as the reference's switch does */
+        case ORC_BASIS_X: {
+            const cf* a = z_to_x;
+            const cf det = cadd(cmul(a[0], a[3]), cmul((cf){-a[1].re, -a[1].im}, a[2]));
+            const float dd = det.re * det.re + det.im * det.im;
+            const cf inv = {det.re / dd, -det.im / dd};
+            m[0] = cmul(a[3], inv);
+            m[1] = cmul((cf){-a[1].re, -a[1].im}, inv);
+            m[2] = cmul((cf){-a[2].re, -a[2].im}, inv);
+            m[3] = cmul(a[0], inv);
+            break;
+        }
+        default: break;
+    }
+    const cf* l = to == ORC_BASIS_Y ? z_to_y : to == ORC_BASIS_X ? z_to_x : NULL;
+    if (l) {
+        const cf t[4] = {cadd(cmul(l[0], m[0]), cmul(l[1], m[2])), cadd(cmul(l[0], m[1]), cmul(l[1], m[3])),
+                         cadd(cmul(l[2], m[0]), cmul(l[3], m[2])), cadd(cmul(l[2], m[1]), cmul(l[3], m[3]))};
+        memcpy(m, t, sizeof(m));
+    }
+    memcpy(out, m, sizeof(m));
+}
+
+void ref32_basis_matrix_f(int from, int to, float* out) { ref32_basis_matrix(from, to, (cf*)out); }
+
+int ref32_set_basis(float* sv, int n, int from, int to) {
+    if (from == to) return 0;
+    if (n < 1 || n > 12) return -1;
+    cf m[4];
+    ref32_basis_matrix(from, to, m);
+    /* gen_tensor_matrix (:446-451): out = m; out = m (x) out, n - 1 times,
+     * then one dense product with the state (:461) */
+    cf* out = (cf*)malloc(sizeof(cf) * 4);
+    memcpy(out, m, sizeof(m));
+    int64_t d = 2;
+    for (int i = 0; i < n - 1; ++i) {
+        const int64_t e = 2 * d;
+        cf* k = (cf*)malloc(sizeof(cf) * (size_t)e * e);
+        for (int64_t r = 0; r < e; ++r)
+            for (int64_t c = 0; c < e; ++c)
+                k[r * e + c] = cmul(out[(r % d) * d + (c % d)], m[(r / d) * 2 + (c / d)]);
+        free(out);
+        out = k;
+        d = e;
+    }
+    dense_apply((cf*)sv, d, 1, out);
+    free(out);
+    return 0;
+}
+
+void orc_set_basis_f64(double* sv, int n, int from, int to) {
+    if (from == to) return;
+    /* the same construction in exact FP64 arithmetic: x_to_z is the inverse
+     * of z_to_x with h = 1/sqrt(2), i.e. z_to_x itself */
+    const double h = 0.70710678118654752440;
+    double m[8] = {1, 0, 0, 0, 0, 0, 1, 0};
+    if (from == ORC_BASIS_Y || from == ORC_BASIS_X) {
+        const double x[8] = {h, 0, h, 0, h, 0, -h, 0};
+        memcpy(m, x, sizeof(m));
+    }
+    if (to == ORC_BASIS_Y || to == ORC_BASIS_X) {
+        const double zy[8] = {h, 0, h, 0, 0, -h, 0, h};
+        const double zx[8] = {h, 0, h, 0, h, 0, -h, 0};
+        const double* l = to == ORC_BASIS_Y ? zy : zx;
+        double t[8];
+        for (int r = 0; r < 2; ++r)
+            for (int c = 0; c < 2; ++c) {
+                double re = 0, im = 0;
+                for (int k = 0; k < 2; ++k) {
+                    const double ar = l[2 * (2 * r + k)], ai = l[2 * (2 * r + k) + 1];
+                    const double br = m[2 * (2 * k + c)], bi = m[2 * (2 * k + c) + 1];
+                    re += ar * br - ai * bi;
+                    im += ar * bi + ai * br;
+                }
+                t[2 * (2 * r + c)] = re;
+                t[2 * (2 * r + c) + 1] = im;
+            }
+        memcpy(m, t, sizeof(m));
+    }
+    const int64_t N = (int64_t)1 << n;
+    for (int q = 0; q < n; ++q) {
+        const int64_t bm = (int64_t)1 << (n - 1 - q);
+        for (int64_t i = 0; i < N; ++i) {
+            if (i & bm) continue;
+            const double ar = sv[2 * i], ai = sv[2 * i + 1];
+            const double br = sv[2 * (i | bm)], bi = sv[2 * (i | bm) + 1];
+            sv[2 * i] = m[0] * ar - m[1] * ai + m[2] * br - m[3] * bi;
+            sv[2 * i + 1] = m[0] * ai + m[1] * ar + m[2] * bi + m[3] * br;
+            sv[2 * (i | bm)] = m[4] * ar - m[5] * ai + m[6] * br - m[7] * bi;
+            sv[2 * (i | bm) + 1] = m[4] * ai + m[5] * ar + m[6] * bi + m[7] * br;
+        }
+    }
+}

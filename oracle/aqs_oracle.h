@@ -77,6 +77,24 @@ void ref32_profile_measure_all(const float* sv, int n, uint32_t R,
 /* qubit_probability_true (quantum.cpp:372-391) in float */
 float ref32_qubit_probability_true(const float* sv, int n, int qubit);
 
+/* ---- change of measurement basis (QSimulator::set_basis) -------------- */
+
+/* Basis values of QSimulator::Basis (include/quantum.h:489-500). */
+#define ORC_BASIS_Z 0
+#define ORC_BASIS_Y 1
+#define ORC_BASIS_X 2
+/* The 2x2 matrix (row-major interleaved complex, 8 floats) set_basis
+ * applies to every qubit to go from basis `from` to `to`
+ * (quantum.cpp:416-465), with the fall-through of the missing break at
+ * :443: leaving Y uses the X-to-Z matrix. */
+void ref32_basis_matrix_f(int from, int to, float* out);
+/* set_basis as the reference computes it: the n-fold Kronecker product of
+ * that matrix as a dense 2^n x 2^n operator times the state, in float
+ * (n <= 12).  Returns -1 for other n. */
+int ref32_set_basis(float* sv, int n, int from, int to);
+/* The same change of basis (same fall-through) in FP64, one 2x2 per qubit. */
+void orc_set_basis_f64(double* sv, int n, int from, int to);
+
 #ifdef __cplusplus
 }
 #endif

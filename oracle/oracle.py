@@ -45,6 +45,9 @@ def lib() -> C.CDLL:
         L.ref32_profile_measure_all.argtypes = [P, C.c_int, C.c_uint32, P, P, P]
         L.ref32_qubit_probability_true.argtypes = [P, C.c_int, C.c_int]
         L.ref32_qubit_probability_true.restype = C.c_float
+        L.ref32_basis_matrix_f.argtypes = [C.c_int, C.c_int, P]
+        L.ref32_set_basis.argtypes = [P, C.c_int, C.c_int, C.c_int]
+        L.orc_set_basis_f64.argtypes = [P, C.c_int, C.c_int, C.c_int]
         _lib = L
     return _lib
 
@@ -153,3 +156,30 @@ def ref32_profile_measure_all(sv: np.ndarray, u) -> tuple[np.ndarray, int]:
 def ref32_qubit_probability_true(sv: np.ndarray, q: int) -> float:
     sv = np.ascontiguousarray(sv, dtype=np.complex64)
     return float(lib().ref32_qubit_probability_true(sv.ctypes.data, _n_of(sv), q))
+
+
+BASIS_Z, BASIS_Y, BASIS_X = 0, 1, 2  # QSimulator::Basis (include/quantum.h:489-500)
+
+
+def ref32_basis_matrix(frm: int, to: int) -> np.ndarray:
+    """The 2x2 change of basis set_basis applies to every qubit (float, with
+    the reference's fall-through: leaving Y uses X-to-Z)."""
+    out = np.zeros(4, dtype=np.complex64)
+    lib().ref32_basis_matrix_f(frm, to, out.ctypes.data)
+    return out.reshape(2, 2)
+
+
+def ref32_set_basis(sv: np.ndarray, frm: int, to: int) -> np.ndarray:
+    """set_basis as the reference computes it (dense Kronecker operator in
+    float), in place on a complex64 vector of at most 12 qubits."""
+    assert sv.dtype == np.complex64 and sv.flags.c_contiguous
+    rc = lib().ref32_set_basis(sv.ctypes.data, _n_of(sv), frm, to)
+    assert rc == 0, rc
+    return sv
+
+
+def set_basis_f64(sv: np.ndarray, frm: int, to: int) -> np.ndarray:
+    """The same change of basis in FP64, in place on a complex128 vector."""
+    assert sv.dtype == np.complex128 and sv.flags.c_contiguous
+    lib().orc_set_basis_f64(sv.ctypes.data, _n_of(sv), frm, to)
+    return sv

@@ -38,3 +38,11 @@ def test_host_api(tmp_path):
 @pytest.mark.gpu
 def test_reference_suite_on_gpu(tmp_path):
     run_program(compile_program("test_reference_suite", tmp_path, with_oracle=False))
+
+
+@pytest.mark.gpu
+def test_set_basis_on_gpu(tmp_path):
+    # QSimulator::set_basis for Z->X, Z->Y, X->Z, Y->Z, X->Y, Y->X against the
+    # oracle's restatement (including the fall-through of the reference's
+    # missing break), full state vector
+    run_program(compile_program("test_set_basis", tmp_path, with_oracle=True))

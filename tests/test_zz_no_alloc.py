@@ -57,3 +57,18 @@ def test_noalloc_rejects_registers_above_30_qubits(gpu_ctx):
         with pytest.raises(aq.InvalidArgument) as e:
             st.sample_noalloc([0.5])
         assert "at most 30 qubits" in e.value.msg
+
+
+def test_noalloc_grows_none_of_the_contexts_scratch():
+    # a fresh context: only the allocation-free sampler runs on it, and every
+    # scratch buffer the context grows on demand stays unallocated; the
+    # allocating sampler on the same register then does grow them
+    with aq.Context(0) as ctx:
+        with aq.State(ctx, 12, aq.C64) as st:
+            st.set_basis(5)
+            assert ctx.scratch_bytes() == [0] * 6
+            got = st.sample_noalloc(np.linspace(0.0, 1.0 - 1e-9, 257))
+            assert set(got.tolist()) == {5}
+            assert ctx.scratch_bytes() == [0] * 6
+            st.sample([0.5])
+            assert sum(ctx.scratch_bytes()) > 0
