@@ -43,7 +43,7 @@ EXPORTS = [
     "aqsg_server_wait_idle", "aqsg_server_get_stats", "aqsg_server_destroy",
     "aqsg_expect_pauli", "aqsg_autotune", "aqsg_batch_tuning", "aqsg_selftest_bounded_wait",
     "aqsg_state_download_async", "aqsg_circuit_to_text", "aqsg_circuit_from_text",
-    "aqsg_debug_tile_plan", "aqsg_debug_batch_image", "aqsg_debug_ctx_scratch",
+    "aqsg_debug_tile_plan", "aqsg_debug_batch_image", "aqsg_debug_ctx_scratch", "aqsg_batch_traffic",
 ]
 
 _lib = None
@@ -631,8 +631,9 @@ def _bind_batch(lib):
     lib.aqsg_batch_info.argtypes = [P, C.POINTER(I), C.POINTER(I), C.POINTER(I)]
     lib.aqsg_batch_free.argtypes = [P]
     lib.aqsg_batch_tuning.argtypes = [P, C.POINTER(I), C.POINTER(I)]
+    lib.aqsg_batch_traffic.argtypes = [P, C.POINTER(C.c_uint64)]
     for f in ("aqsg_batch_create", "aqsg_batch_update", "aqsg_batch_run", "aqsg_batch_info",
-              "aqsg_batch_free", "aqsg_batch_tuning"):
+              "aqsg_batch_free", "aqsg_batch_tuning", "aqsg_batch_traffic"):
         getattr(lib, f).restype = I
 
 
@@ -688,8 +689,10 @@ class Batch:
         _check(self.lib.aqsg_batch_info(self.h, C.byref(s), C.byref(l), C.byref(k)))
         f, t = (C.c_int * max(l.value, 1))(), (C.c_int * max(l.value, 1))()
         _check(self.lib.aqsg_batch_tuning(self.h, f, t))
+        hb = C.c_uint64()
+        _check(self.lib.aqsg_batch_traffic(self.h, C.byref(hb)))
         return {"small": s.value, "large": l.value, "kernels": k.value,
-                "fuse_qubits": list(f[:l.value]), "tensor_cores": list(t[:l.value])}
+                "fuse_qubits": list(f[:l.value]), "tensor_cores": list(t[:l.value]), "hbm_bytes": hb.value}
 
     def free(self) -> None:
         if self.h:
@@ -710,7 +713,8 @@ class ServerStats(C.Structure):
     """struct aqsg_server_stats."""
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
                 ("slab_bytes", C.c_uint64), ("peak_bytes", C.c_uint64),
-                ("peak_running", C.c_int32), ("lanes", C.c_int32), ("launches", C.c_uint64)]
+                ("peak_running", C.c_int32), ("lanes", C.c_int32), ("launches", C.c_uint64),
+                ("hbm_bytes", C.c_uint64)]
 
 
 def _bind_server(lib):

@@ -180,6 +180,10 @@ int run_tiled_cached(aqsg_state_s* st, const std::vector<unsigned char>& key,
 void plan_cache_free(aqsg_ctx_s* c);
 // Largest tile (log2 amplitudes) the tile kernel holds for a dtype.
 int tile_max_bits(int dtype);
+// Algorithmic HBM bytes of running a plan once: one read and one write of
+// the register per tile pass; with renorm, a run with tensor-core passes
+// also reads the register twice for its norms and rescales it once.
+uint64_t plan_hbm_bytes(const TilePlan& plan, bool renorm);
 
 // ---- init / measurement launchers (measure_kernels.cu) -------------------------
 int launch_set_basis(aqsg_state_s* st, uint64_t k);

@@ -779,6 +779,15 @@ int aqsg_batch_info(aqsg_batch b, int* small_circuits, int* large_circuits, int*
     return AQSG_OK;
 }
 
+int aqsg_batch_traffic(aqsg_batch b, uint64_t* hbm_bytes) {
+    if (!b || !hbm_bytes) return set_error(AQSG_ERR_NULL, "NULL argument");
+    uint64_t t = 0;
+    for (size_t k = 0; k < b->large.size(); ++k)
+        t += 2 * ((uint64_t)8 << b->n[b->large[k]]) + plan_hbm_bytes(b->plans[k], false);
+    *hbm_bytes = t;
+    return AQSG_OK;
+}
+
 int aqsg_batch_tuning(aqsg_batch b, int* fuse_qubits, int* tensor_cores) {
     if (!b) return set_error(AQSG_ERR_NULL, "NULL batch");
     for (size_t k = 0; k < b->large.size(); ++k) {

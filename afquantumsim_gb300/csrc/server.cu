@@ -123,6 +123,7 @@ struct aqsg_server_s {
     std::map<std::pair<double, uint64_t>, Request*> pending;  // by arrival, then ticket
     std::deque<aqsg_server_done> done;
     uint64_t next_ticket = 1, submitted = 0, completed = 0, failed = 0, unfinished = 0;
+    uint64_t hbm_bytes = 0;  // algorithmic HBM bytes of the completed requests
     bool stop = false, started = false;
     Clock::time_point t0;
     std::thread worker;
@@ -152,6 +153,11 @@ void finish(aqsg_server_s* s, Lane& L, int status) {
     }
     if (status == AQSG_OK && r->shots) std::memcpy(r->outcomes, L.pinned_out, sizeof(uint64_t) * r->shots);
     d.status = status;
+    // clear to |0...0>, the plan (with its renormalisation), and sampling:
+    // one read for the chunk sums, 2^min(n, 12) amplitudes per shot
+    const uint64_t ab = amp_bytes(r->plan.dtype), reg = ab << r->n;
+    const uint64_t traffic = reg + plan_hbm_bytes(r->plan, true) +
+                             (r->shots ? reg + (uint64_t)r->shots * (ab << (r->n < 12 ? r->n : 12)) : 0);
     s->buddy.release(r->off, r->order);
     s->used -= 1ull << r->order;
     --s->running;
@@ -161,6 +167,7 @@ void finish(aqsg_server_s* s, Lane& L, int status) {
     std::lock_guard<std::mutex> g(s->mu);
     s->done.push_back(d);
     ++s->completed;
+    if (status == AQSG_OK) s->hbm_bytes += traffic;
     if (status != AQSG_OK) ++s->failed;
     if (--s->unfinished == 0) s->cv_idle.notify_all();
 }
@@ -438,6 +445,7 @@ int aqsg_server_get_stats(aqsg_server s, aqsg_server_stats* out) {
     uint64_t l = 0;
     for (const Lane& L : s->lanes) l += L.ctx->launches;
     out->launches = l;
+    out->hbm_bytes = s->hbm_bytes;
     return AQSG_OK;
 }
 

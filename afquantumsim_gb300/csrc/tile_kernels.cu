@@ -1290,6 +1290,13 @@ static int run_encoded(aqsg_state_s* st, const TilePlan& plan, const void* dev_t
     return AQSG_OK;
 }
 
+uint64_t plan_hbm_bytes(const TilePlan& plan, bool renorm) {
+    const uint64_t reg = (uint64_t)amp_bytes(plan.dtype) << plan.n;
+    uint64_t b = 2 * reg * (uint64_t)plan.passes.size();
+    if (renorm && plan.any_tc) b += 4 * reg;
+    return b;
+}
+
 int run_tiled_cached(aqsg_state_s* st, const std::vector<unsigned char>& key,
                      const std::function<int(std::vector<LOp>*)>& lower) {
     aqsg_ctx_s* c = st->ctx;

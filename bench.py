@@ -49,8 +49,6 @@ def parse_args():
     ap.add_argument("--n", type=int, default=30, help="qubits")
     ap.add_argument("--dtype", choices=["c64", "c128"], default="c64")
     ap.add_argument("--mode", choices=["per_gate", "tiled"], default="per_gate")
-    ap.add_argument("--cpu-sample-ops", type=int, default=8,
-                    help="QFT gates in the CPU-baseline sample")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--only", choices=["fused_brickwork", "plain12", "vqe_batch", "vqe_ansatz", "serving", "qft_grid"],
                     help="run one secondary workload alone (at --n qubits where it takes a size) "
@@ -76,6 +74,48 @@ def algorithmic_bytes(n, amp_bytes):
     per = {"H": 2 * amp_bytes * N, "CPhase": 2 * amp_bytes * N // 4, "Swap": 2 * amp_bytes * N // 2}
     total = nh * per["H"] + ncp * per["CPhase"] + nsw * per["Swap"]
     return total, per, (nh, ncp, nsw)
+
+
+def gate_alg_bytes(op, n, amp_bytes):
+    """Algorithmic bytes of one gate applied on its own: the amplitudes it can
+    change, read and written.  General 1-qubit gates and RotZ: N; Z/Phase:
+    N/2; single-control gates: N/2; CZ/CPhase: N/4; Swap: N/2; CSwap, CCNot:
+    N/4; Or: 3N/4; k-qubit unitaries: N; each extra control halves it."""
+    import afquantumsim_gb300 as aq
+    k = aq.kinds
+    N = 1 << n
+    frac = {k.Z: 0.5, k.PHASE: 0.5, k.CX: 0.5, k.CY: 0.5, k.CH: 0.5, k.CRX: 0.5, k.CRY: 0.5, k.CRZ: 0.5,
+            k.CZ: 0.25, k.CPHASE: 0.25, k.SWAP: 0.5, k.CSWAP: 0.25, k.CCX: 0.25, k.OR: 0.75,
+            k.BARRIER: 0.0}.get(op.kind, 1.0)
+    return 2 * amp_bytes * N * frac / (1 << op.num_controls)
+
+
+def qft_cpu_sample(n):
+    """Gates of the QFT with swaps in the proportions of the whole circuit:
+    every 15th H, CPhase and Swap (2 H, 29 CPhase, 1 Swap at 30 qubits)."""
+    import afquantumsim_gb300 as aq
+    ops = qft_ops(n)
+    out = []
+    for kind in (aq.kinds.H, aq.kinds.CPHASE, aq.kinds.SWAP):
+        same = [o for o in ops if o.kind == kind]
+        out += same[7::15] or same[:1]
+    return out
+
+
+def metric_name(n, dtype):
+    return f"QFT gate-apps/s at {n}q ({dtype}, one gate per pass) + HBM GB/s"
+
+
+def workload_config(n, dtype, world):
+    """The workload both arms run (the same dict in both JSON lines)."""
+    _, _, counts = algorithmic_bytes(n, 8)
+    amp_b = 8 if dtype == "c64" else 16
+    return {"workload": f"qft{n}+swaps", "qubits": n, "gates": sum(counts),
+            "gate_mix": {"H": counts[0], "CPhase": counts[1], "Swap": counts[2]},
+            "input": "seeded i.i.d. standard-normal complex amplitudes, normalised",
+            "parallelism": f"replicas{world}",
+            "l2": ("register (2^%d x %d B) larger than L2; no flush" % (n, amp_b)
+                   if (amp_b << n) > 129e6 else "register fits in L2 (2^%d x %d B)" % (n, amp_b))}
 
 
 def measured_peaks():
@@ -154,13 +194,13 @@ class ClockSampler:
 
 # ---- CPU baseline -----------------------------------------------------------------
 
-def cpu_baseline(n, host_sv, sample_ops, dtype):
+def cpu_baseline(n, host_sv, ops, dtype, what):
     """Per-gate CPU restatement of the reference's simulate (oracle port) on
-    the first `sample_ops` gates of the workload, all host threads."""
+    `ops` (a sample of the workload's gates, described by `what`), all host
+    threads."""
     from oracle import oracle
     threads = len(os.sched_getaffinity(0))
     oracle.set_threads(threads)
-    ops = qft_ops(n)[:sample_ops]
     t0 = time.perf_counter()
     if dtype == "c64":
         oracle.apply_f32(host_sv, ops)
@@ -171,9 +211,8 @@ def cpu_baseline(n, host_sv, sample_ops, dtype):
     for o in ops:
         kinds[o.kind] = kinds.get(o.kind, 0) + 1
     return {"value": len(ops) / dt, "unit": "gate-apps/s", "cores": threads, "kind": "port",
-            "sample": f"first {len(ops)} gates of the {n}-qubit QFT ({kinds.get(4, 0)} H, "
-                      f"{kinds.get(14, 0)} CPhase) on the full 2^{n} register, {dtype}, "
-                      f"{dt:.1f} s", "seconds": dt}
+            "sample": f"{what}: {kinds.get(4, 0)} H, {kinds.get(14, 0)} CPhase, {kinds.get(6, 0)} Swap "
+                      f"on the full 2^{n} register, {dtype}, {dt:.1f} s", "seconds": dt}
 
 
 def reference_algorithm_small(n=12):
@@ -219,17 +258,38 @@ def bench_fused_brickwork(ctx, st, stream, n, depth):
     def reset():
         st.set_basis(0)
 
+    def launches_of(fn):
+        l0 = ctx.launch_count()
+        fn()
+        return ctx.launch_count() - l0
+
     reset()
     st.apply(ops, aq.EXEC_PER_GATE)
     res["per_gate_ms"] = round(_time_ms(stream, lambda: st.apply(ops, aq.EXEC_PER_GATE), 1), 2)
-    st.apply(ops, aq.EXEC_TILED)
+    tiled_passes = launches_of(lambda: st.apply(ops, aq.EXEC_TILED))
     res["tiled_ms"] = round(_time_ms(stream, lambda: st.apply(ops, aq.EXEC_TILED), 2), 2)
     ctx.set_tensor_cores(False)
-    prog.run(st, aq.EXEC_TILED)
+    fused_passes = launches_of(lambda: prog.run(st, aq.EXEC_TILED))
     res["fused_cuda_core_ms"] = round(_time_ms(stream, lambda: prog.run(st, aq.EXEC_TILED), 2), 2)
     ctx.set_tensor_cores(True)
-    prog.run(st, aq.EXEC_TILED)
+    tc_launches = launches_of(lambda: prog.run(st, aq.EXEC_TILED))
     res["fused_tensor_core_ms"] = round(_time_ms(stream, lambda: prog.run(st, aq.EXEC_TILED), 3), 2)
+    # HBM roofline of each mode.  One gate per pass: the algorithmic bytes of
+    # each gate (the amplitudes it can change); tile passes: one read and one
+    # write of the register per pass (2 x 8 B x 2^n), so no mode can exceed
+    # 1.0; the tensor-core run also reads the register twice for its FP64
+    # norms and rescales it once (4 x 8 B x 2^n, its launches = passes + 5).
+    peak, peak_src = measured_peaks()
+    reg = 8 * N
+    per_gate_bytes = sum(gate_alg_bytes(o, n, 8) for o in ops)
+    tc_passes = tc_launches - 5
+    modes = {"per_gate": (per_gate_bytes, res["per_gate_ms"], len(ops)),
+             "tiled": (2 * reg * tiled_passes, res["tiled_ms"], tiled_passes),
+             "fused_cuda_core": (2 * reg * fused_passes, res["fused_cuda_core_ms"], fused_passes),
+             "fused_tensor_core": (2 * reg * tc_passes + 4 * reg, res["fused_tensor_core_ms"], tc_passes)}
+    res["hbm"] = {m: {"passes": p, "bytes": b, "achieved_gbs": round(b / (ms / 1e3) / 1e9, 1), "peak_gbs": peak,
+                      "frac": round(b / (ms / 1e3) / 1e9 / peak, 4), "peak_source": peak_src}
+                  for m, (b, ms, p) in modes.items()}
     res["speedup_fused_vs_tiled"] = round(res["tiled_ms"] / res["fused_tensor_core_ms"], 2)
     # tensor-pipe work of the fused run: a k-qubit unitary on the tensor
     # cores is three bf16 products of (2^n / 2^k) x 2^(k+1) x 2^(k+1) per
@@ -435,8 +495,13 @@ def bench_vqe_batch(ctx, count=4096, seed=5):
     cpu_sweep_est = cpu_s * work / cpu_work
     from collections import Counter
     tuned = Counter(f"fuse{f}{'_tc' if t else ''}" for f, t in zip(info["fuse_qubits"], info["tensor_cores"]))
+    peak, peak_src = measured_peaks()
+    hbm = {"bytes_per_sweep": info["hbm_bytes"], "achieved_gbs": round(info["hbm_bytes"] / sweep_s / 1e9, 1),
+           "peak_gbs": peak, "frac": round(info["hbm_bytes"] / sweep_s / 1e9 / peak, 4), "peak_source": peak_src,
+           "note": "registers of > 14 qubits: clear, one read + one write per tile pass, expectation read; "
+                   "registers of <= 14 qubits stay in shared memory"}
     return {"workload": f"vqe_sweep{count}", "gates": gates, "small_circuits": info["small"],
-            "large_circuits": info["large"], "kernels_per_replay": info["kernels"],
+            "large_circuits": info["large"], "kernels_per_replay": info["kernels"], "hbm": hbm,
             "large_circuit_tuning": dict(tuned),
             "create_s": round(create_s, 3), "sweep_ms": round(1e3 * sweep_s, 3),
             "circuits_per_s": round(count / sweep_s, 1), "gate_apps_per_s": round(gates / sweep_s, 1),
@@ -494,7 +559,10 @@ def bench_serving(ctx, count=160, seed=6, shots=1024, fuse=5, lanes=8, budget_gi
         assert len(done) == count and all(d["status"] == 0 for d in done)
         lat = np.array([d["done_s"] - d["arrival_s"] for d in done])
         span = max(d["done_s"] for d in done) - min(d["arrival_s"] for d in done)
-        return {"circuits_per_s": round(count / span, 2), "gate_apps_per_s": round(gates / span, 1),
+        peak, peak_src = measured_peaks()
+        hbm = {"bytes": stats["hbm_bytes"], "achieved_gbs": round(stats["hbm_bytes"] / span / 1e9, 1),
+               "peak_gbs": peak, "frac": round(stats["hbm_bytes"] / span / 1e9 / peak, 4), "peak_source": peak_src}
+        return {"hbm": hbm, "circuits_per_s": round(count / span, 2), "gate_apps_per_s": round(gates / span, 1),
                 "makespan_s": round(span, 3), "p50_latency_ms": round(1e3 * float(np.percentile(lat, 50)), 2),
                 "p99_latency_ms": round(1e3 * float(np.percentile(lat, 99)), 2),
                 "peak_running": stats["peak_running"], "peak_slab_gib": round(stats["peak_bytes"] / 2**30, 2),
@@ -680,6 +748,19 @@ def run_ours(args, rank, world, local_rank):
            "pipeline": "two registers on two streams, gates of consecutive steps ordered (aqsg_ctx_after); "
                        "each step uploads its input and reads its result under the other register's gates"}
 
+    # accuracy of one step against FP64: the circuit applied once to the
+    # seeded input, against the same gates applied to it in complex128 with
+    # PyTorch's own operations (tests/fp64_torch.py, which the tests pin to
+    # the C oracle); both compared on the device
+    from tests import fp64_torch
+    st.upload_ptr(host_in.data_ptr())
+    st.apply(ops, mode)
+    st.download_ptr(host_out.data_ptr())
+    want = fp64_torch.apply_ops(host_in.to(dev).to(torch.complex128), n, qft_ops(n))
+    accuracy = fp64_torch.errors(host_out.to(dev), want)
+    del want
+    torch.cuda.empty_cache()
+
     extras = {}
     if not args.no_extras and rank == 0:
         # the same circuit in shared-memory tiled mode, for comparison
@@ -702,7 +783,8 @@ def run_ours(args, rank, world, local_rank):
     cpu = None
     if rank == 0:
         host_np = host_out.numpy()  # scratch register for the CPU sample
-        cpu = cpu_baseline(n, host_np, args.cpu_sample_ops, args.dtype)
+        cpu = cpu_baseline(n, host_np, qft_cpu_sample(n), args.dtype,
+                           "every 15th gate of each kind of the same circuit (its gate mix)")
         if not args.no_extras:
             extras["reference_algorithm_qft12"] = reference_algorithm_small(12)
 
@@ -711,7 +793,7 @@ def run_ours(args, rank, world, local_rank):
     if rank != 0:
         return None
     return {
-        "metric": f"QFT gate-apps/s at {n}q ({args.dtype}, one gate per pass) + HBM GB/s",
+        "metric": metric_name(n, args.dtype),
         "value": round(value, 3),
         "unit": "gate-apps/s",
         "n_gpus": world,
@@ -723,10 +805,13 @@ def run_ours(args, rank, world, local_rank):
         "vs_baseline": None,
         "dtype": args.dtype,
         "data": "synthetic (seeded standard-normal complex amplitudes)",
-        "config": {"workload": f"qft{n}+swaps", "qubits": n, "gates": gates,
-                   "gate_mix": {"H": counts[0], "CPhase": counts[1], "Swap": counts[2]},
-                   "exec_mode": args.mode, "parallelism": f"replicas{world}",
-                   "l2": "register (2^%d x %d B) larger than L2; no flush" % (n, amp_b)},
+        "config": workload_config(n, args.dtype, world),
+        "exec_mode": args.mode,
+        "max_abs_err_vs_fp64": accuracy["max_abs_err"],
+        "l2_err_vs_fp64": accuracy["l2_err"],
+        "one_minus_fidelity": accuracy["one_minus_fidelity"],
+        "accuracy_reference": "one step on the seeded input against the same gates in complex128 "
+                              "(PyTorch operations, pinned to the C oracle by the tests)",
         "hbm_gbs": round(hbm_gbs, 1),
         "hbm_frac": round(hbm_gbs / world / measured_peaks()[0], 4),
         "algorithmic_bytes_per_step": total_bytes,
@@ -742,8 +827,8 @@ def run_ours(args, rank, world, local_rank):
 
 # Mean DRAM bytes (read + write) per controlled-phase launch over the 325
 # CPhase launches of one 26-qubit complex64 QFT, from an ncu capture of
-# dram__bytes_read.sum + dram__bytes_write.sum (profiles/k_diag1_qft26_c64_traffic.md).
-# Traffic grows with the register (2^n), so other sizes scale it.
+# dram__bytes_read.sum + dram__bytes_write.sum.  Traffic grows with the
+# register (2^n), so other sizes scale it.
 CPHASE_TRAFFIC_C64_26Q = 277.4e6
 
 
@@ -754,8 +839,13 @@ def traffic_per_launch(n, dtype):
 
 
 def run_reference(args):
-    """CPU implementation of the path (oracle port, all host threads) on the
-    same workload: a bounded sample of its gates per step."""
+    """CPU implementation of the path (the per-gate oracle port, all host
+    threads) on the same workload: the same seeded 2^n register, and step s
+    times the s-th contiguous slice of the circuit's gates, so that the K
+    steps together run the whole circuit once, in order (each step holds
+    ceil(gates / K) gates; steps past the end of the circuit start it
+    again).  A warm-up step runs one gate."""
+    import afquantumsim_gb300 as aq
     n = args.n
     N = 1 << n
     dt_np = np.complex64 if args.dtype == "c64" else np.complex128
@@ -766,19 +856,29 @@ def run_reference(args):
         m = min(chunk, N - i)
         sv[i:i + m] = (rng.standard_normal(m) + 1j * rng.standard_normal(m)).astype(dt_np)
     sv /= np.sqrt(np.vdot(sv, sv).real)
-    res = []
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        cpu_baseline(n, sv, 1, args.dtype)
-    for _ in range(args.steps):
-        res.append(cpu_baseline(n, sv, args.cpu_sample_ops, args.dtype))
-    tot_ops = sum(args.cpu_sample_ops for _ in res)
+    ops = qft_ops(n)
+    gates = len(ops)
+    for _ in range(args.warmup):
+        cpu_baseline(n, sv, ops[:1], args.dtype, "warm-up")
+    per = -(-gates // max(args.steps, 1))
+    res, timed = [], 0
+    for s_ in range(args.steps):
+        lo = (s_ * per) % gates
+        sl = ops[lo:lo + per]
+        res.append(cpu_baseline(n, sv, sl, args.dtype, f"gates {lo}..{lo + len(sl) - 1}"))
+        timed += len(sl)
     tot_s = sum(r["seconds"] for r in res)
-    value = tot_ops / tot_s
-    cb = {k: v for k, v in res[0].items() if k != "seconds"}
-    cb["value"] = value
+    value = timed / tot_s
+    kinds = {}
+    for o in ops[:timed] if timed <= gates else ops:
+        kinds[o.kind] = kinds.get(o.kind, 0) + 1
+    sample = (f"the whole {gates}-gate circuit once in order, {per} gates per step over {args.steps} steps "
+              f"({timed} gates: {kinds.get(aq.kinds.H, 0)} H, {kinds.get(aq.kinds.CPHASE, 0)} CPhase, "
+              f"{kinds.get(aq.kinds.SWAP, 0)} Swap), {args.dtype}, {tot_s:.1f} s")
+    cb = {"value": value, "unit": "gate-apps/s", "cores": res[0]["cores"], "kind": "port", "sample": sample}
     return {
         "impl": "reference",
-        "metric": f"QFT gate-apps/s at {n}q ({args.dtype}, one gate per pass) + HBM GB/s",
+        "metric": metric_name(n, args.dtype),
         "value": round(value, 4),
         "unit": "gate-apps/s",
         "n_gpus": args.gpus,
@@ -790,8 +890,9 @@ def run_reference(args):
         "vs_baseline": None,
         "dtype": args.dtype,
         "data": "synthetic (seeded standard-normal complex amplitudes)",
-        "config": {"workload": f"qft{n}+swaps", "qubits": n, "exec_mode": "cpu per-gate",
-                   "sample": cb["sample"]},
+        "config": workload_config(n, args.dtype, args.gpus),
+        "exec_mode": "cpu per-gate (oracle port)",
+        "sample": sample,
         "cpu_baseline": cb,
         "e2e": {"value": round(value, 4), "unit": "gate-apps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},

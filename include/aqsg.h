@@ -365,6 +365,11 @@ int aqsg_batch_run(aqsg_batch b, double* z, double* zz);
 
 /* Circuits run in shared memory / as tile passes, kernels per replay. */
 int aqsg_batch_info(aqsg_batch b, int* small_circuits, int* large_circuits, int* kernels);
+/* Algorithmic HBM bytes of one aqsg_batch_run: for each register of more
+ * than 14 qubits, its clear to |0...0> (one write), one read and one write
+ * per tile pass and the read of the expectation sums; registers of at most
+ * 14 qubits live in shared memory and move no state through HBM. */
+int aqsg_batch_traffic(aqsg_batch b, uint64_t* hbm_bytes);
 
 /* Fusion width (0 = none) and tensor-core use the autotuner chose for each
  * large register, in circuit order (arrays of large_circuits entries, see
@@ -411,6 +416,10 @@ typedef struct aqsg_server_stats {
     int32_t peak_running;      /* most requests in flight at once */
     int32_t lanes;
     uint64_t launches;         /* kernels launched by all lanes */
+    uint64_t hbm_bytes;        /* algorithmic HBM bytes of the completed requests:
+                                  register set to |0...0>, one read + one write per
+                                  tile pass, the renormalisation's reads and rescale
+                                  of tensor-core runs, the sampling reads */
 } aqsg_server_stats;
 
 /* Create a server on `device` for registers of dtype and at most max_qubits
