@@ -64,9 +64,10 @@ int main(int argc, char** argv) {
         worst64 = std::max(worst64, d64);
     }
     // Y -> Z is not the inverse of Z -> Y (the fall-through): the round trip
-    // through Y changes the state, a round trip through X does not
+    // through Y changes |0...0> (each qubit ends as (1 - i, 1 + i) / 2), a
+    // round trip through X does not
     for (B via : {B::Y, B::X}) {
-        QSimulator sim(n, QState::plus());
+        QSimulator sim(n, QState::zero());
         const auto before = sim.statevector();
         sim.set_basis(via);
         sim.set_basis(B::Z);
