@@ -75,6 +75,88 @@ __device__ __forceinline__ void norm2_ff(float x, float y, float& h, float& l) {
     l = __fadd_rn(__fadd_rn(ex, ey), e);
 }
 
+// ---- double-float arithmetic for complex128 gates ----------------------------
+//
+// GB300 executes FP64 at a small fraction of its FP32 rate, so a complex128
+// gate done in FP64 (4-8 FP64 operations per amplitude) is bound by the FP64
+// pipe, not by HBM.  The gate kernels instead split each double into two
+// floats with integer operations (df_split), form the products and sums as
+// unevaluated float pairs on the FP32 pipe (Dekker's TwoProd through an FMA,
+// Knuth's TwoSum: DFAcc), and rebuild each output double with one FP64 add
+// of the pair's two floats (df_join), whose conversion to double is again
+// done with integer operations.  Each output carries about 46 significant
+// bits (the split keeps 24 + 23 of the 53 bits of an input).
+//
+// The split covers inputs of magnitude 2^-80 .. 2^117 (and exact zeros);
+// anything else (tiny, huge, inf, nan) sets `wide`, and the kernel computes
+// that element's gate in plain FP64 instead.
+
+// x = hi + lo (up to the dropped bits): hi = x truncated to its leading 24
+// significant bits, lo = the next 23 bits.  Both carry x's sign.
+__device__ __forceinline__ float2 df_split(double x, bool& wide) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const uint32_t bh = (uint32_t)(b >> 32), bl = (uint32_t)b;
+    const uint32_t e = (bh >> 20) & 0x7FFu;  // biased exponent; 0: zero or below 2^-1022
+    const uint32_t sign = bh & 0x80000000u;
+    wide |= e != 0u && (e < 943u || e > 1140u);
+    const uint32_t ok = (e >= 943u && e <= 1140u) ? 0xFFFFFFFFu : 0u;
+    const uint32_t m23 = ((bh & 0xFFFFFu) << 3) | (bl >> 29);
+    const float hi = __uint_as_float((sign | ((e - 896u) << 23) | m23) & ok);
+    // the remaining 29 mantissa bits, top 23 of them as an exact float
+    // integer, scaled by 2^(e - 1069)
+    const float rf = __fsub_rn(__uint_as_float(0x4B000000u | ((bl & 0x1FFFFFFFu) >> 6)), 8388608.0f);
+    const float scale = __uint_as_float(((e - 942u) << 23) & ok);
+    const float lo = __uint_as_float(__float_as_uint(__fmul_rn(rf, scale)) | (sign & ok));
+    return make_float2(hi, lo);
+}
+
+// A float as a double, by moving its fields (a float below 2^-126 becomes a
+// signed zero; the fast path produces no inf or nan).
+__device__ __forceinline__ double df_f2d(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xFFu;
+    const uint32_t s = u & 0x80000000u;
+    const uint32_t hw = e ? (s | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3)) : s;
+    const uint32_t lw = e ? (u << 29) : 0u;
+    return __hiloint2double((int)hw, (int)lw);
+}
+
+// An unevaluated float sum s + low.
+struct DFAcc {
+    float s, low;
+};
+
+// a * c for a = ah + al and a coefficient c = ch + cl: the exact product of
+// the high parts (TwoProd) plus the cross terms.
+__device__ __forceinline__ DFAcc df_mul(float2 a, float2 c) {
+    const float p = __fmul_rn(a.x, c.x);
+    const float e = __fmaf_rn(a.x, c.x, -p);
+    const float t = __fmaf_rn(a.x, c.y, __fmul_rn(a.y, c.x));
+    return DFAcc{p, __fadd_rn(e, t)};
+}
+
+// acc += a * c, the high parts added with TwoSum.
+__device__ __forceinline__ void df_madd(DFAcc& acc, float2 a, float2 c) {
+    const float p = __fmul_rn(a.x, c.x);
+    const float e = __fmaf_rn(a.x, c.x, -p);
+    const float t = __fmaf_rn(a.x, c.y, __fmul_rn(a.y, c.x));
+    const float s = __fadd_rn(acc.s, p);
+    const float bp = __fsub_rn(s, acc.s);
+    const float err = __fadd_rn(__fsub_rn(acc.s, __fsub_rn(s, bp)), __fsub_rn(p, bp));
+    acc.s = s;
+    acc.low = __fadd_rn(acc.low, __fadd_rn(err, __fadd_rn(e, t)));
+}
+
+// The double nearest to acc.s + acc.low: one FP64 add.
+__device__ __forceinline__ double df_join(const DFAcc& acc) { return __dadd_rn(df_f2d(acc.s), df_f2d(acc.low)); }
+
+__device__ __forceinline__ float2 df_neg(float2 c) { return make_float2(-c.x, -c.y); }
+
+// A complex128 coefficient as double-float parts: (re hi, re lo, im hi, im lo).
+struct DFCoef {
+    float2 re, im;
+};
+
 // Insert NF fixed bits (ascending positions) into a free index, then OR in
 // their values.  NF == 0 is the identity.
 template <int NF>

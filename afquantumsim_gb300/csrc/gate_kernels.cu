@@ -12,6 +12,7 @@
 // (src/quantum.cpp:540-1950): the operators there are 2^n x 2^n (dense
 // Kronecker or CSR); here a gate is a handful of coefficients.
 #include <algorithm>
+#include <cmath>
 
 #include "aqsg_internal.h"
 #include "common.cuh"
@@ -28,6 +29,8 @@ enum PairOp { P_MAT2 = 0, P_DIAG2 = 1, P_PERMX = 2, P_PERMOR = 3, P_MAT2R = 4 };
 template <typename R>
 struct M2 {
     typename Cx<R>::T m[4];
+    DFCoef df[4];  // complex128: the coefficients as double-float parts
+    int df_on;     // all coefficients of modulus <= 4: the double-float path may run
 };
 
 // ---- unit load / store: VEC consecutive amplitudes starting at index i -----
@@ -95,6 +98,56 @@ k_pair(typename Cx<R>::T* __restrict__ sv, FX fx, uint64_t tmask, uint64_t amask
 #pragma unroll
         for (int v = 0; v < VEC; ++v) {
             const T a = lo[it].a[v], b = hi[it].a[v];
+            if constexpr (sizeof(R) == 8 && (OP == P_MAT2 || OP == P_MAT2R || OP == P_DIAG2)) {
+                // complex128 on the FP32 pipe (double-float), FP64 only for
+                // inputs outside the split's range
+                bool wide = !m.df_on;
+                const float2 ar = df_split(a.x, wide), ai = df_split(a.y, wide);
+                const float2 br = df_split(b.x, wide), bi = df_split(b.y, wide);
+                if (!wide) {
+                    T r0, r1;
+                    if constexpr (OP == P_MAT2R) {
+                        DFAcc x0 = df_mul(ar, m.df[0].re), y0 = df_mul(ai, m.df[0].re);
+                        DFAcc x1 = df_mul(ar, m.df[2].re), y1 = df_mul(ai, m.df[2].re);
+                        df_madd(x0, br, m.df[1].re);
+                        df_madd(y0, bi, m.df[1].re);
+                        df_madd(x1, br, m.df[3].re);
+                        df_madd(y1, bi, m.df[3].re);
+                        r0.x = df_join(x0); r0.y = df_join(y0);
+                        r1.x = df_join(x1); r1.y = df_join(y1);
+                    } else if constexpr (OP == P_MAT2) {
+                        // (m0 a + m1 b) and (m2 a + m3 b), complex
+                        DFAcc x0 = df_mul(ar, m.df[0].re), y0 = df_mul(ai, m.df[0].re);
+                        df_madd(x0, ai, df_neg(m.df[0].im));
+                        df_madd(y0, ar, m.df[0].im);
+                        df_madd(x0, br, m.df[1].re);
+                        df_madd(y0, bi, m.df[1].re);
+                        df_madd(x0, bi, df_neg(m.df[1].im));
+                        df_madd(y0, br, m.df[1].im);
+                        DFAcc x1 = df_mul(ar, m.df[2].re), y1 = df_mul(ai, m.df[2].re);
+                        df_madd(x1, ai, df_neg(m.df[2].im));
+                        df_madd(y1, ar, m.df[2].im);
+                        df_madd(x1, br, m.df[3].re);
+                        df_madd(y1, bi, m.df[3].re);
+                        df_madd(x1, bi, df_neg(m.df[3].im));
+                        df_madd(y1, br, m.df[3].im);
+                        r0.x = df_join(x0); r0.y = df_join(y0);
+                        r1.x = df_join(x1); r1.y = df_join(y1);
+                    } else {  // P_DIAG2: m0 on t = 0, m1 on t = 1
+                        DFAcc x0 = df_mul(ar, m.df[0].re), y0 = df_mul(ai, m.df[0].re);
+                        df_madd(x0, ai, df_neg(m.df[0].im));
+                        df_madd(y0, ar, m.df[0].im);
+                        DFAcc x1 = df_mul(br, m.df[1].re), y1 = df_mul(bi, m.df[1].re);
+                        df_madd(x1, bi, df_neg(m.df[1].im));
+                        df_madd(y1, br, m.df[1].im);
+                        r0.x = df_join(x0); r0.y = df_join(y0);
+                        r1.x = df_join(x1); r1.y = df_join(y1);
+                    }
+                    lo[it].a[v] = r0;
+                    hi[it].a[v] = r1;
+                    continue;
+                }
+            }
             if constexpr (OP == P_MAT2) {
                 lo[it].a[v] = cmul2(m.m[0], a, m.m[1], b);
                 hi[it].a[v] = cmul2(m.m[2], a, m.m[3], b);
@@ -135,7 +188,7 @@ k_pair(typename Cx<R>::T* __restrict__ sv, FX fx, uint64_t tmask, uint64_t amask
 // ---- DIAG1: multiply the amplitudes of one index pattern by a phase --------
 template <typename R, int VEC, typename FX>
 __global__ void __launch_bounds__(kThreads)
-k_diag1(typename Cx<R>::T* __restrict__ sv, FX fx, uint64_t units, typename Cx<R>::T ph) {
+k_diag1(typename Cx<R>::T* __restrict__ sv, FX fx, uint64_t units, typename Cx<R>::T ph, DFCoef phd) {
     constexpr int IT = 4;
     const uint64_t first = (uint64_t)blockIdx.x * (kThreads * IT) + threadIdx.x;
     Unit<R, VEC> a[IT];
@@ -154,7 +207,21 @@ k_diag1(typename Cx<R>::T* __restrict__ sv, FX fx, uint64_t units, typename Cx<R
     for (int it = 0; it < IT; ++it) {
         if (!ok[it]) continue;
 #pragma unroll
-        for (int v = 0; v < VEC; ++v) a[it].a[v] = cmul(ph, a[it].a[v]);
+        for (int v = 0; v < VEC; ++v) {
+            if constexpr (sizeof(R) == 8) {  // complex128: double-float on the FP32 pipe
+                bool wide = false;
+                const float2 xr = df_split(a[it].a[v].x, wide), xi = df_split(a[it].a[v].y, wide);
+                if (!wide) {
+                    DFAcc re = df_mul(xr, phd.re), im = df_mul(xi, phd.re);
+                    df_madd(re, xi, df_neg(phd.im));
+                    df_madd(im, xr, phd.im);
+                    a[it].a[v].x = df_join(re);
+                    a[it].a[v].y = df_join(im);
+                    continue;
+                }
+            }
+            a[it].a[v] = cmul(ph, a[it].a[v]);
+        }
         store_unit<R, VEC>(sv, idx[it], a[it]);
     }
 }
@@ -276,6 +343,19 @@ static typename Cx<R>::T cval(double re, double im) {
     return t;
 }
 
+// v = hi + lo as floats (hi rounded to nearest, lo the rounded remainder)
+static float2 host_df(double v) {
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
+}
+
+static DFCoef df_coef(double re, double im) {
+    DFCoef c;
+    c.re = host_df(re);
+    c.im = host_df(im);
+    return c;
+}
+
 template <typename R, int VEC, bool PACKED, int OP>
 static void launch_pair_v(aqsg_state_s* st, const FixedBits& f, uint64_t tmask, uint64_t amask,
                           uint64_t units, const M2<R>& m) {
@@ -297,7 +377,13 @@ static int launch_typed(aqsg_state_s* st, const LOp& op) {
             const uint64_t tmask = 1ull << op.t0;
             FixedBits f = make_fixed(op.cmask | tmask, op.cval);
             M2<R> m;
-            for (int e = 0; e < 4; ++e) m.m[e] = cval<R>(op.m[2 * e], op.m[2 * e + 1]);
+            m.df_on = 1;
+            for (int e = 0; e < 4; ++e) {
+                m.m[e] = cval<R>(op.m[2 * e], op.m[2 * e + 1]);
+                m.df[e] = df_coef(op.m[2 * e], op.m[2 * e + 1]);
+                // user unitaries may hold any values: large ones stay in FP64
+                if (!(std::fabs(op.m[2 * e]) <= 4.0 && std::fabs(op.m[2 * e + 1]) <= 4.0)) m.df_on = 0;
+            }
             const bool real = op.m[1] == 0.0 && op.m[3] == 0.0 && op.m[5] == 0.0 && op.m[7] == 0.0;
             const int OPK = op.cls == L_MAT2 ? (real ? P_MAT2R : P_MAT2) : op.cls == L_DIAG2 ? P_DIAG2
                           : op.cls == L_PERM_X ? P_PERMX : P_PERMOR;
@@ -328,19 +414,20 @@ static int launch_typed(aqsg_state_s* st, const LOp& op) {
             FixedBits f = make_fixed(op.cmask, op.cval);
             uint64_t units = N >> f.nf;
             const T ph = cval<R>(op.m[0], op.m[1]);
+            const DFCoef phd = df_coef(op.m[0], op.m[1]);
             const bool vec2 = is_f && (f.mask & 1ull) == 0;
             if (vec2) {
                 units >>= 1;
                 const unsigned grid = grid_for(units, kThreads * 4);
                 with_fix(f, [&](auto fx) {
                     k_diag1<R, (sizeof(R) == 4 ? 2 : 1), decltype(fx)>
-                        <<<grid, kThreads, 0, st->ctx->stream>>>((T*)st->d, fx, units, ph);
+                        <<<grid, kThreads, 0, st->ctx->stream>>>((T*)st->d, fx, units, ph, phd);
                 });
             } else {
                 const unsigned grid = grid_for(units, kThreads * 4);
                 with_fix(f, [&](auto fx) {
                     k_diag1<R, 1, decltype(fx)><<<grid, kThreads, 0, st->ctx->stream>>>(
-                        (T*)st->d, fx, units, ph);
+                        (T*)st->d, fx, units, ph, phd);
                 });
             }
             break;

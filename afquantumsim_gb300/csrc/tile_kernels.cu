@@ -206,8 +206,9 @@ __device__ __forceinline__ bool group_any(bool v) {
 // Warp 16 is the producer: it copies tiles in 16-byte cp.async chunks into
 // three shared-memory buffers (full[b] completes when all 32 lanes' chunks
 // have landed; many small requests stay in flight without the per-request
-// cost of bulk copies) and writes them back with 128-bit stores once the
-// compute warps have released them (done[b]).  The 16 compute warps form
+// cost of bulk copies), and loads the next tile into a buffer as soon as the
+// compute group that ran its tile has written it back with 128-bit stores
+// and released it (done[b]).  The 16 compute warps form
 // GROUPS groups; group g runs the pass's ops on the CTA's tiles g, g + GROUPS,
 // ... with its own named barrier, A operand, tensor-memory columns and MMA
 // barrier, so one group's operand gathers and write-backs overlap the other
@@ -240,6 +241,7 @@ struct TcTiles {
 // G + GROUPS, ...
 template <int NT, int GROUPS, bool MULTI, bool MATK, class LAY>
 __device__ __forceinline__ void tc_compute_group(unsigned char* smem_raw, const TileGeom& g, const TcTiles& tl,
+                                                 float2* __restrict__ sv0, uint64_t reg_stride,
                                                  const unsigned char* __restrict__ dev0, uint64_t dev_stride,
                                                  uint32_t op_first, int nops, uint64_t pool_off, const TileOp* sops,
                                                  bool ops_in_smem, uint64_t* full, uint64_t* done,
@@ -277,6 +279,20 @@ __device__ __forceinline__ void tc_compute_group(unsigned char* smem_raw, const 
         const TileOp* optab = ops_in_smem ? sops : reinterpret_cast<const TileOp*>(dev) + op_first;
         tile_run_ops<float, (1 << M) / NT, true, LAY, SYNC, MATK, false, NT / 32>(s, 1u << M, NT, base, optab, nops,
                                                                                 dev + pool_off, &tcs, &tph);
+        // the group writes its tile back itself (16-byte chunks of the rows,
+        // 2048 / NT per thread), so the buffer is free as soon as the last
+        // chunk has been read and the producer only issues loads
+        {
+            const uint64_t* rowoff = reinterpret_cast<const uint64_t*>(smem_raw + TcStreamSmem::kRowOff);
+            float2* dstg = sv0 + (uint64_t)m * reg_stride + base;
+            const unsigned char* src = smem_raw + buf * kBufBytes;
+#pragma unroll 4
+            for (uint32_t q = threadIdx.x & (NT - 1u); q < kRows * 16u; q += NT) {
+                const uint32_t r = q >> 4, c = q & 15u;
+                const uint4 v = *reinterpret_cast<const uint4*>(src + r * TcStreamSmem::kRowStride + c * 16u);
+                __stcs(reinterpret_cast<uint4*>(dstg + rowoff[r]) + c, v);
+            }
+        }
         fence_async_smem();
         __syncwarp();
         if (lane == 0) mbar_arrive(done + buf);
@@ -400,18 +416,11 @@ k_stream_tc(float2* __restrict__ sv0, const TileGeom g, const unsigned char* __r
                 if (lane == 0) atomicExch(err, 1);
                 break;
             }
-            // tiles are released in order, so every tile up to i is done: at
-            // a change of register its blob and op table may be replaced
+            // tiles are released in order (the compute groups have written
+            // them back), so every tile up to i is done: at a change of
+            // register its blob and op table may be replaced
             if (MULTI && lane == 0 && i + 1 < count && member_of(i + 1) != member_of(i)) load_blob(member_of(i + 1));
-            float2* dstg = sv_of(member_of(i)) + tile_base(local_of(i));
-            const unsigned char* src = smem_raw + buf * kBufBytes;
-#pragma unroll 8
-            for (uint32_t q = lane; q < kRows * 16u; q += 32u) {
-                const uint32_t r = q >> 4, c = q & 15u;
-                const uint4 v = *reinterpret_cast<const uint4*>(src + r * kRowStride + c * 16u);
-                __stcs(reinterpret_cast<uint4*>(dstg + rowoff[r]) + c, v);
-            }
-            __syncwarp();  // every lane's reads of the buffer are done
+            __syncwarp();
             if (i + NB < count) issue_load(i + NB);
         }
         // the copies this warp started have landed before the shared memory
@@ -431,8 +440,9 @@ k_stream_tc(float2* __restrict__ sv0, const TileGeom g, const unsigned char* __r
         tl.count = count;
         tl.first = first;
         tl.ntiles = ntiles;
-        tc_compute_group<NT, GROUPS, MULTI, MATK, LAY>(smem_raw, g, tl, dev0, dev_stride, op_first, nops, pool_off,
-                                                        sops, ops_in_smem, full, done, blob_bar, tcs, err);
+        tc_compute_group<NT, GROUPS, MULTI, MATK, LAY>(smem_raw, g, tl, sv0, reg_stride, dev0, dev_stride, op_first,
+                                                        nops, pool_off, sops, ops_in_smem, full, done, blob_bar, tcs,
+                                                        err);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
