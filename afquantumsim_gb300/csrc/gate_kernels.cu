@@ -62,6 +62,25 @@ __device__ __forceinline__ void store_unit(typename Cx<R>::T* sv, uint64_t i, co
     }
 }
 
+// FP64 forms of the complex128 gate arithmetic, for elements outside the
+// double-float split's range.  Out of line, so that the compiler branches
+// around them instead of issuing their FP64 instructions, predicated off,
+// for every element (GB300's FP64 pipe would then bound the kernel).
+template <typename T, int OP>
+__device__ __noinline__ void pair_fp64(const T* m, T& a, T& b) {
+    const T x = a, y = b;
+    if constexpr (OP == P_DIAG2) {
+        a = cmul(m[0], x);
+        b = cmul(m[1], y);
+    } else {
+        a = cmul2(m[0], x, m[1], y);
+        b = cmul2(m[2], x, m[3], y);
+    }
+}
+
+template <typename T>
+__device__ __noinline__ void diag_fp64(T ph, T& a) { a = cmul(ph, a); }
+
 // ---- pair kernels: MAT2 / DIAG2 / PERM_X / PERM_OR ---------------------------
 // PACKED: c64 with target bit 0 — the pair is one 128-bit access.
 template <typename R, int VEC, bool PACKED, int OP, typename FX>
@@ -104,7 +123,12 @@ k_pair(typename Cx<R>::T* __restrict__ sv, FX fx, uint64_t tmask, uint64_t amask
                 bool wide = !m.df_on;
                 const float2 ar = df_split(a.x, wide), ai = df_split(a.y, wide);
                 const float2 br = df_split(b.x, wide), bi = df_split(b.y, wide);
-                if (!wide) {
+                if (__any_sync(__activemask(), wide)) {  // the whole warp takes the FP64 route
+                    T x = a, y = b;
+                    pair_fp64<T, OP == P_DIAG2 ? P_DIAG2 : P_MAT2>(m.m, x, y);
+                    lo[it].a[v] = x;
+                    hi[it].a[v] = y;
+                } else {
                     T r0, r1;
                     if constexpr (OP == P_MAT2R) {
                         DFAcc x0 = df_mul(ar, m.df[0].re), y0 = df_mul(ai, m.df[0].re);
@@ -145,8 +169,8 @@ k_pair(typename Cx<R>::T* __restrict__ sv, FX fx, uint64_t tmask, uint64_t amask
                     }
                     lo[it].a[v] = r0;
                     hi[it].a[v] = r1;
-                    continue;
                 }
+                continue;
             }
             if constexpr (OP == P_MAT2) {
                 lo[it].a[v] = cmul2(m.m[0], a, m.m[1], b);
@@ -211,14 +235,16 @@ k_diag1(typename Cx<R>::T* __restrict__ sv, FX fx, uint64_t units, typename Cx<R
             if constexpr (sizeof(R) == 8) {  // complex128: double-float on the FP32 pipe
                 bool wide = false;
                 const float2 xr = df_split(a[it].a[v].x, wide), xi = df_split(a[it].a[v].y, wide);
-                if (!wide) {
+                if (__any_sync(__activemask(), wide)) {
+                    diag_fp64(ph, a[it].a[v]);
+                } else {
                     DFAcc re = df_mul(xr, phd.re), im = df_mul(xi, phd.re);
                     df_madd(re, xi, df_neg(phd.im));
                     df_madd(im, xr, phd.im);
                     a[it].a[v].x = df_join(re);
                     a[it].a[v].y = df_join(im);
-                    continue;
                 }
+                continue;
             }
             a[it].a[v] = cmul(ph, a[it].a[v]);
         }
