@@ -167,15 +167,15 @@ __device__ __forceinline__ void fence_async_smem() {
 // K = 2D) and B is the real form above (N = 2D).  Both operands are split
 // into BF16 hi + lo parts; D = Ahi Bhi + Ahi Blo + Alo Bhi accumulates in
 // FP32 in tensor memory (the dropped Alo Blo term is ~2^-18 relative).
-// Operands sit in shared memory in the no-swizzle K-major canonical layout:
-// 8 x 16-byte core matrices, K-direction stride 128 B, M/N-direction stride
-// (K/8) * 128 B.  The interleaved K order lets one bf16x2 conversion turn one
-// amplitude into one 4-byte operand word.
+// A sits in tensor memory (one data column per TMEM lane, one amplitude per
+// 32-bit column: the interleaved K order lets one bf16x2 conversion turn an
+// amplitude into one operand word); B sits in shared memory in the
+// no-swizzle K-major canonical layout: 8 x 16-byte core matrices,
+// K-direction stride 128 B, N-direction stride (K/8) * 128 B.
 
 constexpr int kTcTileBits = 12;
-constexpr int kTcThreads = 512;                    // compute threads: 16 warps in 1 or 2 groups
-constexpr uint32_t kTcTmemCols = 64;               // per compute group: 2^(12+1) / 128
-constexpr uint32_t kTcABytes = 4u << kTcTileBits;  // one split of A: 16 KiB
+constexpr int kTcThreads = 512;                    // compute threads: 16 warps in 2 groups of 8
+constexpr uint32_t kTcTmemCols = 128;              // per compute group: A hi, A lo, D (32 + 32 + 64)
 // A pass's tensor-core operands (per op: B hi and lo splits, then the index
 // tables) are loaded into shared memory once per CTA; at most this many bytes
 // (three 5-qubit unitaries: 3 x 17 KiB).
@@ -227,7 +227,6 @@ __host__ __device__ __forceinline__ uint32_t kmajor_off(uint32_t row, uint32_t k
 }
 
 struct TcSmem {
-    unsigned char* a;      // A hi, then A lo (kTcABytes each)
     const unsigned char* blob;  // the pass's operands; an op's B hi at blob + op.mat
     uint64_t* mma_bar;     // MMAs done
     uint32_t tmem;         // tensor-memory base address (kTcTmemCols columns)
@@ -238,76 +237,114 @@ struct TcPhase {
     uint32_t mma = 0;
 };
 
-// One fused unitary on the tile through the tensor cores, for a unitary on KQ
-// tile bits whose operand gather puts CB lane bits on data columns (and
-// 5 - CB on matrix rows; op.lt1, chosen on the host).  All WARPS x 32 threads
-// of the compute group call it (an aligned block of threads; t.a, t.tmem and
-// t.mma_bar are the group's own).  A bounded wait that gives up sets the
-// error flag (the caller checks it once per tile).
+// ---- fused unitaries with the data operand in tensor memory ---------------------
 //
-// The op's blob entry holds B hi, B lo (2 N K bytes each), then colbase[c]
-// (tile index of data column c; 512 x u16) and offr[r] (tile-index bits of
-// matrix row r; 32 x u16).
+// Each thread gathers the amplitudes of one data column (its TMEM lane = the
+// MMA's M row) from the tile, splits them into BF16 hi and lo and stores
+// them to its lane with tcgen05.st; the MMAs read A from tensor memory and B
+// from the pass's operand blob, so the operand never makes a round trip
+// through shared memory.  A compute
+// group of 8 warps owns 128 TMEM columns: A hi at [0, 32), A lo at [32, 64)
+// (block b of the data columns at 32-bit column b * D, one column per
+// matrix row r = the (re, im) BF16 pair of K indices 2r, 2r + 1), and the
+// FP32 accumulators D at [64, 128) (block b at 64 + b * N).
 //
-// Operand gather: item it of thread (warp w, lane l) is data column
-// c = c0 + it * CSTEP and matrix row r (both fixed by w and l), so a
-// thread's row bits and its column's low bits stay in registers; the column
-// table is linear over disjoint bits, colbase[c] = colbase[c0] |
-// colbase[it * CSTEP], and the operand offset advances by a constant.
-template <class LAY, class SYNC, int KQ, int CB, int WARPS>
-__device__ __forceinline__ void tc_apply_k(float2* s, const TileOp& op, const TcSmem& t, TcPhase& ph) {
+// Thread (warp w, lane l) of the group: lane quarter q = w % 4, half
+// h = w / 4, M row 32 q + l of block b (b = 0 for 5 qubits, b = h for 4, b
+// = h and h + 2 for 3); it gathers rows [r0, r0 + RPT) of that column (r0 =
+// 16 h for 5 qubits, else 0) and later writes back the same amplitudes, so
+// no two threads touch one amplitude within an op.  The host orders the
+// data columns (colbase) so that the 32 lanes of a warp spread over the
+// shared-memory banks.
+
+__device__ __forceinline__ void tc_st16(uint32_t taddr, const uint32_t* r) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+        "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};"
+        ::"r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+          "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+        : "memory");
+}
+__device__ __forceinline__ void tc_st8(uint32_t taddr, const uint32_t* r) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};"
+                 ::"r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]),
+                   "r"(r[7])
+                 : "memory");
+}
+__device__ __forceinline__ void tc_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// D (+)= A B with A in tensor memory (a_tmem), B in shared memory (desc)
+__device__ __forceinline__ void tc_mma_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t idesc,
+                                          uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "r"(a_tmem), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+template <class LAY, class SYNC, int KQ>
+__device__ __forceinline__ void tc_apply_tm(float2* s, const TileOp& op, const TcSmem& t, TcPhase& ph) {
     constexpr uint32_t D = 1u << KQ, K = 2u * D, N = 2u * D;
-    constexpr uint32_t blocks = 1u << (kTcTileBits - KQ - 7);
+    constexpr uint32_t blocks = 1u << (kTcTileBits - KQ - 7);  // 1, 2, 4 blocks of 128 data columns
     constexpr uint32_t bsplit = 2u * N * K;
-    constexpr int WB = WARPS == 16 ? 4 : 3;
-    static_assert(WARPS == 16 || WARPS == 8, "compute group of 8 or 16 warps");
-    constexpr int RB = 5 - CB, KD = KQ - RB;
-    static_assert(RB >= 1 && KD >= 0 && KD <= WB, "lane split");
-    constexpr int ITEMS = 1 << (7 - WB);                 // gathered amplitudes per thread
-    constexpr uint32_t CSTEP = 1u << (5 + WB - KQ);      // column step per item
-    constexpr uint32_t OSTEP = (CSTEP / 8u) * 16u * K;   // operand offset step per item
-    const uint32_t tid = threadIdx.x & (WARPS * 32u - 1u), w = tid >> 5, lane = tid & 31u;
+    constexpr uint32_t RPT = KQ == 3 ? 8u : 16u;               // matrix rows per thread and block
+    constexpr uint32_t BPT = KQ == 3 ? 2u : 1u;                // blocks per thread
+    static_assert(blocks * D == 32u, "A hi and lo take 32 columns each");
+    const uint32_t tid = threadIdx.x & 255u, w = tid >> 5, lane = tid & 31u;
+    const uint32_t q = w & 3u, h = w >> 2;
     const unsigned char* bsm = t.blob + op.mat;
     const uint16_t* colbase = reinterpret_cast<const uint16_t*>(bsm + 2u * bsplit);
     const uint16_t* offr = colbase + 512;
+    const uint32_t lane_base = t.tmem + ((32u * q) << 16);
+    const uint32_t r0 = KQ == 5 ? 16u * h : 0u;
 
-    {
-        const uint32_t r = ((w & ((1u << KD) - 1u)) << RB) | (lane & ((1u << RB) - 1u));
-        const uint32_t c0 = ((w >> KD) << CB) | (lane >> RB);
-        const uint32_t j0 = (uint32_t)colbase[c0] | (uint32_t)offr[r];
-        const uint32_t off0 = (c0 >> 3) * 16u * K + (r >> 2) * 128u + (c0 & 7u) * 16u + (r & 3u) * 4u;
-        unsigned char* ahi = t.a + off0;
-#pragma unroll 8
-        for (int it = 0; it < ITEMS; ++it) {
-            const uint32_t j = j0 | (uint32_t)colbase[CSTEP * it];
-            const float2 x = s[LAY::at(j)];
-            const __nv_bfloat162 hi = __float22bfloat162_rn(x);
-            const float2 hf = __bfloat1622float2(hi);
-            const __nv_bfloat162 lo = __float22bfloat162_rn(make_float2(x.x - hf.x, x.y - hf.y));
-            *reinterpret_cast<__nv_bfloat162*>(ahi + OSTEP * it) = hi;
-            *reinterpret_cast<__nv_bfloat162*>(ahi + kTcABytes + OSTEP * it) = lo;
+    uint32_t jb[BPT], bk[BPT];
+#pragma unroll
+    for (uint32_t i = 0; i < BPT; ++i) {
+        bk[i] = KQ == 5 ? 0u : (KQ == 4 ? h : h + 2u * i);
+        jb[i] = colbase[128u * bk[i] + 32u * q + lane];
+    }
+#pragma unroll
+    for (uint32_t i = 0; i < BPT; ++i) {
+        uint32_t hi[RPT], lo[RPT];
+#pragma unroll
+        for (uint32_t e = 0; e < RPT; ++e) {
+            const float2 x = s[LAY::at(jb[i] | (uint32_t)offr[r0 + e])];
+            const __nv_bfloat162 bh = __float22bfloat162_rn(x);
+            const float2 hf = __bfloat1622float2(bh);
+            const __nv_bfloat162 bl = __float22bfloat162_rn(make_float2(x.x - hf.x, x.y - hf.y));
+            hi[e] = *reinterpret_cast<const uint32_t*>(&bh);
+            lo[e] = *reinterpret_cast<const uint32_t*>(&bl);
+        }
+        const uint32_t col = bk[i] * D + r0;
+        if constexpr (RPT == 16) {
+            tc_st16(lane_base + col, hi);
+            tc_st16(lane_base + 32u + col, lo);
+        } else {
+            tc_st8(lane_base + col, hi);
+            tc_st8(lane_base + 32u + col, lo);
         }
     }
-    fence_async_smem();
+    tc_st_wait();
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     SYNC::sync();
 
     if (tid == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t idesc = tc_idesc(128, N);
         constexpr uint32_t sbo = (K / 8u) * 128u;
-        const uint32_t a_hi = smem_u32(t.a), a_lo = a_hi + kTcABytes;
         const uint32_t b_hi = smem_u32(bsm), b_lo = b_hi + bsplit;
 #pragma unroll
         for (uint32_t blk = 0; blk < blocks; ++blk) {
-            const uint32_t dcol = t.tmem + blk * N;
-            const uint32_t aoff = blk * (256u * K);
+            const uint32_t dcol = t.tmem + 64u + blk * N;
+            const uint32_t a_hi = t.tmem + blk * D, a_lo = a_hi + 32u;
 #pragma unroll
             for (uint32_t st = 0; st < K / 16u; ++st) {
-                const uint32_t ko = st * 256u;  // two core matrices along K
-                tc_mma(dcol, tc_desc(a_hi + aoff + ko, 128u, sbo), tc_desc(b_hi + ko, 128u, sbo), idesc,
-                       st > 0 ? 1u : 0u);
-                tc_mma(dcol, tc_desc(a_hi + aoff + ko, 128u, sbo), tc_desc(b_lo + ko, 128u, sbo), idesc, 1u);
-                tc_mma(dcol, tc_desc(a_lo + aoff + ko, 128u, sbo), tc_desc(b_hi + ko, 128u, sbo), idesc, 1u);
+                const uint32_t ko = st * 256u;  // two core matrices of B along K
+                tc_mma_ta(dcol, a_hi + 8u * st, tc_desc(b_hi + ko, 128u, sbo), idesc, st > 0 ? 1u : 0u);
+                tc_mma_ta(dcol, a_hi + 8u * st, tc_desc(b_lo + ko, 128u, sbo), idesc, 1u);
+                tc_mma_ta(dcol, a_lo + 8u * st, tc_desc(b_hi + ko, 128u, sbo), idesc, 1u);
             }
         }
         tc_commit(t.mma_bar);
@@ -316,46 +353,35 @@ __device__ __forceinline__ void tc_apply_k(float2* s, const TileOp& op, const Tc
     ph.mma ^= 1u;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
-    // D straight to the tile: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its
-    // data columns) and the 16-column chunks w / 4, w / 4 + WARPS / 4, ...
-    // of the 64 (8 output rows each)
-    const uint32_t g = w & 3u;
-#pragma unroll 1
-    for (uint32_t h = w >> 2; h < 4u; h += WARPS / 4u) {
-        uint32_t v[16];
-        tc_ld16(t.tmem + ((g * 32u) << 16) + h * 16u, v);
-        tc_ld_wait();
-        const uint32_t tcol = h * 16u;
-        const uint32_t c = ((tcol >> (KQ + 1)) << 7) + g * 32u + lane;
-        const uint32_t r0 = (tcol & (N - 1u)) >> 1;
-        const uint32_t cbase = colbase[c];
+    // D back to the amplitudes this thread gathered: output row r0 + e of
+    // block bk is D columns 2 (r0 + e) and 2 (r0 + e) + 1
 #pragma unroll
-        for (int i = 0; i < 8; ++i)
-            s[LAY::at(cbase | (uint32_t)offr[r0 + i])] =
-                make_float2(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1]));
+    for (uint32_t i = 0; i < BPT; ++i) {
+        const uint32_t dbase = lane_base + 64u + bk[i] * N + 2u * r0;
+#pragma unroll
+        for (uint32_t c16 = 0; c16 < 2u * RPT; c16 += 16u) {
+            uint32_t v[16];
+            tc_ld16(dbase + c16, v);
+            tc_ld_wait();
+#pragma unroll
+            for (uint32_t e = 0; e < 8u; ++e)
+                s[LAY::at(jb[i] | (uint32_t)offr[r0 + c16 / 2u + e])] =
+                    make_float2(__uint_as_float(v[2 * e]), __uint_as_float(v[2 * e + 1]));
+        }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     SYNC::sync();
 }
 
+// One fused unitary of 3..5 qubits on the tile through the tensor cores; all
+// 256 threads of the compute group (8 warps) call it.
 template <class LAY, class SYNC, int WARPS>
 __device__ __forceinline__ void tc_apply(float2* s, const TileOp& op, const TcSmem& t, TcPhase& ph) {
-    switch (op.k * 8 + op.lt1) {
-        case 3 * 8 + 2: tc_apply_k<LAY, SYNC, 3, 2, WARPS>(s, op, t, ph); break;
-        case 3 * 8 + 3: tc_apply_k<LAY, SYNC, 3, 3, WARPS>(s, op, t, ph); break;
-        case 3 * 8 + 4: tc_apply_k<LAY, SYNC, 3, 4, WARPS>(s, op, t, ph); break;
-        case 4 * 8 + 2: tc_apply_k<LAY, SYNC, 4, 2, WARPS>(s, op, t, ph); break;
-        case 4 * 8 + 3: tc_apply_k<LAY, SYNC, 4, 3, WARPS>(s, op, t, ph); break;
-        case 4 * 8 + 4: tc_apply_k<LAY, SYNC, 4, 4, WARPS>(s, op, t, ph); break;
-        case 5 * 8 + 2: tc_apply_k<LAY, SYNC, 5, 2, WARPS>(s, op, t, ph); break;
-        default:
-            if constexpr (WARPS == 16) {
-                if (op.lt1 == 4) tc_apply_k<LAY, SYNC, 5, 4, WARPS>(s, op, t, ph);
-                else tc_apply_k<LAY, SYNC, 5, 3, WARPS>(s, op, t, ph);
-            } else {
-                tc_apply_k<LAY, SYNC, 5, 3, WARPS>(s, op, t, ph);  // the host keeps 5 - lt1 >= 2 here
-            }
-            break;
+    static_assert(WARPS == 8, "compute groups of 8 warps");
+    switch (op.k) {
+        case 3: tc_apply_tm<LAY, SYNC, 3>(s, op, t, ph); break;
+        case 4: tc_apply_tm<LAY, SYNC, 4>(s, op, t, ph); break;
+        default: tc_apply_tm<LAY, SYNC, 5>(s, op, t, ph); break;
     }
 }
 

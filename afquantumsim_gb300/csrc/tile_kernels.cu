@@ -165,22 +165,22 @@ constexpr int kTcMaxOps = 48;                       // op tables up to this size
 constexpr uint32_t kTcRowStride = 272u;             // padded tile row in the tensor-core kernel
 static_assert(sizeof(TileOp) % 16 == 0, "op tables are bulk-copied: 16-byte multiples");
 
-// Shared memory of the tensor-core streaming kernel: three tile buffers (the
-// compute groups' tiles, the next loaded, the previous storing), then per
-// compute group an A operand (hi and lo splits), then the pass's operand blob.
-// Rows are padded by 16 bytes (a 272-byte stride) so the operand gathers of
-// rows that share their low index bits spread over the banks.
+// Shared memory of the tensor-core streaming kernel: four tile buffers (the
+// two compute groups' tiles and two loading), the row offsets, barriers, the
+// op table and the pass's operand blob (the MMAs' data operand lives in
+// tensor memory).  Rows are padded by 16 bytes (a 272-byte stride) so the
+// operand gathers of rows that share their low index bits spread over the
+// banks.
 template <int GROUPS>
 struct TcStreamSmemT {
-    static constexpr int kBufs = 3;
+    static constexpr int kBufs = 4;
     static constexpr uint32_t kRowStride = kTcRowStride;
     static constexpr uint32_t kBufBytes = kRows * kRowStride;          // 34 KiB
     static constexpr uint32_t kRowOff = kBufs * kBufBytes;              // kRows x u64
-    static constexpr uint32_t kBars = kRowOff + kRows * 8u;             // full[3] done[3] mma[2] blob
+    static constexpr uint32_t kBars = kRowOff + kRows * 8u;             // full[4] done[4] mma[2] blob
     static constexpr uint32_t kTmemSlot = kBars + 16u * 8u;
     static constexpr uint32_t kOps = (kTmemSlot + 16u + 127u) & ~127u;  // kTcMaxOps TileOps
-    static constexpr uint32_t kA = (kOps + kTcMaxOps * (uint32_t)sizeof(TileOp) + 1023u) & ~1023u;
-    static constexpr uint32_t kBlob = kA + GROUPS * 2u * kTcABytes;
+    static constexpr uint32_t kBlob = (kOps + kTcMaxOps * (uint32_t)sizeof(TileOp) + 1023u) & ~1023u;
     static constexpr uint32_t kBytes = kBlob + kTcBlobMax;
     static_assert(kBytes <= 232448u, "more shared memory than a CTA may have");
 };
@@ -204,7 +204,7 @@ __device__ __forceinline__ bool group_any(bool v) {
 // CTA per SM walks its tiles; a tile is 128 rows of 256 contiguous bytes
 // (the 5 low index bits) at the row offsets of the pass's 7 high tile bits.
 // Warp 16 is the producer: it copies tiles in 16-byte cp.async chunks into
-// three shared-memory buffers (full[b] completes when all 32 lanes' chunks
+// four shared-memory buffers (full[b] completes when all 32 lanes' chunks
 // have landed; many small requests stay in flight without the per-request
 // cost of bulk copies), and loads the next tile into a buffer as soon as the
 // compute group that ran its tile has written it back with 128-bit stores
@@ -431,7 +431,6 @@ k_stream_tc(float2* __restrict__ sv0, const TileGeom g, const unsigned char* __r
         // ---- compute groups ----
         const uint32_t grp = warp / (NT / 32);
         TcSmem tcs;
-        tcs.a = smem_raw + SM::kA + grp * 2u * kTcABytes;
         tcs.blob = smem_raw + SM::kBlob;
         tcs.mma_bar = mma_bar + grp;
         tcs.tmem = *reinterpret_cast<volatile uint32_t*>(smem_raw + SM::kTmemSlot) + grp * kTcTmemCols;
@@ -642,21 +641,22 @@ static size_t tc_op_bytes(int k) {
 }
 
 // Index tables of a tensor-core op, appended to the blob after its B splits:
-// colbase[c] = tile index of data column c (c spread over the non-target
-// tile bits, ascending), offr[r] = tile-index bits of matrix row r (qubit
-// ltb[0] is the row's most significant bit).  Also picks the op's lane split
-// for the operand gather (t.lt1 = lane bits on data columns, the rest on
-// matrix rows): the split whose first warps touch the fewest shared-memory
-// wavefronts, reading the padded tile (row stride kTcRowStride bytes) and
-// writing the 4-byte operand words.  Both depend only on the op's tile
-// bits, so they are computed once per host thread and bit set.
+// colbase[c] = tile index of data column c (c over the non-target tile
+// bits), offr[r] = tile-index bits of matrix row r (qubit ltb[0] is the
+// row's most significant bit).  Data column c is the MMA's M row c % 128 of
+// block c / 128 and the TMEM lane of the thread that gathers it, so the 32
+// lanes of a warp read columns c .. c + 31 at once: the five lowest bits of
+// c go to the five non-target tile bits that spread those reads (and the
+// write-back) over the most shared-memory banks in the padded tile layout,
+// the remaining bits of c to the other non-target bits in ascending order.
+// Both tables depend only on the op's tile bits, so they are computed once
+// per host thread and bit set.
 constexpr size_t kTcTableBytes = 1024 + 64;
-static int tc_tables_compute(const TileOp& t, unsigned char* out);
+static void tc_tables_compute(const TileOp& t, unsigned char* out);
 
 static void tc_tables(TileOp& t, std::vector<unsigned char>& blob) {
     struct Entry {
         unsigned char bytes[kTcTableBytes];
-        int cb;
     };
     thread_local std::unordered_map<uint64_t, Entry> memo;
     uint64_t key = (uint64_t)t.k;
@@ -669,72 +669,84 @@ static void tc_tables(TileOp& t, std::vector<unsigned char>& blob) {
         if (memo.size() >= 4096) memo.clear();
         Entry e;
         std::memset(e.bytes, 0, sizeof(e.bytes));
-        e.cb = tc_tables_compute(t, e.bytes);
+        tc_tables_compute(t, e.bytes);
         it = memo.emplace(key, e).first;
     }
     blob.insert(blob.end(), it->second.bytes, it->second.bytes + kTcTableBytes);
-    t.lt1 = it->second.cb;
+    t.lt1 = 0;
 }
 
-// The tables of tc_tables into out (kTcTableBytes, zeroed); returns the
-// lane split.
-static int tc_tables_compute(const TileOp& t, unsigned char* out) {
+// Shared-memory wavefronts of 32 lanes reading one float2 each at tile
+// indices j[0..31] in the padded layout (row stride kTcRowStride): the most
+// distinct 4-byte words any bank must deliver.
+static int tc_wavefronts(const uint32_t* j) {
+    const uint32_t pad = (kTcRowStride - 256u) / 8u;  // float2 elements of padding per row
+    uint32_t words[32][64];
+    int cnt[32] = {0};
+    int worst = 0;
+    for (int l = 0; l < 32; ++l) {
+        const uint32_t w0 = 2u * (j[l] + (j[l] >> 5) * pad);  // first 4-byte word
+        for (uint32_t w = w0; w < w0 + 2u; ++w) {
+            const uint32_t b = w & 31u;
+            bool seen = false;
+            for (int i = 0; i < cnt[b]; ++i) seen |= words[b][i] == w;
+            if (!seen) words[b][cnt[b]++] = w;
+            worst = std::max(worst, cnt[b]);
+        }
+    }
+    return worst;
+}
+
+static void tc_tables_compute(const TileOp& t, unsigned char* out) {
     const int k = t.k;
     uint32_t tmask = 0;
     for (int i = 0; i < k; ++i) tmask |= 1u << t.ltb[i];
     const uint32_t nmask = ((1u << kTcTileBits) - 1u) & ~tmask;
-    const uint32_t cols = 1u << (kTcTileBits - k);
-    std::vector<uint32_t> colbase(cols), offr(1u << k);
+    std::vector<int> free_bits;
+    for (int b = 0; b < kTcTileBits; ++b)
+        if ((nmask >> b) & 1u) free_bits.push_back(b);
+    const int nf = (int)free_bits.size();  // 12 - k >= 7
+    // the five lane bits: every choice of 5 of the free bits, fewest
+    // wavefronts first, then the lowest bits
+    uint32_t best_sel = 0;
+    int best_cost = 1 << 30;
+    for (uint32_t sel = 0; sel < (1u << nf); ++sel) {
+        if (__builtin_popcount(sel) != 5) continue;
+        uint32_t lanes[32];
+        for (uint32_t l = 0; l < 32; ++l) {
+            uint32_t j = 0, x = l;
+            for (int i = 0; i < nf; ++i)
+                if ((sel >> i) & 1u) {
+                    j |= (x & 1u) << free_bits[i];
+                    x >>= 1;
+                }
+            lanes[l] = j;
+        }
+        const int cost = tc_wavefronts(lanes);
+        if (cost < best_cost) {
+            best_cost = cost;
+            best_sel = sel;
+        }
+    }
+    std::vector<int> order;  // bit i of c -> tile bit order[i]
+    for (int i = 0; i < nf; ++i)
+        if ((best_sel >> i) & 1u) order.push_back(free_bits[i]);
+    for (int i = 0; i < nf; ++i)
+        if (!((best_sel >> i) & 1u)) order.push_back(free_bits[i]);
+    const uint32_t cols = 1u << nf;
     for (uint32_t c = 0; c < cols; ++c) {
-        uint32_t x = c, j = 0;
-        for (int b = 0; b < kTcTileBits; ++b)
-            if ((nmask >> b) & 1u) {
-                j |= (x & 1u) << b;
-                x >>= 1;
-            }
-        colbase[c] = j;
+        uint32_t j = 0;
+        for (int i = 0; i < nf; ++i) j |= ((c >> i) & 1u) << order[i];
+        const uint16_t v = (uint16_t)j;
+        std::memcpy(out + 2 * c, &v, 2);
     }
     for (uint32_t r = 0; r < (1u << k); ++r) {
         uint32_t off = 0;
         for (int i = 0; i < k; ++i)
             if ((r >> (k - 1 - i)) & 1u) off |= 1u << t.ltb[i];
-        offr[r] = off;
-    }
-    for (uint32_t c = 0; c < cols; ++c) {
-        const uint16_t v = (uint16_t)colbase[c];
-        std::memcpy(out + 2 * c, &v, 2);
-    }
-    for (uint32_t r = 0; r < (1u << k); ++r) {
-        const uint16_t v = (uint16_t)offr[r];
+        const uint16_t v = (uint16_t)off;
         std::memcpy(out + 1024 + 2 * r, &v, 2);
     }
-    // lane split: cb column bits, 5 - cb row bits (5 - cb <= k)
-    const uint32_t pad = (kTcRowStride - 256u) / 8u;  // float2 elements of padding per row
-    int best_cb = 3, best_cost = 1 << 30;
-    for (int cb = 2; cb <= 4; ++cb) {
-        const int rb = 5 - cb;
-        // the row bits beyond the lane's come from the warp index within a
-        // compute group of 16 / kTcGroups warps
-        if (rb > k || k - rb > (kTcGroups == 1 ? 4 : 3)) continue;
-        int cost = 0;
-        for (uint32_t w = 0; w < 4; ++w) {
-            int rd[16] = {0}, wr[32] = {0};
-            for (uint32_t lane = 0; lane < 32; ++lane) {
-                const uint32_t u = w * 32 + lane, rest = u >> 5;
-                const uint32_t c = ((rest >> (k - rb)) << cb) | (lane >> rb);
-                const uint32_t r = ((rest & ((1u << (k - rb)) - 1u)) << rb) | (lane & ((1u << rb) - 1u));
-                const uint32_t j = colbase[c % cols] | offr[r];
-                ++rd[(j + (j >> 5) * pad) & 15u];
-                ++wr[(((c & 127u) & 7u) * 4u + (r & 3u)) & 31u];
-            }
-            cost += *std::max_element(rd, rd + 16) + 2 * *std::max_element(wr, wr + 32);
-        }
-        if (cost < best_cost) {
-            best_cost = cost;
-            best_cb = cb;
-        }
-    }
-    return best_cb;
 }
 
 // Encode the passes of `ops` into a table of TileOps and an operand pool.
