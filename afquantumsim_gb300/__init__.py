@@ -44,6 +44,7 @@ EXPORTS = [
     "aqsg_expect_pauli", "aqsg_autotune", "aqsg_batch_tuning", "aqsg_selftest_bounded_wait",
     "aqsg_state_download_async", "aqsg_circuit_to_text", "aqsg_circuit_from_text",
     "aqsg_debug_tile_plan", "aqsg_debug_batch_image", "aqsg_debug_ctx_scratch", "aqsg_batch_traffic",
+    "aqsg_noise_trajectory", "aqsg_noise_expect_z",
 ]
 
 _lib = None
@@ -701,6 +702,61 @@ class Batch:
 
 
 # ---- serving runtime -----------------------------------------------------------
+
+class Noise(C.Structure):
+    """struct aqsg_noise: X, Y, Z probabilities per touched qubit after
+    one-qubit gates (p1) and after gates on several qubits (p2)."""
+    _fields_ = [("p1", C.c_float * 3), ("p2", C.c_float * 3)]
+
+    @classmethod
+    def pauli(cls, p1=(0.0, 0.0, 0.0), p2=(0.0, 0.0, 0.0)) -> "Noise":
+        return cls((C.c_float * 3)(*p1), (C.c_float * 3)(*p2))
+
+    @classmethod
+    def depolarizing(cls, p1: float, p2: float) -> "Noise":
+        """Depolarizing noise of strength p1 / p2 on each touched qubit."""
+        return cls.pauli((p1 / 3,) * 3, (p2 / 3,) * 3)
+
+
+def _bind_noise(lib):
+    P, I, U64, D = C.c_void_p, C.c_int, C.c_uint64, C.POINTER(C.c_double)
+    lib.aqsg_noise_trajectory.argtypes = [I, C.POINTER(Op), I, C.POINTER(Noise), U64, U64, C.POINTER(Op), I,
+                                          C.POINTER(I)]
+    lib.aqsg_noise_expect_z.argtypes = [P, I, C.POINTER(Op), I, C.POINTER(Noise), U64, I, D, D, D, D]
+    lib.aqsg_noise_trajectory.restype = I
+    lib.aqsg_noise_expect_z.restype = I
+
+
+def noise_trajectory(n: int, ops, noise: Noise, seed: int, trajectory: int):
+    """aqsg_noise_trajectory: the ops of one trajectory of the noisy circuit
+    (the sampled Paulis inserted after the gates they follow)."""
+    lib = load_library()
+    _bind_noise(lib)
+    arr = op_array(list(ops)) if not isinstance(ops, C.Array) else ops
+    cnt = C.c_int()
+    _check(lib.aqsg_noise_trajectory(n, arr, len(arr), C.byref(noise), seed, trajectory, None, 0, C.byref(cnt)))
+    out = (Op * max(cnt.value, 1))()
+    _check(lib.aqsg_noise_trajectory(n, arr, len(arr), C.byref(noise), seed, trajectory, out, cnt.value,
+                                      C.byref(cnt)))
+    res = (Op * cnt.value).from_buffer(out)
+    res._keep = (arr, out)
+    return res
+
+
+def noisy_expect_z(ctx: "Context", n: int, ops, noise: Noise, seed: int, trajectories: int):
+    """aqsg_noise_expect_z: (<Z_q>, <Z_q Z_q+1>, their standard errors) of
+    the noisy circuit from |0...0>, estimated by `trajectories` trajectories
+    run as one batch."""
+    lib = load_library()
+    _bind_noise(lib)
+    arr = op_array(list(ops)) if not isinstance(ops, C.Array) else ops
+    z, zz = np.zeros(n), np.zeros(n - 1)
+    ze, zze = np.zeros(n), np.zeros(n - 1)
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    _check(lib.aqsg_noise_expect_z(ctx.h, n, arr, len(arr), C.byref(noise), seed, trajectories, dp(z), dp(zz),
+                                   dp(ze), dp(zze)))
+    return z, zz, ze, zze
+
 
 class ServerDone(C.Structure):
     """struct aqsg_server_done."""

@@ -28,7 +28,7 @@ ORACLE_BUILD = ORACLE / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"] + ARCH
-CU_SOURCES = ["api.cu", "gate_kernels.cu", "measure_kernels.cu", "tile_kernels.cu", "fusion.cu", "batch.cu", "server.cu", "tune.cu", "circuit_text.cu"]
+CU_SOURCES = ["api.cu", "gate_kernels.cu", "measure_kernels.cu", "tile_kernels.cu", "fusion.cu", "batch.cu", "server.cu", "tune.cu", "circuit_text.cu", "noise.cu"]
 CPP_SOURCES = ["quantum.cpp", "quantum_gates.cpp", "quantum_algo.cpp"]
 
 

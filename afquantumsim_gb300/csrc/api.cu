@@ -46,7 +46,7 @@ static const char* kAt = "Cannot add gate at the given qubit position";
 static const char* kCtlTgt = "Control qubit cannot be the same as the target qubit";
 static const char* kSwapSame = "Cannot use the swap gate on the same target qubits";
 
-static int arity(int kind) {
+int op_arity(int kind) {
     switch (kind) {
         case AQSG_OP_BARRIER: return 0;
         case AQSG_OP_X: case AQSG_OP_Y: case AQSG_OP_Z: case AQSG_OP_H:
@@ -120,7 +120,7 @@ int check_op(int n, const aqsg_op& op) {
     if (op.num_controls < 0 || op.num_controls > AQSG_OP_MAX_CONTROLS)
         return set_error(AQSG_ERR_INVALID_ARGUMENT, "Too many control qubits");
     if (op.num_controls > 0) {
-        int na = op.kind == AQSG_OP_UNITARY ? op.num_qubits : arity(op.kind);
+        int na = op.kind == AQSG_OP_UNITARY ? op.num_qubits : op_arity(op.kind);
         for (int i = 0; i < op.num_controls; ++i) {
             int c = op.controls[i];
             // ControlGate::check, quantum.cpp:1871-1886

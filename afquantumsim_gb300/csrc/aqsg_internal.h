@@ -81,6 +81,9 @@ struct LOp {
     bool diagonal() const { return cls == L_DIAG1 || cls == L_DIAG2; }
 };
 
+// Number of target qubits of a gate kind (0 for a barrier, -1 if unknown;
+// unitaries carry theirs in num_qubits).
+int op_arity(int kind);
 // Validate one op against an n-qubit register with the reference's check()
 // messages; returns AQSG_OK or an error code (message set).
 int check_op(int n, const aqsg_op& op);

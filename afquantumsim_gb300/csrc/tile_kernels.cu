@@ -20,6 +20,9 @@
 #include <mutex>
 #include <unordered_map>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "tile_device.cuh"
 
 namespace aqsg {
@@ -164,6 +167,54 @@ constexpr int kTcGroups = 2;                        // compute groups (tiles in 
 constexpr int kTcMaxOps = 48;                       // op tables up to this size go to shared memory
 constexpr uint32_t kTcRowStride = 272u;             // padded tile row in the tensor-core kernel
 static_assert(sizeof(TileOp) % 16 == 0, "op tables are bulk-copied: 16-byte multiples");
+
+// ---- tile loads by the tensor memory accelerator -----------------------------
+//
+// A tensor-core pass loads each tile with one cp.async.bulk.tensor.  The
+// register is described to the TMA unit as a tensor of rank 2..5: dimension
+// 0 is index bits [0, start[1]) (the 32-amplitude row and the non-tile bits
+// above it up to the first run of high tile bits), dimension i >= 1 is bits
+// [start[i], start[i] + bits[i]) (one run of high tile bits and the
+// non-tile bits above it), so a tile is the box of 34 x 2^run_1 x ... rows:
+// each row of 32 amplitudes plus the next 2, which land in the row padding
+// of the shared-memory layout (272-byte rows).  Amplitudes past the end of a
+// dimension read as zero (they only ever reach padding).  A grouped pass
+// (several registers back to back) extends the top dimension over the
+// members.  Passes whose high tile bits form more than four runs keep the
+// cp.async loader (rank 0).
+struct TmaGeom {
+    int32_t rank;      // 0: no tensor map
+    int32_t start[5];  // first index bit of each dimension
+    int32_t bits[5];   // index bits each dimension covers
+};
+constexpr uint32_t kTmaRowBox = 34;  // amplitudes per row the box reads: 32 + the padding
+
+__device__ __forceinline__ void tma_load_tile(void* dst, const CUtensorMap* map, int rank, const int32_t* c,
+                                              uint64_t* bar) {
+    const uint64_t m = reinterpret_cast<uint64_t>(map);
+    const uint32_t d = smem_u32(dst), b = smem_u32(bar);
+    switch (rank) {
+        case 2:
+            asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                         " [%0], [%1, {%2, %3}], [%4];" ::"r"(d), "l"(m), "r"(c[0]), "r"(c[1]), "r"(b) : "memory");
+            break;
+        case 3:
+            asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                         " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(d), "l"(m), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(b)
+                         : "memory");
+            break;
+        case 4:
+            asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                         " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(d), "l"(m), "r"(c[0]), "r"(c[1]), "r"(c[2]),
+                         "r"(c[3]), "r"(b) : "memory");
+            break;
+        default:
+            asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                         " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(d), "l"(m), "r"(c[0]), "r"(c[1]),
+                         "r"(c[2]), "r"(c[3]), "r"(c[4]), "r"(b) : "memory");
+            break;
+    }
+}
 
 // Shared memory of the tensor-core streaming kernel: four tile buffers (the
 // two compute groups' tiles and two loading), the row offsets, barriers, the
@@ -315,7 +366,7 @@ template <bool MULTI, bool MATK>
 __global__ void __launch_bounds__(kTcCta, 1)
 k_stream_tc(float2* __restrict__ sv0, const TileGeom g, const unsigned char* __restrict__ dev0, uint32_t op_first,
             int nops, uint64_t pool_off, int* err, uint32_t ntiles, uint32_t members, uint64_t reg_stride,
-            uint64_t dev_stride) {
+            uint64_t dev_stride, const __grid_constant__ CUtensorMap tmap, const TmaGeom tg) {
     using SM = TcStreamSmem;
     constexpr int NB = SM::kBufs;
     constexpr int GROUPS = kTcGroups;
@@ -340,7 +391,7 @@ k_stream_tc(float2* __restrict__ sv0, const TileGeom g, const unsigned char* __r
     }
     if (tid == 0) {
         for (int b = 0; b < NB; ++b) {
-            mbar_init(full + b, 32);  // one cp.async arrival per producer lane
+            mbar_init(full + b, tg.rank ? 1 : 32);  // the TMA load, or one cp.async arrival per producer lane
             mbar_init(done + b, NT / 32);
         }
         for (int q = 0; q < GROUPS; ++q) mbar_init(mma_bar + q, 1);
@@ -400,8 +451,20 @@ k_stream_tc(float2* __restrict__ sv0, const TileGeom g, const unsigned char* __r
         if (lane == 0) load_blob(count ? member_of(0) : 0u);
         auto issue_load = [&](uint32_t i) {
             const uint32_t buf = i % NB;
-            const float2* src = sv_of(member_of(i)) + tile_base(local_of(i));
             unsigned char* dst = smem_raw + buf * kBufBytes;
+            if (tg.rank) {  // one TMA load of the whole tile (lane 0)
+                if (lane == 0) {
+                    const uint64_t base = tile_base(local_of(i));
+                    int32_t c[5];
+                    for (int d = 0; d < tg.rank; ++d)
+                        c[d] = (int32_t)((base >> tg.start[d]) & ((1ull << tg.bits[d]) - 1ull));
+                    if (MULTI) c[tg.rank - 1] += (int32_t)(member_of(i) << tg.bits[tg.rank - 1]);
+                    mbar_expect_tx(full + buf, kBufBytes);
+                    tma_load_tile(dst, &tmap, tg.rank, c, full + buf);
+                }
+                return;
+            }
+            const float2* src = sv_of(member_of(i)) + tile_base(local_of(i));
 #pragma unroll 8
             for (uint32_t q = lane; q < kRows * 16u; q += 32u) {
                 const uint32_t r = q >> 4, c = q & 15u;
@@ -1129,6 +1192,62 @@ static int stream_shape(K kernel, int threads, int shm, StreamShape* out) {
     return AQSG_OK;
 }
 
+// cuTensorMapEncodeTiled from the driver, looked up once (null if the
+// driver has none: tile loads then stay on cp.async).
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// The tensor map of a tensor-core pass's tiles over `members` registers of
+// 2^n amplitudes stored back to back at sv (see TmaGeom); tg->rank = 0 when
+// the pass's high tile bits form more than four runs or the encoding fails.
+static void tile_tensor_map(void* sv, int n, const TilePass& p, uint32_t members, CUtensorMap* map, TmaGeom* tg) {
+    std::memset(tg, 0, sizeof(*tg));
+    std::memset(map, 0, sizeof(*map));
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc || p.m != kTcTileBits || p.L != 5) return;
+    int rank = 1;
+    int start[5] = {0, 0, 0, 0, 0}, run[5] = {5, 0, 0, 0, 0};
+    for (int i = p.L; i < p.m; ++i) {
+        const int b = p.tbits[i];
+        if (rank > 1 && b == start[rank - 1] + run[rank - 1]) {
+            ++run[rank - 1];
+            continue;
+        }
+        if (rank == 5) return;  // a fifth run of high bits
+        start[rank] = b;
+        run[rank] = 1;
+        ++rank;
+    }
+    cuuint64_t dim[5], stride[4];
+    cuuint32_t box[5], estride[5] = {1, 1, 1, 1, 1};
+    for (int d = 0; d < rank; ++d) {
+        const int end = d + 1 < rank ? start[d + 1] : n;
+        tg->start[d] = start[d];
+        tg->bits[d] = end - start[d];
+        dim[d] = (cuuint64_t)1 << (end - start[d]);
+        box[d] = d == 0 ? kTmaRowBox : (cuuint32_t)1 << run[d];
+        if (d > 0) stride[d - 1] = ((cuuint64_t)1 << start[d]) * sizeof(float2);
+    }
+    dim[rank - 1] *= members;
+    const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_INT64, (cuuint32_t)rank, sv, dim, stride, box, estride,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r == CUDA_SUCCESS) tg->rank = rank;
+}
+
 template <typename R>
 static int launch_plan_t(void* sv, const TilePlan& plan, const void* dev, cudaStream_t stream, int* d_err,
                          uint64_t* launches) {
@@ -1174,9 +1293,12 @@ static int launch_plan_t(void* sv, const TilePlan& plan, const void* dev, cudaSt
             if (p.tc_bytes > kTcBlobMax) return set_error(AQSG_ERR_RUNTIME, "Tensor-core operands exceed the blob");
             const uint32_t tiles = 1u << (n - geo.m);
             const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)(tshape.sms * tshape.per_sm));
+            CUtensorMap map;
+            TmaGeom tg;
+            tile_tensor_map(sv, n, p, 1u, &map, &tg);
             ktc<<<grid, kTcCta, TcStreamSmem::kBytes, stream>>>(
                 (float2*)sv, geo, (const unsigned char*)dev, p.first, (int)p.count, plan.pool_offset(), d_err, tiles,
-                1u, 0ull, 0ull);
+                1u, 0ull, 0ull, map, tg);
         } else if (geo.m == n) {
             const int rb = phase_reg_bits(plan.dtype);
             int threads = (int)(geo.m >= rb + kPhaseMinSlotBits ? size >> rb : size / EPT_WHOLE);
@@ -1231,9 +1353,15 @@ int launch_tile_plan_multi(void* sv0, uint64_t reg_stride, int members, const Ti
             }
             if (p.tc_bytes > kTcBlobMax) return set_error(AQSG_ERR_RUNTIME, "Tensor-core operands exceed the blob");
             const uint32_t grid = (uint32_t)std::min<uint64_t>(blocks, (uint64_t)tshape.sms * tshape.per_sm);
+            CUtensorMap map;
+            TmaGeom tg;
+            std::memset(&map, 0, sizeof(map));
+            std::memset(&tg, 0, sizeof(tg));
+            // the members' registers must lie back to back for one tensor map
+            if (reg_stride == (1ull << n)) tile_tensor_map(sv0, n, p, (uint32_t)members, &map, &tg);
             ktc<<<grid, kTcCta, TcStreamSmem::kBytes, stream>>>(
                 (float2*)sv0, geo, (const unsigned char*)dev0, p.first, (int)p.count, plan.pool_offset(), d_err,
-                tiles, (uint32_t)members, reg_stride, dev_stride);
+                tiles, (uint32_t)members, reg_stride, dev_stride, map, tg);
         } else {
             const size_t shm = sizeof(float2) * size + (size_t(1) << (geo.m - geo.L)) * sizeof(uint64_t);
             (p.matk ? kplain_k : kplain)<<<(unsigned)blocks, 256, shm, stream>>>(

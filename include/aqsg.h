@@ -378,6 +378,37 @@ int aqsg_batch_tuning(aqsg_batch b, int* fuse_qubits, int* tensor_cores);
 
 int aqsg_batch_free(aqsg_batch b);
 
+/* ---- noise by trajectories ------------------------------------------------ */
+
+/* A Pauli channel after every gate: each qubit the gate touches (targets and
+ * controls) independently gets X, Y or Z with probability p[0], p[1], p[2]
+ * (and is left alone with 1 - p[0] - p[1] - p[2]); p1 applies after gates
+ * on one qubit, p2 after gates on several.  Depolarizing noise of strength
+ * p is p/3 for each.  The reference reserves a class for noise (QNoise,
+ * include/quantum.h:475) but leaves it empty; this is the engine's own. */
+typedef struct aqsg_noise {
+    float p1[3];
+    float p2[3];
+} aqsg_noise;
+
+/* Trajectory `trajectory` of the noisy circuit: the ops with the Paulis it
+ * draws inserted right after the gates they follow.  Each draw is a
+ * counter-based function of (seed, trajectory, gate index, qubit), so a
+ * trajectory is the same circuit whatever else is drawn.  With out NULL,
+ * *out_count receives the trajectory's length; otherwise at most capacity
+ * ops are written (AQSG_ERR_OUT_OF_RANGE if they do not fit).  Probabilities
+ * must be >= 0 with sums <= 1 (AQSG_ERR_INVALID_ARGUMENT). */
+int aqsg_noise_trajectory(int n, const aqsg_op* ops, int count, const aqsg_noise* noise, uint64_t seed,
+                          uint64_t trajectory, aqsg_op* out, int capacity, int* out_count);
+
+/* <Z_q> and <Z_q Z_q+1> of the noisy circuit run from |0...0> (n <= 30),
+ * estimated by trajectories 0 .. trajectories - 1 of (seed) run as one
+ * batch (aqsg_batch_create): z[n], zz[n - 1] are the means over the
+ * trajectories, z_err / zz_err (may be NULL) their standard errors
+ * (sample standard deviation / sqrt(trajectories)). */
+int aqsg_noise_expect_z(aqsg_ctx ctx, int n, const aqsg_op* ops, int count, const aqsg_noise* noise,
+                        uint64_t seed, int trajectories, double* z, double* zz, double* z_err, double* zz_err);
+
 /* ---- serving runtime (a stream of independent requests) ------------------ */
 
 /* A request is one circuit run from |0...0> followed by `shots` seeded
