@@ -28,22 +28,15 @@ def small_circuit(n, seed):
 def test_sampler_matches_restatement(seed, traj):
     n = 4
     ops = small_circuit(n, 3)
-    nz = aq.Noise.pauli((0.05, 0.02, 0.08), (0.1, 0.05, 0.03))
-    got = aq.noise_trajectory(n, ops, nz, seed, traj)
-    want = onoise.trajectory_kinds(ops, (0.05, 0.02, 0.08), (0.1, 0.05, 0.03), seed, traj)
-    # walk the trajectory: source gates in order, each followed by its Paulis
-    i, inserted = 0, []
+    p1, p2 = (0.05, 0.02, 0.08), (0.1, 0.05, 0.03)
+    got = aq.noise_trajectory(n, ops, aq.Noise.pauli(p1, p2), seed, traj)
+    draws = onoise.trajectory_kinds(ops, p1, p2, seed, traj)
+    want = []  # (kind, first qubit) of each op: every source gate, then the Paulis drawn after it
     for g, op in enumerate(ops):
-        assert got[i].kind == op.kind and list(got[i].qubits) == list(op.qubits)
-        i += 1
-        while i < len(got) and (g + 1 == len(ops) or got[i].kind != ops[g + 1].kind
-                                or list(got[i].qubits) != list(ops[g + 1].qubits)) \
-                and got[i].kind in (aq.kinds.X, aq.kinds.Y, aq.kinds.Z) and got[i].num_qubits == 1 \
-                and len([w for w in want if w[0] == g]) > len([w for w in inserted if w[0] == g]):
-            inserted.append((g, got[i].qubits[0], got[i].kind))
-            i += 1
-    assert i == len(got)
-    assert inserted == want
+        want.append((op.kind, op.qubits[0]))
+        want += [(kind, q) for gg, q, kind in draws if gg == g]
+    assert [(o.kind, o.qubits[0]) for o in got] == want
+    assert len(draws) > 0
 
 
 def test_insertion_rates():
