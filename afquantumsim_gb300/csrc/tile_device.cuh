@@ -5,6 +5,8 @@
 
 #include <cuda_bf16.h>
 
+#include <type_traits>
+
 #include "aqsg_internal.h"
 #include "common.cuh"
 
@@ -285,6 +287,7 @@ __device__ __forceinline__ void tc_mma_ta(uint32_t d_tmem, uint32_t a_tmem, uint
 
 template <class LAY, class SYNC, int KQ>
 __device__ __forceinline__ void tc_apply_tm(float2* s, const TileOp& op, const TcSmem& t, TcPhase& ph) {
+    static_assert(std::is_same<LAY, TileLay<5, 2>>::value, "the index tables are byte offsets in 272-byte rows");
     constexpr uint32_t D = 1u << KQ, K = 2u * D, N = 2u * D;
     constexpr uint32_t blocks = 1u << (kTcTileBits - KQ - 7);  // 1, 2, 4 blocks of 128 data columns
     constexpr uint32_t bsplit = 2u * N * K;
@@ -294,8 +297,12 @@ __device__ __forceinline__ void tc_apply_tm(float2* s, const TileOp& op, const T
     const uint32_t tid = threadIdx.x & 255u, w = tid >> 5, lane = tid & 31u;
     const uint32_t q = w & 3u, h = w >> 2;
     const unsigned char* bsm = t.blob + op.mat;
+    // byte offsets in the padded tile (the layout is additive over disjoint
+    // index bits, so a data column's offset plus a matrix row's is the
+    // amplitude's): colbase[c], offr[r]
     const uint16_t* colbase = reinterpret_cast<const uint16_t*>(bsm + 2u * bsplit);
     const uint16_t* offr = colbase + 512;
+    unsigned char* sb = reinterpret_cast<unsigned char*>(s);
     const uint32_t lane_base = t.tmem + ((32u * q) << 16);
     const uint32_t r0 = KQ == 5 ? 16u * h : 0u;
 
@@ -310,7 +317,7 @@ __device__ __forceinline__ void tc_apply_tm(float2* s, const TileOp& op, const T
         uint32_t hi[RPT], lo[RPT];
 #pragma unroll
         for (uint32_t e = 0; e < RPT; ++e) {
-            const float2 x = s[LAY::at(jb[i] | (uint32_t)offr[r0 + e])];
+            const float2 x = *reinterpret_cast<const float2*>(sb + jb[i] + offr[r0 + e]);
             const __nv_bfloat162 bh = __float22bfloat162_rn(x);
             const float2 hf = __bfloat1622float2(bh);
             const __nv_bfloat162 bl = __float22bfloat162_rn(make_float2(x.x - hf.x, x.y - hf.y));
@@ -365,7 +372,7 @@ __device__ __forceinline__ void tc_apply_tm(float2* s, const TileOp& op, const T
             tc_ld_wait();
 #pragma unroll
             for (uint32_t e = 0; e < 8u; ++e)
-                s[LAY::at(jb[i] | (uint32_t)offr[r0 + c16 / 2u + e])] =
+                *reinterpret_cast<float2*>(sb + jb[i] + offr[r0 + c16 / 2u + e]) =
                     make_float2(__uint_as_float(v[2 * e]), __uint_as_float(v[2 * e + 1]));
         }
     }

@@ -704,9 +704,9 @@ static size_t tc_op_bytes(int k) {
 }
 
 // Index tables of a tensor-core op, appended to the blob after its B splits:
-// colbase[c] = tile index of data column c (c over the non-target tile
-// bits), offr[r] = tile-index bits of matrix row r (qubit ltb[0] is the
-// row's most significant bit).  Data column c is the MMA's M row c % 128 of
+// colbase[c] = byte offset of data column c in the padded tile (c over the
+// non-target tile bits), offr[r] = byte offset of matrix row r's index bits
+// (qubit ltb[0] is the row's most significant bit).  Data column c is the MMA's M row c % 128 of
 // block c / 128 and the TMEM lane of the thread that gathers it, so the 32
 // lanes of a warp read columns c .. c + 31 at once: the five lowest bits of
 // c go to the five non-target tile bits that spread those reads (and the
@@ -796,18 +796,23 @@ static void tc_tables_compute(const TileOp& t, unsigned char* out) {
         if ((best_sel >> i) & 1u) order.push_back(free_bits[i]);
     for (int i = 0; i < nf; ++i)
         if (!((best_sel >> i) & 1u)) order.push_back(free_bits[i]);
+    // both tables hold byte offsets in the padded tile layout of the
+    // tensor-core kernel (row stride kTcRowStride): it is additive over
+    // disjoint index bits, so colbase[c] + offr[r] addresses the amplitude
+    const uint32_t pad = (kTcRowStride - 256u) / 8u;
+    auto byte_at = [pad](uint32_t j) { return (uint16_t)(8u * (j + (j >> 5) * pad)); };
     const uint32_t cols = 1u << nf;
     for (uint32_t c = 0; c < cols; ++c) {
         uint32_t j = 0;
         for (int i = 0; i < nf; ++i) j |= ((c >> i) & 1u) << order[i];
-        const uint16_t v = (uint16_t)j;
+        const uint16_t v = byte_at(j);
         std::memcpy(out + 2 * c, &v, 2);
     }
     for (uint32_t r = 0; r < (1u << k); ++r) {
         uint32_t off = 0;
         for (int i = 0; i < k; ++i)
             if ((r >> (k - 1 - i)) & 1u) off |= 1u << t.ltb[i];
-        const uint16_t v = (uint16_t)off;
+        const uint16_t v = byte_at(off);
         std::memcpy(out + 1024 + 2 * r, &v, 2);
     }
 }

@@ -50,7 +50,8 @@ def parse_args():
     ap.add_argument("--dtype", choices=["c64", "c128"], default="c64")
     ap.add_argument("--mode", choices=["per_gate", "tiled"], default="per_gate")
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--only", choices=["fused_brickwork", "plain12", "vqe_batch", "vqe_ansatz", "serving", "qft_grid"],
+    ap.add_argument("--only", choices=["fused_brickwork", "fused_tc", "plain12", "vqe_batch", "vqe_ansatz", "serving",
+                                       "qft_grid"],
                     help="run one secondary workload alone (at --n qubits where it takes a size) "
                          "and print its JSON; for profiling")
     ap.add_argument("--depth", type=int, default=20,
@@ -326,6 +327,24 @@ def bench_fused_brickwork(ctx, st, stream, n, depth):
     res["max_rel_err_scaled"] = mx * np.sqrt(N)  # error relative to a typical |a| = 2^(-n/2)
     res["l2_bytes_note"] = "fused/tiled passes move 2 x 8 B x 2^n each"
     return res
+
+
+def bench_fused_tc(ctx, stream, n, depth):
+    """Only the compiled brick-work program on the tensor cores (two untimed
+    runs, then three timed): the launches a profiler of the tensor-core
+    tile pass captures, without the other modes of fused_brickwork."""
+    import afquantumsim_gb300 as aq
+    from afquantumsim_gb300 import circuits
+    prog = aq.Program(n, circuits.brickwork(n, depth, seed=4), aq.C64, max_qubits=5)
+    ctx.set_tensor_cores(True)
+    with aq.State(ctx, n, aq.C64) as st:
+        st.set_basis(0)
+        prog.run(st, aq.EXEC_TILED)
+        prog.run(st, aq.EXEC_TILED)
+        ms = _time_ms(stream, lambda: prog.run(st, aq.EXEC_TILED), 3)
+    fused, src = prog.info()
+    prog.free()
+    return {"workload": f"brickwork{n}x{depth}", "gates": src, "fused_ops": fused, "fused_tensor_core_ms": round(ms, 2)}
 
 
 def bench_qft_grid(ctx, stream, sizes=((24, "c64"), (28, "c64"), (24, "c128"), (28, "c128"), (30, "c128"))):
@@ -907,6 +926,8 @@ def run_only(args):
     if args.only == "fused_brickwork":
         with aq.State(ctx, args.n, aq.C64) as st:
             res = bench_fused_brickwork(ctx, st, stream, args.n, args.depth)
+    elif args.only == "fused_tc":
+        res = bench_fused_tc(ctx, stream, args.n, args.depth)
     elif args.only == "plain12":
         res = bench_plain12(ctx, stream)
     elif args.only == "qft_grid":
