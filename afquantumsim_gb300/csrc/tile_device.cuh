@@ -176,7 +176,7 @@ __device__ __forceinline__ void fence_async_smem() {
 // K-direction stride 128 B, N-direction stride (K/8) * 128 B.
 
 constexpr int kTcTileBits = 12;
-constexpr int kTcThreads = 512;                    // compute threads: 16 warps in 2 groups of 8
+constexpr int kTcThreads = 768;                    // compute threads: 24 warps in 3 groups of 8
 constexpr uint32_t kTcTmemCols = 128;              // per compute group: A hi, A lo, D (32 + 32 + 64)
 // A pass's tensor-core operands (per op: B hi and lo splits, then the index
 // tables) are loaded into shared memory once per CTA; at most this many bytes

@@ -161,10 +161,10 @@ k_tile_stream_multi(typename Cx<R>::T* __restrict__ sv0, uint64_t reg_stride, co
 
 constexpr uint32_t kRowBytes = 256;
 constexpr uint32_t kRows = 128;                     // rows of a 2^12-amplitude c64 tile
-constexpr int kTcCta = kTcThreads + 32;             // 16 compute warps + 1 producer warp
-                                                    // (17 warps: at most 96 registers per thread)
-constexpr int kTcGroups = 2;                        // compute groups (tiles in flight) per CTA
-constexpr int kTcMaxOps = 48;                       // op tables up to this size go to shared memory
+constexpr int kTcCta = kTcThreads + 32;             // 24 compute warps + 1 producer warp
+                                                    // (25 warps: at most 72 registers per thread)
+constexpr int kTcGroups = 3;                        // compute groups (tiles in flight) per CTA
+constexpr int kTcMaxOps = 24;                       // op tables up to this size go to shared memory
 constexpr uint32_t kTcRowStride = 272u;             // padded tile row in the tensor-core kernel
 static_assert(sizeof(TileOp) % 16 == 0, "op tables are bulk-copied: 16-byte multiples");
 
@@ -216,19 +216,19 @@ __device__ __forceinline__ void tma_load_tile(void* dst, const CUtensorMap* map,
     }
 }
 
-// Shared memory of the tensor-core streaming kernel: four tile buffers (the
-// two compute groups' tiles and two loading), the row offsets, barriers, the
+// Shared memory of the tensor-core streaming kernel: five tile buffers (the
+// three compute groups' tiles and two loading), the row offsets, barriers, the
 // op table and the pass's operand blob (the MMAs' data operand lives in
 // tensor memory).  Rows are padded by 16 bytes (a 272-byte stride) so the
 // operand gathers of rows that share their low index bits spread over the
 // banks.
 template <int GROUPS>
 struct TcStreamSmemT {
-    static constexpr int kBufs = 4;
+    static constexpr int kBufs = 5;
     static constexpr uint32_t kRowStride = kTcRowStride;
     static constexpr uint32_t kBufBytes = kRows * kRowStride;          // 34 KiB
     static constexpr uint32_t kRowOff = kBufs * kBufBytes;              // kRows x u64
-    static constexpr uint32_t kBars = kRowOff + kRows * 8u;             // full[4] done[4] mma[2] blob
+    static constexpr uint32_t kBars = kRowOff + kRows * 8u;             // full[5] done[5] mma[3] blob
     static constexpr uint32_t kTmemSlot = kBars + 16u * 8u;
     static constexpr uint32_t kOps = (kTmemSlot + 16u + 127u) & ~127u;  // kTcMaxOps TileOps
     static constexpr uint32_t kBlob = (kOps + kTcMaxOps * (uint32_t)sizeof(TileOp) + 1023u) & ~1023u;
@@ -236,6 +236,10 @@ struct TcStreamSmemT {
     static_assert(kBytes <= 232448u, "more shared memory than a CTA may have");
 };
 using TcStreamSmem = TcStreamSmemT<kTcGroups>;
+// tensor-memory columns a CTA allocates: the groups' columns, rounded up to
+// a power of two
+constexpr uint32_t kTcTmemAlloc = 512;
+static_assert(kTcTmemCols * kTcGroups <= kTcTmemAlloc, "tensor memory of the compute groups");
 
 // any(v) over the N threads of this thread's compute group (named barrier
 // 1 + group, as GroupSync)
@@ -254,16 +258,17 @@ __device__ __forceinline__ bool group_any(bool v) {
 // Tensor-core streaming passes (c64, 4096-amplitude tiles).  A persistent
 // CTA per SM walks its tiles; a tile is 128 rows of 256 contiguous bytes
 // (the 5 low index bits) at the row offsets of the pass's 7 high tile bits.
-// Warp 16 is the producer: it copies tiles in 16-byte cp.async chunks into
-// four shared-memory buffers (full[b] completes when all 32 lanes' chunks
-// have landed; many small requests stay in flight without the per-request
-// cost of bulk copies), and loads the next tile into a buffer as soon as the
-// compute group that ran its tile has written it back with 128-bit stores
-// and released it (done[b]).  The 16 compute warps form
-// GROUPS groups; group g runs the pass's ops on the CTA's tiles g, g + GROUPS,
-// ... with its own named barrier, A operand, tensor-memory columns and MMA
-// barrier, so one group's operand gathers and write-backs overlap the other
-// group's MMAs and waits.  The pass's operand blob and op table are
+// Warp 24 is the producer: it loads each tile into one of five
+// shared-memory buffers with one TMA copy (full[b] completes on its byte
+// count), or, for a pass whose tile bits the tensor map cannot describe, in
+// 16-byte cp.async chunks (full[b] completes when all 32 lanes' chunks have
+// landed), and loads the next tile into a buffer as soon as the compute
+// group that ran its tile has written it back with 128-bit stores and
+// released it (done[b]).  The 24 compute warps form GROUPS = 3 groups of 8;
+// group g runs the pass's ops on the CTA's tiles g, g + GROUPS, ... with its
+// own named barrier, tensor-memory columns and MMA barrier, so the groups'
+// gathers, MMAs, waits and write-backs overlap one another (three groups
+// instead of two took the fused 30-qubit brick-work from 164 to 132 ms).  The pass's operand blob and op table are
 // bulk-loaded into shared memory.  Every wait is bounded: one that gives up
 // sets the error flag and the CTA winds down.
 //
@@ -386,7 +391,7 @@ k_stream_tc(float2* __restrict__ sv0, const TileGeom g, const unsigned char* __r
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                     ::"r"(smem_u32(smem_raw + SM::kTmemSlot)), "r"(kTcTmemCols * GROUPS));
+                     ::"r"(smem_u32(smem_raw + SM::kTmemSlot)), "r"(kTcTmemAlloc));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
@@ -512,7 +517,7 @@ k_stream_tc(float2* __restrict__ sv0, const TileGeom g, const unsigned char* __r
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(
                          *reinterpret_cast<volatile uint32_t*>(smem_raw + SM::kTmemSlot)),
-                     "r"(kTcTmemCols * GROUPS));
+                     "r"(kTcTmemAlloc));
     }
 }
 
