@@ -177,6 +177,23 @@ struct Fix {
     }
 };
 
+// The same in 32-bit arithmetic, for registers of at most 2^32 amplitudes
+// (half the integer instructions of the 64-bit form per index).
+template <int NF>
+struct Fix32 {
+    uint32_t pos[NF > 0 ? NF : 1];
+    uint32_t val;
+    __device__ __forceinline__ uint64_t expand(uint64_t k64) const {
+        uint32_t k = (uint32_t)k64;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            const uint32_t lo = k & ((1u << pos[f]) - 1u);
+            k = ((k - lo) << 1) | lo;
+        }
+        return (uint64_t)(k | val);
+    }
+};
+
 // Runtime-count variant for ops with many controls.
 struct FixN {
     int nf;

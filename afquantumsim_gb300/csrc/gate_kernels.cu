@@ -330,10 +330,10 @@ static FixedBits make_fixed(uint64_t mask, uint64_t val) {
 }
 
 template <int NF>
-static Fix<NF> to_fix(const FixedBits& f) {
-    Fix<NF> x;
+static Fix32<NF> to_fix32(const FixedBits& f) {
+    Fix32<NF> x;
     for (int i = 0; i < NF; ++i) x.pos[i] = f.pos[i];
-    x.val = f.val;
+    x.val = (uint32_t)f.val;
     return x;
 }
 
@@ -349,14 +349,19 @@ static inline unsigned grid_for(uint64_t units, int per_block) {
     return (unsigned)((units + per_block - 1) / per_block);
 }
 
-// Calls fn(fixer) with the narrowest fixer type for f.nf.
+// Calls fn(fixer) with the narrowest fixer type for f.nf: 32-bit index
+// arithmetic for registers of up to 32 qubits, 64-bit above.
 template <typename Fn>
-static void with_fix(const FixedBits& f, Fn&& fn) {
+static void with_fix(const FixedBits& f, int n, Fn&& fn) {
+    if (n > 32) {
+        fn(to_fixn(f));
+        return;
+    }
     switch (f.nf) {
-        case 1: fn(to_fix<1>(f)); break;
-        case 2: fn(to_fix<2>(f)); break;
-        case 3: fn(to_fix<3>(f)); break;
-        case 4: fn(to_fix<4>(f)); break;
+        case 1: fn(to_fix32<1>(f)); break;
+        case 2: fn(to_fix32<2>(f)); break;
+        case 3: fn(to_fix32<3>(f)); break;
+        case 4: fn(to_fix32<4>(f)); break;
         default: fn(to_fixn(f)); break;
     }
 }
@@ -387,7 +392,7 @@ static void launch_pair_v(aqsg_state_s* st, const FixedBits& f, uint64_t tmask, 
                           uint64_t units, const M2<R>& m) {
     using T = typename Cx<R>::T;
     const unsigned grid = grid_for(units, kThreads * 2);
-    with_fix(f, [&](auto fx) {
+    with_fix(f, st->n, [&](auto fx) {
         k_pair<R, VEC, PACKED, OP, decltype(fx)><<<grid, kThreads, 0, st->ctx->stream>>>(
             (T*)st->d, fx, tmask, amask, units, m);
     });
@@ -445,13 +450,13 @@ static int launch_typed(aqsg_state_s* st, const LOp& op) {
             if (vec2) {
                 units >>= 1;
                 const unsigned grid = grid_for(units, kThreads * 4);
-                with_fix(f, [&](auto fx) {
+                with_fix(f, st->n, [&](auto fx) {
                     k_diag1<R, (sizeof(R) == 4 ? 2 : 1), decltype(fx)>
                         <<<grid, kThreads, 0, st->ctx->stream>>>((T*)st->d, fx, units, ph, phd);
                 });
             } else {
                 const unsigned grid = grid_for(units, kThreads * 4);
-                with_fix(f, [&](auto fx) {
+                with_fix(f, st->n, [&](auto fx) {
                     k_diag1<R, 1, decltype(fx)><<<grid, kThreads, 0, st->ctx->stream>>>(
                         (T*)st->d, fx, units, ph, phd);
                 });
@@ -466,13 +471,13 @@ static int launch_typed(aqsg_state_s* st, const LOp& op) {
             if (vec2) {
                 units >>= 1;
                 const unsigned grid = grid_for(units, kThreads * 2);
-                with_fix(f, [&](auto fx) {
+                with_fix(f, st->n, [&](auto fx) {
                     k_swap<R, (sizeof(R) == 4 ? 2 : 1), decltype(fx)>
                         <<<grid, kThreads, 0, st->ctx->stream>>>((T*)st->d, fx, ma | mb, units);
                 });
             } else {
                 const unsigned grid = grid_for(units, kThreads * 2);
-                with_fix(f, [&](auto fx) {
+                with_fix(f, st->n, [&](auto fx) {
                     k_swap<R, 1, decltype(fx)><<<grid, kThreads, 0, st->ctx->stream>>>(
                         (T*)st->d, fx, ma | mb, units);
                 });
@@ -496,7 +501,7 @@ static int launch_typed(aqsg_state_s* st, const LOp& op) {
                     mk->off[r] = off;
                 }
                 for (int e = 0; e < D * D; ++e) mk->m[e] = cval<R>(op.mk[2 * e], op.mk[2 * e + 1]);
-                with_fix(f, [&](auto fx) {
+                with_fix(f, st->n, [&](auto fx) {
                     k_matk<R, K, decltype(fx)><<<grid, kThreads, 0, st->ctx->stream>>>(
                         (T*)st->d, fx, units, *mk);
                 });
