@@ -51,7 +51,7 @@ def parse_args():
     ap.add_argument("--mode", choices=["per_gate", "tiled"], default="per_gate")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--only", choices=["fused_brickwork", "fused_tc", "plain12", "vqe_batch", "vqe_ansatz", "serving",
-                                       "qft_grid"],
+                                       "qft_grid", "noise"],
                     help="run one secondary workload alone (at --n qubits where it takes a size) "
                          "and print its JSON; for profiling")
     ap.add_argument("--depth", type=int, default=20,
@@ -345,6 +345,28 @@ def bench_fused_tc(ctx, stream, n, depth):
     fused, src = prog.info()
     prog.free()
     return {"workload": f"brickwork{n}x{depth}", "gates": src, "fused_ops": fused, "fused_tensor_core_ms": round(ms, 2)}
+
+
+def bench_noise(ctx, n=12, layers=8, trajectories=4096, seed=7):
+    """Noise by trajectories: a hardware-efficient ansatz (RotY + RotZ per
+    qubit, CX ring; seeded angles) under depolarizing noise (p = 1e-3 after
+    one-qubit gates, 1e-2 per qubit after CX), <Z_q> and <Z_q Z_q+1> averaged
+    over `trajectories` seeded trajectories run as one batch; wall time of
+    aqsg_noise_expect_z (sampling, batch planning, the run and the averages)."""
+    import time as _t
+
+    import afquantumsim_gb300 as aq
+    from afquantumsim_gb300 import circuits
+    params = np.random.default_rng(seed).uniform(-np.pi, np.pi, size=(layers, n, 2)).astype(np.float32)
+    ops = circuits.vqe_ansatz(n, layers, params)
+    noise = aq.Noise.depolarizing(1e-3, 1e-2)
+    aq.noisy_expect_z(ctx, n, ops, noise, seed, 64)  # warm-up (tuning caches, kernels)
+    t0 = _t.perf_counter()
+    z, zz, ze, zze = aq.noisy_expect_z(ctx, n, ops, noise, seed, trajectories)
+    dt = _t.perf_counter() - t0
+    return {"workload": f"ansatz{n}x{layers}_depolarizing", "gates": len(ops), "trajectories": trajectories,
+            "seconds": round(dt, 3), "trajectories_per_s": round(trajectories / dt, 1),
+            "max_std_err_z": float(np.max(ze)), "mean_z": float(np.mean(z))}
 
 
 def bench_qft_grid(ctx, stream, sizes=((24, "c64"), (28, "c64"), (24, "c128"), (28, "c128"), (30, "c128"))):
@@ -796,6 +818,7 @@ def run_ours(args, rank, world, local_rank):
         extras["qft_grid"] = bench_qft_grid(ctx, stream)
         extras["plain12"] = bench_plain12(ctx, stream)
         extras["vqe_batch"] = bench_vqe_batch(ctx)
+        extras["noise"] = bench_noise(ctx)
         if args.dtype == "c64":
             extras["serving"] = bench_serving(ctx)
 
@@ -930,6 +953,8 @@ def run_only(args):
         res = bench_fused_tc(ctx, stream, args.n, args.depth)
     elif args.only == "plain12":
         res = bench_plain12(ctx, stream)
+    elif args.only == "noise":
+        res = bench_noise(ctx)
     elif args.only == "qft_grid":
         res = bench_qft_grid(ctx, stream)
     elif args.only == "vqe_batch":
