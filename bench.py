@@ -757,25 +757,48 @@ def run_ours(args, rank, world, local_rank):
     st.download_async_ptr(host_out.data_ptr())
     ctx.synchronize()
     d2h_s = time.perf_counter() - t_c
+    # events on each register's stream around its gate batches, the first
+    # upload and the last result copy: where the end-to-end time goes
+    lane_streams = [stream, torch.cuda.ExternalStream(ctx2.stream_handle(), device=dev)]
+
+    def mark(li):
+        e = torch.cuda.Event(enable_timing=True)
+        e.record(lane_streams[li])
+        return e
+
+    gate_ev = []
     if world > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
     for step in range(e2e_steps):
-        c, r, ho = lanes[step % 2]
+        li = step % 2
+        c, r, ho = lanes[li]
         c.synchronize()  # this register's previous step (its result copy) is done
+        if step == 0:
+            up0 = mark(li)
         r.upload_ptr(host_in.data_ptr())
         if step > 0:
             pc, pr, pho = lanes[(step - 1) % 2]
             c.after(pc)  # after the previous step's gates (its queue holds nothing else)
+            g0 = mark(li)
             r.apply(ops, mode)
+            gate_ev.append((g0, mark(li)))
             pr.download_async_ptr(pho.data_ptr())  # previous result, under this step's gates
         else:
+            g0 = mark(li)
             r.apply(ops, mode)
-    c, r, ho = lanes[(e2e_steps - 1) % 2]
+            gate_ev.append((g0, mark(li)))
+    li = (e2e_steps - 1) % 2
+    c, r, ho = lanes[li]
     r.download_async_ptr(ho.data_ptr())
+    down_end = mark(li)
     ctx.synchronize()
     ctx2.synchronize()
     e2e_s = time.perf_counter() - t0
+    e2e_gates_ms = sum(a.elapsed_time(b) for a, b in gate_ev)
+    e2e_span_ms = up0.elapsed_time(down_end)
+    e2e_first_upload_ms = up0.elapsed_time(gate_ev[0][0])
+    e2e_last_copy_ms = gate_ev[-1][1].elapsed_time(down_end)
     st2.free()
     ctx2.close()
     if world > 1:
@@ -786,6 +809,10 @@ def run_ours(args, rank, world, local_rank):
            "h2d_bytes_per_step": N * amp_b, "d2h_bytes_per_step": N * amp_b,
            "ms_per_step": round(e2e_s / e2e_steps * 1e3, 3), "steps": e2e_steps,
            "h2d_gbs": round(N * amp_b / h2d_s / 1e9, 1), "d2h_gbs": round(N * amp_b / d2h_s / 1e9, 1),
+           # device time of the loop (first upload to last result copy), of
+           # its gate batches, and the copies that no gates hide
+           "device_span_ms": round(e2e_span_ms, 1), "gates_ms_per_step": round(e2e_gates_ms / e2e_steps, 2),
+           "first_upload_ms": round(e2e_first_upload_ms, 1), "last_copy_ms": round(e2e_last_copy_ms, 1),
            "pipeline": "two registers on two streams, gates of consecutive steps ordered (aqsg_ctx_after); "
                        "each step uploads its input and reads its result under the other register's gates"}
 
