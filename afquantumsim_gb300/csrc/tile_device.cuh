@@ -146,6 +146,10 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
 }
 // one arrival on `bar` once this thread's earlier cp.async copies have landed
 // (the barrier's expected count includes it)
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_arrive(uint64_t* bar) {
     asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
@@ -529,72 +533,214 @@ __device__ __forceinline__ bool r_on(uint32_t em, int e) {
     return !P || ((em >> e) & 1u);
 }
 
-template <typename T, int RB, int I, bool P>
-__device__ __forceinline__ void r_mat2c(T (&v)[1 << RB], const T* c, uint32_t em) {
-    const T m00 = c[0], m01 = c[1], m10 = c[2], m11 = c[3];
+// In-place updates of register-held amplitudes, written as PTX whose
+// outputs are tied to their inputs.  Each op of a register phase rewrites
+// the same 2^RB registers; written as plain expressions, the compiler put
+// an op's results in fresh registers and copied them back before the next
+// op (MOV/IMAD moves were ~40 % of a pass's instructions).  The arithmetic
+// is the same: products rounded once, sums fused (mul.rn + fma.rn).
+//
+// (a, b) <- (m00 a + m01 b, m10 a + m11 b) on one real component
+__device__ __forceinline__ void ip_rot(float& a, float& b, float m00, float m01, float m10, float m11) {
+    asm("{\n\t.reg .f32 t0, t1;\n\t"
+        "mul.rn.f32 t0, %3, %1;\n\t"
+        "mul.rn.f32 t1, %4, %0;\n\t"
+        "fma.rn.f32 %0, %2, %0, t0;\n\t"
+        "fma.rn.f32 %1, %5, %1, t1;\n\t}"
+        : "+f"(a), "+f"(b)
+        : "f"(m00), "f"(m01), "f"(m10), "f"(m11));
+}
+__device__ __forceinline__ void ip_rot(double& a, double& b, double m00, double m01, double m10, double m11) {
+    asm("{\n\t.reg .f64 t0, t1;\n\t"
+        "mul.rn.f64 t0, %3, %1;\n\t"
+        "mul.rn.f64 t1, %4, %0;\n\t"
+        "fma.rn.f64 %0, %2, %0, t0;\n\t"
+        "fma.rn.f64 %1, %5, %1, t1;\n\t}"
+        : "+d"(a), "+d"(b)
+        : "d"(m00), "d"(m01), "d"(m10), "d"(m11));
+}
+// (x + iy) <- (px + i py)(x + iy); npy = -py
+__device__ __forceinline__ void ip_cmul(float& x, float& y, float px, float py, float npy) {
+    asm("{\n\t.reg .f32 t0, t1;\n\t"
+        "mul.rn.f32 t0, %4, %1;\n\t"
+        "mul.rn.f32 t1, %3, %0;\n\t"
+        "fma.rn.f32 %0, %2, %0, t0;\n\t"
+        "fma.rn.f32 %1, %2, %1, t1;\n\t}"
+        : "+f"(x), "+f"(y)
+        : "f"(px), "f"(py), "f"(npy));
+}
+__device__ __forceinline__ void ip_cmul(double& x, double& y, double px, double py, double npy) {
+    asm("{\n\t.reg .f64 t0, t1;\n\t"
+        "mul.rn.f64 t0, %4, %1;\n\t"
+        "mul.rn.f64 t1, %3, %0;\n\t"
+        "fma.rn.f64 %0, %2, %0, t0;\n\t"
+        "fma.rn.f64 %1, %2, %1, t1;\n\t}"
+        : "+d"(x), "+d"(y)
+        : "d"(px), "d"(py), "d"(npy));
+}
+// exchange a and b; where c only.  Written as XOR exchanges, which keep
+// both values in their registers: a permuting op then needs no copies in
+// the paths of the other ops of a register phase.
+__device__ __forceinline__ void ip_swap(float& a, float& b) {
+    asm("{\n\txor.b32 %0, %0, %1;\n\txor.b32 %1, %1, %0;\n\txor.b32 %0, %0, %1;\n\t}" : "+f"(a), "+f"(b));
+}
+__device__ __forceinline__ void ip_swap(double& a, double& b) {
+    asm("{\n\txor.b64 %0, %0, %1;\n\txor.b64 %1, %1, %0;\n\txor.b64 %0, %0, %1;\n\t}" : "+d"(a), "+d"(b));
+}
+// m: all ones to exchange, zero to keep
+__device__ __forceinline__ void ip_cswap(float& a, float& b, bool c) {
+    const uint32_t m = 0u - (uint32_t)c;
+    asm("{\n\t.reg .b32 d;\n\txor.b32 d, %0, %1;\n\tand.b32 d, d, %2;\n\t"
+        "xor.b32 %0, %0, d;\n\txor.b32 %1, %1, d;\n\t}"
+        : "+f"(a), "+f"(b)
+        : "r"(m));
+}
+__device__ __forceinline__ void ip_cswap(double& a, double& b, bool c) {
+    const uint64_t m = 0ull - (uint64_t)c;
+    asm("{\n\t.reg .b64 d;\n\txor.b64 d, %0, %1;\n\tand.b64 d, d, %2;\n\t"
+        "xor.b64 %0, %0, d;\n\txor.b64 %1, %1, d;\n\t}"
+        : "+d"(a), "+d"(b)
+        : "l"(m));
+}
+template <typename T>
+__device__ __forceinline__ void ip_swap2(T& a, T& b) {
+    ip_swap(a.x, b.x);
+    ip_swap(a.y, b.y);
+}
+template <typename T>
+__device__ __forceinline__ void ip_cswap2(T& a, T& b, bool c) {
+    ip_cswap(a.x, b.x, c);
+    ip_cswap(a.y, b.y, c);
+}
+
+// complex 2x2: (a, b) <- (m00 a + m01 b, m10 a + m11 b).  Every output
+// needs every input, so three terms of each output go to a temporary first
+// and each output's last term is the one with its own input.
+// q = {m00.x, m00.y, m01.x, m01.y, m10.x, m10.y, m11.x, m11.y},
+// nq = {-m00.y, -m01.y, -m10.y, -m11.y}.
+#define AQSG_IP_CMAT2_BODY(TY)                                               \
+    "{\n\t.reg ." TY " ax, ay, bx, by;\n\t"                                  \
+    "mul.rn." TY " ax, %6, %2;\n\t"                                          \
+    "fma.rn." TY " ax, %13, %3, ax;\n\t"                                     \
+    "fma.rn." TY " ax, %12, %1, ax;\n\t"                                     \
+    "mul.rn." TY " ay, %6, %3;\n\t"                                          \
+    "fma.rn." TY " ay, %7, %2, ay;\n\t"                                      \
+    "fma.rn." TY " ay, %5, %0, ay;\n\t"                                      \
+    "mul.rn." TY " bx, %8, %0;\n\t"                                          \
+    "fma.rn." TY " bx, %14, %1, bx;\n\t"                                     \
+    "fma.rn." TY " bx, %15, %3, bx;\n\t"                                     \
+    "mul.rn." TY " by, %8, %1;\n\t"                                          \
+    "fma.rn." TY " by, %9, %0, by;\n\t"                                      \
+    "fma.rn." TY " by, %11, %2, by;\n\t"                                     \
+    "fma.rn." TY " %0, %4, %0, ax;\n\t"                                      \
+    "fma.rn." TY " %1, %4, %1, ay;\n\t"                                      \
+    "fma.rn." TY " %2, %10, %2, bx;\n\t"                                     \
+    "fma.rn." TY " %3, %10, %3, by;\n\t}"
+__device__ __forceinline__ void ip_cmat2(float2& a, float2& b, const float (&q)[8], const float (&nq)[4]) {
+    asm(AQSG_IP_CMAT2_BODY("f32")
+        : "+f"(a.x), "+f"(a.y), "+f"(b.x), "+f"(b.y)
+        : "f"(q[0]), "f"(q[1]), "f"(q[2]), "f"(q[3]), "f"(q[4]), "f"(q[5]), "f"(q[6]), "f"(q[7]), "f"(nq[0]),
+          "f"(nq[1]), "f"(nq[2]), "f"(nq[3]));
+}
+__device__ __forceinline__ void ip_cmat2(double2& a, double2& b, const double (&q)[8], const double (&nq)[4]) {
+    asm(AQSG_IP_CMAT2_BODY("f64")
+        : "+d"(a.x), "+d"(a.y), "+d"(b.x), "+d"(b.y)
+        : "d"(q[0]), "d"(q[1]), "d"(q[2]), "d"(q[3]), "d"(q[4]), "d"(q[5]), "d"(q[6]), "d"(q[7]), "d"(nq[0]),
+          "d"(nq[1]), "d"(nq[2]), "d"(nq[3]));
+}
+#undef AQSG_IP_CMAT2_BODY
+
+// The leaves below apply one op to the SL slots a thread holds (v[sl]),
+// to slot sl only where on[sl] (its control on the slot's other bits
+// holds), and within a slot to the elements of mask em where P.
+template <typename T, int RB, int I, bool P, int SL, typename R>
+__device__ __forceinline__ void r_mat2c(T (&v)[SL][1 << RB], const bool (&on)[SL], const R (&q)[8], uint32_t em) {
+    const R nq[4] = {-q[1], -q[3], -q[5], -q[7]};
 #pragma unroll
-    for (int e = 0; e < (1 << RB); ++e) {
-        if (e & (1 << I)) continue;
-        if (!r_on<P>(em, e)) continue;
-        const T a = v[e], b = v[e | (1 << I)];
-        v[e] = cmul2(m00, a, m01, b);
-        v[e | (1 << I)] = cmul2(m10, a, m11, b);
+    for (int sl = 0; sl < SL; ++sl) {
+        if (!on[sl]) continue;
+#pragma unroll
+        for (int e = 0; e < (1 << RB); ++e) {
+            if (e & (1 << I)) continue;
+            if (!r_on<P>(em, e)) continue;
+            ip_cmat2(v[sl][e], v[sl][e | (1 << I)], q, nq);
+        }
     }
 }
 
-template <typename T, typename R, int RB, int I, bool P>
-__device__ __forceinline__ void r_mat2r(T (&v)[1 << RB], const R* r, uint32_t em) {
-    const R m00 = r[0], m01 = r[1], m10 = r[2], m11 = r[3];
+// r = {m00, m01, m10, m11}, real
+template <typename T, typename R, int RB, int I, bool P, int SL>
+__device__ __forceinline__ void r_mat2r(T (&v)[SL][1 << RB], const bool (&on)[SL], const R (&r)[4], uint32_t em) {
 #pragma unroll
-    for (int e = 0; e < (1 << RB); ++e) {
-        if (e & (1 << I)) continue;
-        if (!r_on<P>(em, e)) continue;
-        const T a = v[e], b = v[e | (1 << I)];
-        v[e].x = m00 * a.x + m01 * b.x;
-        v[e].y = m00 * a.y + m01 * b.y;
-        v[e | (1 << I)].x = m10 * a.x + m11 * b.x;
-        v[e | (1 << I)].y = m10 * a.y + m11 * b.y;
+    for (int sl = 0; sl < SL; ++sl) {
+        if (!on[sl]) continue;
+#pragma unroll
+        for (int e = 0; e < (1 << RB); ++e) {
+            if (e & (1 << I)) continue;
+            if (!r_on<P>(em, e)) continue;
+            ip_rot(v[sl][e].x, v[sl][e | (1 << I)].x, r[0], r[1], r[2], r[3]);
+            ip_rot(v[sl][e].y, v[sl][e | (1 << I)].y, r[0], r[1], r[2], r[3]);
+        }
     }
 }
 
-template <typename T, int RB, int I, bool P>
-__device__ __forceinline__ void r_perm(T (&v)[1 << RB], uint32_t pm) {
+// pm[sl]: the elements (target bit 0) of slot sl whose pair is exchanged
+template <typename T, int RB, int I, bool P, int SL>
+__device__ __forceinline__ void r_perm(T (&v)[SL][1 << RB], const bool (&on)[SL], const uint32_t (&pm)[SL]) {
 #pragma unroll
-    for (int e = 0; e < (1 << RB); ++e) {
-        if (e & (1 << I)) continue;
-        const bool on = r_on<P>(pm, e);
-        const T a = v[e], b = v[e | (1 << I)];
-        v[e] = on ? b : a;
-        v[e | (1 << I)] = on ? a : b;
+    for (int sl = 0; sl < SL; ++sl) {
+        if (!on[sl]) continue;
+#pragma unroll
+        for (int e = 0; e < (1 << RB); ++e) {
+            if (e & (1 << I)) continue;
+            if (P) ip_cswap2(v[sl][e], v[sl][e | (1 << I)], (pm[sl] >> e) & 1u);
+            else ip_swap2(v[sl][e], v[sl][e | (1 << I)]);
+        }
     }
 }
 
-template <typename T, int RB, int I, int J, bool P>
-__device__ __forceinline__ void r_swap(T (&v)[1 << RB], uint32_t em) {
+template <typename T, int RB, int I, int J, bool P, int SL>
+__device__ __forceinline__ void r_swap(T (&v)[SL][1 << RB], const bool (&on)[SL], uint32_t em) {
 #pragma unroll
-    for (int e = 0; e < (1 << RB); ++e) {
-        if ((e & (1 << I)) || !(e & (1 << J))) continue;
-        const int f = e ^ (1 << I) ^ (1 << J);
-        const bool on = r_on<P>(em, e);
-        const T a = v[e], b = v[f];
-        v[e] = on ? b : a;
-        v[f] = on ? a : b;
+    for (int sl = 0; sl < SL; ++sl) {
+        if (!on[sl]) continue;
+#pragma unroll
+        for (int e = 0; e < (1 << RB); ++e) {
+            if ((e & (1 << I)) || !(e & (1 << J))) continue;
+            const int f = e ^ (1 << I) ^ (1 << J);
+            if (P) ip_cswap2(v[sl][e], v[sl][f], (em >> e) & 1u);
+            else ip_swap2(v[sl][e], v[sl][f]);
+        }
     }
 }
 
-template <typename T, int RB, bool P>
-__device__ __forceinline__ void r_diag(T (&v)[1 << RB], T ph, uint32_t em) {
+// ph[sl]: the phase of slot sl
+template <typename T, int RB, bool P, int SL>
+__device__ __forceinline__ void r_diag(T (&v)[SL][1 << RB], const bool (&on)[SL], const T (&ph)[SL], uint32_t em) {
 #pragma unroll
-    for (int e = 0; e < (1 << RB); ++e)
-        if (r_on<P>(em, e)) v[e] = cmul(ph, v[e]);
+    for (int sl = 0; sl < SL; ++sl) {
+        if (!on[sl]) continue;
+        const auto npy = -ph[sl].y;
+#pragma unroll
+        for (int e = 0; e < (1 << RB); ++e)
+            if (r_on<P>(em, e)) ip_cmul(v[sl][e].x, v[sl][e].y, ph[sl].x, ph[sl].y, npy);
+    }
 }
 
-template <typename T, int RB, int I, bool P>
-__device__ __forceinline__ void r_diagr(T (&v)[1 << RB], const T* c, uint32_t em) {
-    const T c0 = c[0], c1 = c[1];
+// c = {c0.x, c0.y, c1.x, c1.y}: c0 where register bit I is 0, c1 where 1
+template <typename T, int RB, int I, bool P, int SL, typename R>
+__device__ __forceinline__ void r_diagr(T (&v)[SL][1 << RB], const bool (&on)[SL], const R (&c)[4], uint32_t em) {
+    const R n0 = -c[1], n1 = -c[3];
 #pragma unroll
-    for (int e = 0; e < (1 << RB); ++e)
-        if (r_on<P>(em, e)) v[e] = cmul(((e >> I) & 1) ? c1 : c0, v[e]);
+    for (int sl = 0; sl < SL; ++sl) {
+        if (!on[sl]) continue;
+#pragma unroll
+        for (int e = 0; e < (1 << RB); ++e) {
+            if (!r_on<P>(em, e)) continue;
+            if ((e >> I) & 1) ip_cmul(v[sl][e].x, v[sl][e].y, c[2], c[3], n1);
+            else ip_cmul(v[sl][e].x, v[sl][e].y, c[0], c[1], n0);
+        }
+    }
 }
 
 template <int RM, int K>
@@ -608,31 +754,37 @@ __device__ __forceinline__ constexpr int r_dep(int r) {  // matrix index -> slot
     return out;
 }
 
-template <typename T, int RB, int RM>
-__device__ __forceinline__ void r_matk(T (&v)[1 << RB], const T* __restrict__ mat, uint32_t em) {
+template <typename T, int RB, int RM, int SL>
+__device__ __forceinline__ void r_matk(T (&vv)[SL][1 << RB], const bool (&on)[SL], const T* __restrict__ mat,
+                                       uint32_t em) {
     constexpr int K = __builtin_popcount(RM), D = 1 << K, E = 1 << RB;
-    T a[E];
 #pragma unroll
-    for (int e = 0; e < E; ++e) a[e] = v[e];
+    for (int sl = 0; sl < SL; ++sl) {
+        if (!on[sl]) continue;
+        T (&v)[E] = vv[sl];
+        T a[E];
 #pragma unroll
-    for (int r = 0; r < D; ++r) {
-        T row[D];
+        for (int e = 0; e < E; ++e) a[e] = v[e];
 #pragma unroll
-        for (int c = 0; c < D; ++c) row[c] = mat[r * D + c];
+        for (int r = 0; r < D; ++r) {
+            T row[D];
 #pragma unroll
-        for (int e0 = 0; e0 < E; ++e0) {
-            if (e0 & RM) continue;
-            if (!((em >> e0) & 1u)) continue;
-            T acc;
-            acc.x = 0;
-            acc.y = 0;
+            for (int c = 0; c < D; ++c) row[c] = mat[r * D + c];
 #pragma unroll
-            for (int c = 0; c < D; ++c) {
-                const T x = a[e0 | r_dep<RM, K>(c)];
-                acc.x += row[c].x * x.x - row[c].y * x.y;
-                acc.y += row[c].x * x.y + row[c].y * x.x;
+            for (int e0 = 0; e0 < E; ++e0) {
+                if (e0 & RM) continue;
+                if (!((em >> e0) & 1u)) continue;
+                T acc;
+                acc.x = 0;
+                acc.y = 0;
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    const T x = a[e0 | r_dep<RM, K>(c)];
+                    acc.x += row[c].x * x.x - row[c].y * x.y;
+                    acc.y += row[c].x * x.y + row[c].y * x.x;
+                }
+                v[e0 | r_dep<RM, K>(r)] = acc;
             }
-            v[e0 | r_dep<RM, K>(r)] = acc;
         }
     }
 }
@@ -660,12 +812,103 @@ __device__ __forceinline__ void r_matk(T (&v)[1 << RB], const T* __restrict__ ma
         }                                                               \
     } while (0)
 
+// The op loop's other kinds: permutations (X, CX, Or, Swap and their
+// controlled forms) and dense 2- and 3-qubit unitaries on register bits.
+template <typename T, int RB, bool MATK, int SL>
+__device__ __forceinline__ void rop_other(T (&v)[SL][1 << RB], const bool (&on)[SL], const uint32_t (&jt)[SL],
+                                          uint32_t kind, uint32_t code, uint4 hd, uint32_t em, bool pred, int a,
+                                          uint64_t base, const ROp* op, const unsigned char* __restrict__ pool) {
+    constexpr uint32_t ALL = (1u << (1 << RB)) - 1u;
+    switch (kind) {
+        case RK_PERM: {
+            uint32_t pm[SL];
+            bool ppred = false;
+#pragma unroll
+            for (int sl = 0; sl < SL; ++sl) {
+                pm[sl] = em;
+                if (code & RF_OR) {
+                    const bool or_t = ((jt[sl] & op->amt) != 0u) || ((base & op->am_ext) != 0ull);
+                    pm[sl] = em & (or_t ? ALL : (hd.z >> 16));
+                }
+                ppred |= pm[sl] != ALL;
+            }
+            AQSG_R_BIT(RB, a, ppred, (r_perm<T, RB, I_, P_, SL>(v, on, pm)));
+            break;
+        }
+        case RK_SWAP: {
+            const int b = (code >> 12) & 15;
+            if (pred) {
+                switch (a * 4 + b) {
+                    case 0 * 4 + 1: r_swap<T, RB, 0, 1, true, SL>(v, on, em); break;
+                    case 0 * 4 + 2: r_swap<T, RB, 0, 2, true, SL>(v, on, em); break;
+                    case 1 * 4 + 2: r_swap<T, RB, 1, 2, true, SL>(v, on, em); break;
+                    default:
+                        if constexpr (RB > 3) {
+                            constexpr int H = RB > 3 ? 3 : 0;
+                            switch (a) {
+                                case 0: r_swap<T, RB, 0, H, true, SL>(v, on, em); break;
+                                case 1: r_swap<T, RB, 1, H, true, SL>(v, on, em); break;
+                                default: r_swap<T, RB, 2, H, true, SL>(v, on, em); break;
+                            }
+                        }
+                        break;
+                }
+            } else {
+                switch (a * 4 + b) {
+                    case 0 * 4 + 1: r_swap<T, RB, 0, 1, false, SL>(v, on, em); break;
+                    case 0 * 4 + 2: r_swap<T, RB, 0, 2, false, SL>(v, on, em); break;
+                    case 1 * 4 + 2: r_swap<T, RB, 1, 2, false, SL>(v, on, em); break;
+                    default:
+                        if constexpr (RB > 3) {
+                            constexpr int H = RB > 3 ? 3 : 0;
+                            switch (a) {
+                                case 0: r_swap<T, RB, 0, H, false, SL>(v, on, em); break;
+                                case 1: r_swap<T, RB, 1, H, false, SL>(v, on, em); break;
+                                default: r_swap<T, RB, 2, H, false, SL>(v, on, em); break;
+                            }
+                        }
+                        break;
+                }
+            }
+            break;
+        }
+        default:
+            if constexpr (MATK) {
+                const T* mat = reinterpret_cast<const T*>(pool + hd.w);
+                const int rm = (code >> 8) & 0xFF;
+                switch (rm) {
+                    case 0x3: r_matk<T, RB, 0x3, SL>(v, on, mat, em); break;
+                    case 0x5: r_matk<T, RB, 0x5, SL>(v, on, mat, em); break;
+                    case 0x6: r_matk<T, RB, 0x6, SL>(v, on, mat, em); break;
+                    case 0x7: r_matk<T, RB, 0x7, SL>(v, on, mat, em); break;
+                    default:
+                        if constexpr (RB > 3) {
+                            switch (rm) {
+                                case 0x9: r_matk<T, RB, 0x9, SL>(v, on, mat, em); break;
+                                case 0xA: r_matk<T, RB, 0xA, SL>(v, on, mat, em); break;
+                                case 0xC: r_matk<T, RB, 0xC, SL>(v, on, mat, em); break;
+                                case 0xB: r_matk<T, RB, 0xB, SL>(v, on, mat, em); break;
+                                case 0xD: r_matk<T, RB, 0xD, SL>(v, on, mat, em); break;
+                                default: r_matk<T, RB, 0xE, SL>(v, on, mat, em); break;
+                            }
+                        }
+                        break;
+                }
+            }
+            break;
+    }
+}
+
 // One register phase: hp[0] the header, hp[1..k] its ROps.  LAY must be
 // linear over GF(2) (the identity or SwzLay): the position of slot element
 // e is then at(jt) ^ at(e's register bits), an XOR of per-bit offsets.
-template <typename T, int RB, class LAY, bool MATK>
+// SL: slots a thread holds at once (slot, slot + nthr, ...); the caller
+// guarantees that 2^(log2 size - RB) is a multiple of SL x nthr.  Two
+// slots per thread halve the per-element cost of decoding each op.
+template <typename T, int RB, class LAY, bool MATK, int SL>
 __device__ __forceinline__ void rphase_run(T* s, uint32_t size, uint32_t nthr, uint64_t base,
                                            const TileOp* __restrict__ hp, const unsigned char* __restrict__ pool) {
+    static_assert(SL == 1 || SL == 2, "one or two slots per thread");
     using R = decltype(T{}.x);
     constexpr int E = 1 << RB;
     constexpr uint32_t ALL = (1u << E) - 1u;
@@ -684,13 +927,25 @@ __device__ __forceinline__ void rphase_run(T* s, uint32_t size, uint32_t nthr, u
             if ((e >> i) & 1) o ^= bo[i];
         return o;
     };
-    for (uint32_t slot = tile_tid(nthr); slot < (size >> RB); slot += nthr) {
-        uint32_t jt = 0;
-        for (int i = 0; i < tbits; ++i) jt |= ((slot >> i) & 1u) << ((tpos >> (4 * i)) & 15u);
-        const uint32_t ajt = LAY::at(jt) * (uint32_t)sizeof(T);
-        T v[E];
+    for (uint32_t slot0 = tile_tid(nthr); slot0 < (size >> RB); slot0 += SL * nthr) {
+        uint32_t jt[SL], ajt[SL];
+        T v[SL][E];
+        {
+            uint32_t j = 0;
+            for (int i = 0; i < tbits; ++i) j |= ((slot0 >> i) & 1u) << ((tpos >> (4 * i)) & 15u);
+            jt[0] = j;
+        }
+        if constexpr (SL == 2) {
+            // slot0 + nthr: slot0 has bit log2(nthr) clear (nthr is a power
+            // of two and slot0 = tid + k 2 nthr), so one tile bit is added
+            jt[1] = jt[0] | (1u << ((tpos >> (4 * (31 - __clz(nthr)))) & 15u));
+        }
 #pragma unroll
-        for (int e = 0; e < E; ++e) v[e] = *reinterpret_cast<const T*>(sb + off_of(ajt, e));
+        for (int sl = 0; sl < SL; ++sl) {
+            ajt[sl] = LAY::at(jt[sl]) * (uint32_t)sizeof(T);
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[sl][e] = *reinterpret_cast<const T*>(sb + off_of(ajt[sl], e));
+        }
         // the next op's header is loaded while this one runs
         uint4 hd_next = nops > 0 ? *reinterpret_cast<const uint4*>(rops) : make_uint4(0u, 0u, 0u, 0u);
         for (int q = 0; q < nops; ++q) {
@@ -701,102 +956,60 @@ __device__ __forceinline__ void rphase_run(T* s, uint32_t size, uint32_t nthr, u
             if (code & RF_EXT) {
                 if ((base & op->cm_ext) != op->cv_ext) continue;
             }
-            if ((jt & (hd.y & 0xFFFFu)) != (hd.y >> 16)) continue;
+            bool on[SL];
+            bool any = false;
+#pragma unroll
+            for (int sl = 0; sl < SL; ++sl) {
+                on[sl] = (jt[sl] & (hd.y & 0xFFFFu)) == (hd.y >> 16);
+                any |= on[sl];
+            }
+            if (!any) continue;
             const uint32_t em = hd.z & ALL;
             const bool pred = em != ALL;
             const int a = (code >> 8) & 15;
-            const T* c = reinterpret_cast<const T*>(op->coef);
-            switch (code & 0xFFu) {
-                case RK_MAT2C: AQSG_R_BIT(RB, a, pred, (r_mat2c<T, RB, I_, P_>(v, c, em))); break;
+            const uint32_t kind = code & 0xFFu;
+            // the leaves read their coefficients from the op table where they
+            // use them (loading them into registers ahead measured slower)
+            switch (kind) {
+                case RK_MAT2C: {
+                    const R(&q)[8] = *reinterpret_cast<const R(*)[8]>(op->coef);
+                    AQSG_R_BIT(RB, a, pred, (r_mat2c<T, RB, I_, P_, SL>(v, on, q, em)));
+                    break;
+                }
                 case RK_MAT2R: {
-                    const R* rc = reinterpret_cast<const R*>(op->coef);
-                    AQSG_R_BIT(RB, a, pred, (r_mat2r<T, R, RB, I_, P_>(v, rc, em)));
+                    const R(&r)[4] = *reinterpret_cast<const R(*)[4]>(op->coef);
+                    AQSG_R_BIT(RB, a, pred, (r_mat2r<T, R, RB, I_, P_, SL>(v, on, r, em)));
                     break;
                 }
-                case RK_PERM: {
-                    uint32_t pm = em;
-                    if (code & RF_OR) {
-                        const bool or_t = ((jt & op->amt) != 0u) || ((base & op->am_ext) != 0ull);
-                        pm = em & (or_t ? ALL : (hd.z >> 16));
-                    }
-                    AQSG_R_BIT(RB, a, pm != ALL, (r_perm<T, RB, I_, P_>(v, pm)));
-                    break;
-                }
-                case RK_SWAP: {
-                    const int b = (code >> 12) & 15;
-                    if (pred) {
-                        switch (a * 4 + b) {
-                            case 0 * 4 + 1: r_swap<T, RB, 0, 1, true>(v, em); break;
-                            case 0 * 4 + 2: r_swap<T, RB, 0, 2, true>(v, em); break;
-                            case 1 * 4 + 2: r_swap<T, RB, 1, 2, true>(v, em); break;
-                            default:
-                                if constexpr (RB > 3) {
-                                    constexpr int H = RB > 3 ? 3 : 0;
-                                    switch (a) {
-                                        case 0: r_swap<T, RB, 0, H, true>(v, em); break;
-                                        case 1: r_swap<T, RB, 1, H, true>(v, em); break;
-                                        default: r_swap<T, RB, 2, H, true>(v, em); break;
-                                    }
-                                }
-                                break;
-                        }
-                    } else {
-                        switch (a * 4 + b) {
-                            case 0 * 4 + 1: r_swap<T, RB, 0, 1, false>(v, em); break;
-                            case 0 * 4 + 2: r_swap<T, RB, 0, 2, false>(v, em); break;
-                            case 1 * 4 + 2: r_swap<T, RB, 1, 2, false>(v, em); break;
-                            default:
-                                if constexpr (RB > 3) {
-                                    constexpr int H = RB > 3 ? 3 : 0;
-                                    switch (a) {
-                                        case 0: r_swap<T, RB, 0, H, false>(v, em); break;
-                                        case 1: r_swap<T, RB, 1, H, false>(v, em); break;
-                                        default: r_swap<T, RB, 2, H, false>(v, em); break;
-                                    }
-                                }
-                                break;
-                        }
-                    }
+                case RK_DIAGR: {
+                    const R(&c)[4] = *reinterpret_cast<const R(*)[4]>(op->coef);
+                    AQSG_R_BIT(RB, a, pred, (r_diagr<T, RB, I_, P_, SL>(v, on, c, em)));
                     break;
                 }
                 case RK_DIAG: {
-                    bool one = false;
-                    if (code & RF_TTHR) one = (jt >> hd.w) & 1u;
-                    else if (code & RF_TEXT) one = (base >> op->ext_t) & 1ull;
-                    const T ph = one ? c[1] : c[0];
-                    if (pred) r_diag<T, RB, true>(v, ph, em);
-                    else r_diag<T, RB, false>(v, ph, em);
+                    const R* cf = reinterpret_cast<const R*>(op->coef);
+                    T ph[SL];
+#pragma unroll
+                    for (int sl = 0; sl < SL; ++sl) {
+                        bool one = false;
+                        if (code & RF_TTHR) one = (jt[sl] >> hd.w) & 1u;
+                        else if (code & RF_TEXT) one = (base >> op->ext_t) & 1ull;
+                        ph[sl].x = one ? cf[2] : cf[0];
+                        ph[sl].y = one ? cf[3] : cf[1];
+                    }
+                    if (pred) r_diag<T, RB, true, SL>(v, on, ph, em);
+                    else r_diag<T, RB, false, SL>(v, on, ph, em);
                     break;
                 }
-                case RK_DIAGR: AQSG_R_BIT(RB, a, pred, (r_diagr<T, RB, I_, P_>(v, c, em))); break;
                 default:
-                    if constexpr (MATK) {
-                        const T* mat = reinterpret_cast<const T*>(pool + hd.w);
-                        const int rm = (code >> 8) & 0xFF;
-                        switch (rm) {
-                            case 0x3: r_matk<T, RB, 0x3>(v, mat, em); break;
-                            case 0x5: r_matk<T, RB, 0x5>(v, mat, em); break;
-                            case 0x6: r_matk<T, RB, 0x6>(v, mat, em); break;
-                            case 0x7: r_matk<T, RB, 0x7>(v, mat, em); break;
-                            default:
-                                if constexpr (RB > 3) {
-                                    switch (rm) {
-                                        case 0x9: r_matk<T, RB, 0x9>(v, mat, em); break;
-                                        case 0xA: r_matk<T, RB, 0xA>(v, mat, em); break;
-                                        case 0xC: r_matk<T, RB, 0xC>(v, mat, em); break;
-                                        case 0xB: r_matk<T, RB, 0xB>(v, mat, em); break;
-                                        case 0xD: r_matk<T, RB, 0xD>(v, mat, em); break;
-                                        default: r_matk<T, RB, 0xE>(v, mat, em); break;
-                                    }
-                                }
-                                break;
-                        }
-                    }
+                    rop_other<T, RB, MATK, SL>(v, on, jt, kind, code, hd, em, pred, a, base, op, pool);
                     break;
             }
         }
 #pragma unroll
-        for (int e = 0; e < E; ++e) *reinterpret_cast<T*>(sb + off_of(ajt, e)) = v[e];
+        for (int sl = 0; sl < SL; ++sl)
+#pragma unroll
+            for (int e = 0; e < E; ++e) *reinterpret_cast<T*>(sb + off_of(ajt[sl], e)) = v[sl][e];
     }
 }
 #undef AQSG_R_BIT
@@ -810,7 +1023,7 @@ __device__ __forceinline__ void rphase_run(T* s, uint32_t size, uint32_t nthr, u
 // ops runs from registers: each thread keeps the same EPT elements for the
 // whole run, so the run costs one shared-memory round trip and one barrier.
 template <typename R, int EPT, bool TC, class LAY, class SYNC = CtaSync, bool MATK = true, bool RPH = !TC,
-          int TCW = 16>
+          int TCW = 16, int SL = 1>
 __device__ __forceinline__ void tile_run_ops(typename Cx<R>::T* s, uint32_t size, uint32_t nthr, uint64_t base,
                                              const TileOp* __restrict__ ops, int nops,
                                              const unsigned char* __restrict__ pool, const TcSmem* tcs,
@@ -821,7 +1034,7 @@ __device__ __forceinline__ void tile_run_ops(typename Cx<R>::T* s, uint32_t size
         const int cls = op.cls;
         if constexpr (RPH) {
             if (cls == T_RPHASE) {
-                rphase_run<T, (sizeof(R) == 4 ? 4 : 3), LAY, MATK>(s, size, nthr, base, ops + oi, pool);
+                rphase_run<T, (sizeof(R) == 4 ? 4 : 3), LAY, MATK, SL>(s, size, nthr, base, ops + oi, pool);
                 SYNC::sync();
                 oi += 1 + op.k;
                 continue;

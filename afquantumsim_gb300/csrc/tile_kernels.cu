@@ -83,16 +83,32 @@ k_tile(typename Cx<R>::T* __restrict__ sv, const TileGeom g, const TileOp* __res
 // amplitudes (rows of 2^L contiguous amplitudes = 256 B at the row offsets of
 // the pass's high tile bits); several CTAs per SM overlap one another's
 // loads, compute and stores.  MATK: the pass has dense k-qubit ops on CUDA
-// cores (their register groups allow two CTAs per SM instead of three).
-template <typename R, int EPT, bool MATK>
+// cores.  kStreamThreads threads per tile: each holds two slots of every
+// register phase (the tile's 2^(m - RB) slots = 2 x kStreamThreads).
+constexpr int kStreamThreads = 128;
+
+// Op tables of up to this many bytes are copied into each CTA's shared
+// memory (after the tile and its row offsets): the op loop then reads them
+// with shared-memory loads instead of L1 hits (a 16 % shorter brick-work
+// pass).  140 entries; four CTAs per SM still fit.
+constexpr uint32_t kStreamOpsSmemMax = 140u * (uint32_t)sizeof(TileOp);
+
+// SOPS: the op table is staged in shared memory (a compile-time choice, so
+// that the op loop's loads are shared-memory loads, not generic ones).
+template <typename R, int EPT, bool MATK, bool SOPS>
 __device__ __forceinline__ void tile_stream_body(typename Cx<R>::T* __restrict__ sv, const TileGeom& g,
                                                  const TileOp* __restrict__ ops, int nops,
                                                  const unsigned char* __restrict__ pool, uint64_t tile) {
     using T = typename Cx<R>::T;
     using LAY = TileSwz<R>;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    const int m = g.m, L = g.L;
-    const uint32_t size = 1u << m;
+    // tile size and thread count are compile-time constants (the launch
+    // checks g.m): the interpreter's slot loop then runs exactly once per
+    // thread and keeps no loop-carried state
+    constexpr uint32_t size = (uint32_t)EPT * kStreamThreads;
+    constexpr int m = __builtin_ctz(size);
+    constexpr uint32_t nthr = kStreamThreads;
+    const int L = g.L;
     T* s = reinterpret_cast<T*>(smem_raw);
     uint64_t* rowoff = reinterpret_cast<uint64_t*>(smem_raw + sizeof(T) * size);
     const uint32_t rows = 1u << (m - L), rowlen = 1u << L;
@@ -102,45 +118,56 @@ __device__ __forceinline__ void tile_stream_body(typename Cx<R>::T* __restrict__
         const uint64_t lo = base & ((1ull << b) - 1ull);
         base = ((base - lo) << 1) | lo;
     }
-    for (uint32_t r = threadIdx.x; r < rows; r += blockDim.x) {
+    for (uint32_t r = threadIdx.x; r < rows; r += nthr) {
         uint64_t off = 0;
         for (int k = 0; k < m - L; ++k)
             if ((r >> k) & 1u) off |= 1ull << g.tbits[L + k];
         rowoff[r] = off;
     }
-    __syncthreads();
-    if constexpr (sizeof(R) == 4) {
-        for (uint32_t i = threadIdx.x; i < (size >> 1); i += blockDim.x) {
-            const uint32_t j = i << 1;
-            const uint64_t gi = base + rowoff[j >> L] + (j & (rowlen - 1));
-            const float4 x = __ldcs(reinterpret_cast<const float4*>(sv) + (gi >> 1));
-            s[LAY::at(j)] = make_float2(x.x, x.y);
-            s[LAY::at(j + 1)] = make_float2(x.z, x.w);
-        }
-    } else {
-        for (uint32_t j = threadIdx.x; j < size; j += blockDim.x)
-            s[LAY::at(j)] = __ldcs(sv + base + rowoff[j >> L] + (j & (rowlen - 1)));
+    if constexpr (SOPS) {
+        uint4* dst = reinterpret_cast<uint4*>(rowoff + rows);
+        const uint4* src = reinterpret_cast<const uint4*>(ops);
+        const uint32_t words = (uint32_t)nops * (uint32_t)(sizeof(TileOp) / 16);
+        for (uint32_t i = threadIdx.x; i < words; i += nthr) dst[i] = __ldg(src + i);
+        ops = reinterpret_cast<const TileOp*>(dst);
     }
     __syncthreads();
-    tile_run_ops<R, EPT, false, LAY, CtaSync, MATK>(s, size, blockDim.x, base, ops, nops, pool, nullptr, nullptr);
+    // the tile arrives by asynchronous copies straight into shared memory:
+    // all of a thread's copies are in flight at once and hold no registers
+    // (one amplitude per copy: the swizzle can reverse a pair's order)
     if constexpr (sizeof(R) == 4) {
-        for (uint32_t i = threadIdx.x; i < (size >> 1); i += blockDim.x) {
+        for (uint32_t i = threadIdx.x; i < (size >> 1); i += nthr) {
+            const uint32_t j = i << 1;
+            const T* src = sv + base + rowoff[j >> L] + (j & (rowlen - 1));
+            cp_async8(s + LAY::at(j), src);
+            cp_async8(s + LAY::at(j + 1), src + 1);
+        }
+    } else {
+        for (uint32_t j = threadIdx.x; j < size; j += nthr)
+            cp_async16(s + LAY::at(j), sv + base + rowoff[j >> L] + (j & (rowlen - 1)));
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    tile_run_ops<R, EPT, false, LAY, CtaSync, MATK, true, 16, 2>(s, size, nthr, base, ops, nops, pool, nullptr,
+                                                                nullptr);
+    if constexpr (sizeof(R) == 4) {
+        for (uint32_t i = threadIdx.x; i < (size >> 1); i += nthr) {
             const uint32_t j = i << 1;
             const uint64_t gi = base + rowoff[j >> L] + (j & (rowlen - 1));
             const float2 a = s[LAY::at(j)], b = s[LAY::at(j + 1)];
             __stcs(reinterpret_cast<float4*>(sv) + (gi >> 1), make_float4(a.x, a.y, b.x, b.y));
         }
     } else {
-        for (uint32_t j = threadIdx.x; j < size; j += blockDim.x)
+        for (uint32_t j = threadIdx.x; j < size; j += nthr)
             __stcs(sv + base + rowoff[j >> L] + (j & (rowlen - 1)), s[LAY::at(j)]);
     }
 }
 
-template <typename R, int EPT, bool MATK>
-__global__ void __launch_bounds__(256, 2)
-k_tile_stream(typename Cx<R>::T* __restrict__ sv, const TileGeom g, const TileOp* __restrict__ ops, int nops,
-              const unsigned char* __restrict__ pool) {
-    tile_stream_body<R, EPT, MATK>(sv, g, ops, nops, pool, blockIdx.x);
+template <typename R, int EPT, bool MATK, bool SOPS>
+__global__ void __launch_bounds__(kStreamThreads, MATK ? 3 : 4)
+k_tile_stream(typename Cx<R>::T* __restrict__ sv, const __grid_constant__ TileGeom g,
+              const TileOp* __restrict__ ops, int nops, const unsigned char* __restrict__ pool) {
+    tile_stream_body<R, EPT, MATK, SOPS>(sv, g, ops, nops, pool, blockIdx.x);
 }
 
 // The same pass over `members` registers of equal shape and plan geometry,
@@ -148,15 +175,15 @@ k_tile_stream(typename Cx<R>::T* __restrict__ sv, const TileGeom g, const TileOp
 // amplitudes start reg_stride amplitudes after the previous register's and
 // whose op table + operand pool start dev_stride bytes after the previous
 // one's (the batched engine's groups of equal-structure circuits).
-template <typename R, int EPT, bool MATK>
-__global__ void __launch_bounds__(256, 2)
-k_tile_stream_multi(typename Cx<R>::T* __restrict__ sv0, uint64_t reg_stride, const TileGeom g,
+template <typename R, int EPT, bool MATK, bool SOPS>
+__global__ void __launch_bounds__(kStreamThreads, MATK ? 3 : 4)
+k_tile_stream_multi(typename Cx<R>::T* __restrict__ sv0, uint64_t reg_stride, const __grid_constant__ TileGeom g,
                     const unsigned char* __restrict__ dev0, uint64_t dev_stride, uint32_t op_first, int nops,
                     uint64_t pool_off, uint32_t tiles) {
     const uint32_t member = blockIdx.x / tiles, tile = blockIdx.x % tiles;
     const unsigned char* dev = dev0 + (uint64_t)member * dev_stride;
-    tile_stream_body<R, EPT, MATK>(sv0 + (uint64_t)member * reg_stride, g,
-                                   reinterpret_cast<const TileOp*>(dev) + op_first, nops, dev + pool_off, tile);
+    tile_stream_body<R, EPT, MATK, SOPS>(sv0 + (uint64_t)member * reg_stride, g,
+                                         reinterpret_cast<const TileOp*>(dev) + op_first, nops, dev + pool_off, tile);
 }
 
 constexpr uint32_t kRowBytes = 256;
@@ -1272,8 +1299,16 @@ static int launch_plan_t(void* sv, const TilePlan& plan, const void* dev, cudaSt
     constexpr int M_STREAM = sizeof(R) == 4 ? 12 : 11;
     auto kwhole = k_tile<R, EPT_WHOLE, false>;
     auto kwhole_k = k_tile<R, EPT_WHOLE, true>;
-    auto kplain = k_tile_stream<R, (1 << M_STREAM) / 256, false>;
-    auto kplain_k = k_tile_stream<R, (1 << M_STREAM) / 256, true>;
+    constexpr int EPT_S = (1 << M_STREAM) / kStreamThreads;
+    // [MATK][op table in shared memory]
+    void (*const kstream[2][2])(T*, const TileGeom, const TileOp*, int, const unsigned char*) = {
+        {k_tile_stream<R, EPT_S, false, false>, k_tile_stream<R, EPT_S, false, true>},
+        {k_tile_stream<R, EPT_S, true, false>, k_tile_stream<R, EPT_S, true, true>}};
+    static_assert(((1 << M_STREAM) >> (sizeof(R) == 4 ? 4 : 3)) == 2 * kStreamThreads,
+                  "two register-phase slots per thread");
+    constexpr int kStreamShmMax = (int)(sizeof(T) << M_STREAM) + 8 * 128 + (int)kStreamOpsSmemMax;
+    for (int a = 0; a < 2; ++a)
+        AQSG_CUDA_TRY(cudaFuncSetAttribute(kstream[a][1], cudaFuncAttributeMaxDynamicSharedMemorySize, kStreamShmMax));
     constexpr int kWholeShmMax = 232448;  // the register plus, where it fits, its op table
     AQSG_CUDA_TRY(cudaFuncSetAttribute(kwhole, cudaFuncAttributeMaxDynamicSharedMemorySize, kWholeShmMax));
     AQSG_CUDA_TRY(cudaFuncSetAttribute(kwhole_k, cudaFuncAttributeMaxDynamicSharedMemorySize, kWholeShmMax));
@@ -1319,8 +1354,11 @@ static int launch_plan_t(void* sv, const TilePlan& plan, const void* dev, cudaSt
                 (T*)sv, geo, dops + p.first, (int)p.count, dpool, ops_smem);
         } else {
             if (geo.m != M_STREAM) return set_error(AQSG_ERR_RUNTIME, "Streaming pass with an unexpected tile size");
-            const size_t shm = sizeof(T) * size + (size_t(1) << (geo.m - geo.L)) * sizeof(uint64_t);
-            (p.matk ? kplain_k : kplain)<<<(unsigned)(1ull << (n - geo.m)), 256, shm, stream>>>(
+            const size_t ops_bytes = sizeof(TileOp) * p.count;
+            const int ops_smem = ops_bytes <= kStreamOpsSmemMax ? 1 : 0;
+            const size_t shm = sizeof(T) * size + (size_t(1) << (geo.m - geo.L)) * sizeof(uint64_t) +
+                               (ops_smem ? ops_bytes : 0);
+            kstream[p.matk ? 1 : 0][ops_smem]<<<(unsigned)(1ull << (n - geo.m)), kStreamThreads, shm, stream>>>(
                 (T*)sv, geo, dops + p.first, (int)p.count, dpool);
         }
         if (launches) ++*launches;
@@ -1333,9 +1371,15 @@ int launch_tile_plan_multi(void* sv0, uint64_t reg_stride, int members, const Ti
                            uint64_t dev_stride, cudaStream_t stream, int* d_err, uint64_t* launches) {
     if (plan.dtype != AQSG_C64) return set_error(AQSG_ERR_RUNTIME, "Grouped tile passes take complex64 plans");
     const int n = plan.n;
-    constexpr int EPT = (1 << 12) / 256;
-    auto kplain = k_tile_stream_multi<float, EPT, false>;
-    auto kplain_k = k_tile_stream_multi<float, EPT, true>;
+    constexpr int EPT = (1 << 12) / kStreamThreads;
+    // [MATK][op table in shared memory]
+    void (*const kmulti[2][2])(float2*, uint64_t, const TileGeom, const unsigned char*, uint64_t, uint32_t, int,
+                               uint64_t, uint32_t) = {
+        {k_tile_stream_multi<float, EPT, false, false>, k_tile_stream_multi<float, EPT, false, true>},
+        {k_tile_stream_multi<float, EPT, true, false>, k_tile_stream_multi<float, EPT, true, true>}};
+    constexpr int kStreamShmMax = (int)(sizeof(float2) << 12) + 8 * 128 + (int)kStreamOpsSmemMax;
+    for (int a = 0; a < 2; ++a)
+        AQSG_CUDA_TRY(cudaFuncSetAttribute(kmulti[a][1], cudaFuncAttributeMaxDynamicSharedMemorySize, kStreamShmMax));
     StreamShape tshape;
     bool have_t = false;
     for (const TilePass& p : plan.passes) {
@@ -1373,8 +1417,11 @@ int launch_tile_plan_multi(void* sv0, uint64_t reg_stride, int members, const Ti
                 (float2*)sv0, geo, (const unsigned char*)dev0, p.first, (int)p.count, plan.pool_offset(), d_err,
                 tiles, (uint32_t)members, reg_stride, dev_stride, map, tg);
         } else {
-            const size_t shm = sizeof(float2) * size + (size_t(1) << (geo.m - geo.L)) * sizeof(uint64_t);
-            (p.matk ? kplain_k : kplain)<<<(unsigned)blocks, 256, shm, stream>>>(
+            const size_t ops_bytes = sizeof(TileOp) * p.count;
+            const int ops_smem = ops_bytes <= kStreamOpsSmemMax ? 1 : 0;
+            const size_t shm = sizeof(float2) * size + (size_t(1) << (geo.m - geo.L)) * sizeof(uint64_t) +
+                               (ops_smem ? ops_bytes : 0);
+            kmulti[p.matk ? 1 : 0][ops_smem]<<<(unsigned)blocks, kStreamThreads, shm, stream>>>(
                 (float2*)sv0, reg_stride, geo, (const unsigned char*)dev0, dev_stride, p.first, (int)p.count,
                 plan.pool_offset(), tiles);
         }

@@ -50,7 +50,7 @@ def parse_args():
     ap.add_argument("--dtype", choices=["c64", "c128"], default="c64")
     ap.add_argument("--mode", choices=["per_gate", "tiled"], default="per_gate")
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--only", choices=["fused_brickwork", "fused_tc", "plain12", "vqe_batch", "vqe_ansatz", "serving",
+    ap.add_argument("--only", choices=["fused_brickwork", "fused_tc", "tiled_brickwork", "plain12", "vqe_batch", "vqe_ansatz", "serving",
                                        "qft_grid", "noise"],
                     help="run one secondary workload alone (at --n qubits where it takes a size) "
                          "and print its JSON; for profiling")
@@ -345,6 +345,23 @@ def bench_fused_tc(ctx, stream, n, depth):
     fused, src = prog.info()
     prog.free()
     return {"workload": f"brickwork{n}x{depth}", "gates": src, "fused_ops": fused, "fused_tensor_core_ms": round(ms, 2)}
+
+
+def bench_tiled_brickwork(ctx, stream, n, depth):
+    """Only the brick-work circuit in plain tile passes (no fusion, CUDA
+    cores; two untimed runs, then three timed): the launches a profiler of
+    the CUDA-core tile pass captures."""
+    import afquantumsim_gb300 as aq
+    from afquantumsim_gb300 import circuits
+    ops = aq.op_array(circuits.brickwork(n, depth, seed=4))
+    with aq.State(ctx, n, aq.C64) as st:
+        st.set_basis(0)
+        l0 = ctx.launch_count()
+        st.apply(ops, aq.EXEC_TILED)
+        passes = ctx.launch_count() - l0
+        st.apply(ops, aq.EXEC_TILED)
+        ms = _time_ms(stream, lambda: st.apply(ops, aq.EXEC_TILED), 3)
+    return {"workload": f"brickwork{n}x{depth}", "gates": len(ops), "passes": passes, "tiled_ms": round(ms, 2)}
 
 
 def bench_noise(ctx, n=12, layers=8, trajectories=4096, seed=7):
@@ -978,6 +995,8 @@ def run_only(args):
             res = bench_fused_brickwork(ctx, st, stream, args.n, args.depth)
     elif args.only == "fused_tc":
         res = bench_fused_tc(ctx, stream, args.n, args.depth)
+    elif args.only == "tiled_brickwork":
+        res = bench_tiled_brickwork(ctx, stream, args.n, args.depth)
     elif args.only == "plain12":
         res = bench_plain12(ctx, stream)
     elif args.only == "noise":
