@@ -333,7 +333,7 @@ int aqsg_shutdown(aqsg_ctx ctx) {
         return set_error(AQSG_ERR_RUNTIME, "Context still owns live states");
     DeviceScope scope(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    Scratch* all[] = {&ctx->partial, &ctx->prefix, &ctx->sample_u, &ctx->sample_o,
+    Scratch* all[] = {&ctx->partial, &ctx->tcnorm, &ctx->prefix, &ctx->sample_u, &ctx->sample_o,
                       &ctx->ops, &ctx->probs};
     for (Scratch* s : all)
         if (s->ptr) cudaFree(s->ptr);
@@ -381,7 +381,8 @@ int aqsg_ctx_after(aqsg_ctx ctx, aqsg_ctx other) {
 
 int aqsg_debug_ctx_scratch(aqsg_ctx ctx, size_t* bytes, int capacity, int* count) {
     if (!ctx || !count) return set_error(AQSG_ERR_NULL, "NULL argument");
-    const Scratch* all[] = {&ctx->partial, &ctx->prefix, &ctx->sample_u, &ctx->sample_o, &ctx->ops, &ctx->probs};
+    const Scratch* all[] = {&ctx->partial, &ctx->tcnorm, &ctx->prefix, &ctx->sample_u,
+                            &ctx->sample_o,  &ctx->ops,    &ctx->probs};
     *count = 6;
     for (int i = 0; i < 6 && i < capacity && bytes; ++i) bytes[i] = all[i]->ptr ? all[i]->bytes : 0;
     return AQSG_OK;

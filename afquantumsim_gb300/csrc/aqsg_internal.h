@@ -110,6 +110,7 @@ struct aqsg_ctx_s {
     uint64_t launches = 0;
     int live_states = 0;
     aqsg::Scratch partial;   // FP64 partial sums of reductions
+    aqsg::Scratch tcnorm;    // per-CTA norm partials of the first / last tensor-core pass
     aqsg::Scratch prefix;    // FP64 chunk prefix sums for sampling
     aqsg::Scratch sample_u;  // uniforms of one sampling call
     aqsg::Scratch sample_o;  // outcomes of one sampling call
@@ -167,8 +168,14 @@ struct TilePlan {
 bool relocate_tile_matrices(unsigned char* table, size_t count, int32_t delta);
 int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, TilePlan* plan, bool exact_perm = true);
 // Launch the passes on `stream`; dev = device copy of table + pool.
+// norm_part (optional, 2 x tc_grid doubles): the first pass, when it runs on
+// the tensor cores, writes per-CTA FP64 partial sums of |a|^2 of its input
+// to norm_part[0, grid), the last such pass of its output to
+// norm_part[grid, 2 grid); *tc_grid = the tensor-core passes' grid.
 int launch_tile_plan(void* sv, const TilePlan& plan, const void* dev, cudaStream_t stream, int* d_err,
-                     uint64_t* launches);
+                     uint64_t* launches, double* norm_part = nullptr, uint32_t* tc_grid = nullptr);
+// One FP64 sum of count partials into *out (device), on the context stream.
+int launch_sum_partials(aqsg_ctx_s* c, const double* parts, int count, double* out);
 // A plain (no tensor-core) complex64 streaming plan over `members` registers
 // at reg_stride amplitudes from one another, whose tables (the same geometry,
 // their own ops) sit dev_stride bytes apart from dev0: one launch per pass.

@@ -933,6 +933,13 @@ int launch_expz_raw_multi(const void* sv0, uint64_t reg_stride, int members, int
 
 namespace aqsg {
 
+int launch_sum_partials(aqsg_ctx_s* c, const double* parts, int count, double* out) {
+    k_sum_partials<<<1, 256, 0, c->stream>>>(parts, count, out);
+    c->launches++;
+    AQSG_CUDA_TRY(cudaGetLastError());
+    return AQSG_OK;
+}
+
 // FP64 sum of |a|^2 into d_out (device), on the context stream.
 int launch_norm_to_device(aqsg_state_s* st, double* d_out) {
     aqsg_ctx_s* c = st->ctx;

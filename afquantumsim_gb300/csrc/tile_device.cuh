@@ -224,6 +224,18 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t* r) {
           "=r"(r[14]), "=r"(r[15])
         : "r"(taddr));
 }
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t* r) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+          "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+          "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+          "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+}
 __device__ __forceinline__ void tc_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // Byte offset of element (row, kk) in a no-swizzle K-major operand with
@@ -369,16 +381,15 @@ __device__ __forceinline__ void tc_apply_tm(float2* s, const TileOp& op, const T
 #pragma unroll
     for (uint32_t i = 0; i < BPT; ++i) {
         const uint32_t dbase = lane_base + 64u + bk[i] * N + 2u * r0;
+        // all of a block's accumulator columns in one load and one wait
+        uint32_t v[2u * RPT];
+        if constexpr (RPT == 16) tc_ld32(dbase, v);
+        else tc_ld16(dbase, v);
+        tc_ld_wait();
 #pragma unroll
-        for (uint32_t c16 = 0; c16 < 2u * RPT; c16 += 16u) {
-            uint32_t v[16];
-            tc_ld16(dbase + c16, v);
-            tc_ld_wait();
-#pragma unroll
-            for (uint32_t e = 0; e < 8u; ++e)
-                *reinterpret_cast<float2*>(sb + jb[i] + offr[r0 + c16 / 2u + e]) =
-                    make_float2(__uint_as_float(v[2 * e]), __uint_as_float(v[2 * e + 1]));
-        }
+        for (uint32_t e = 0; e < RPT; ++e)
+            *reinterpret_cast<float2*>(sb + jb[i] + offr[r0 + e]) =
+                make_float2(__uint_as_float(v[2 * e]), __uint_as_float(v[2 * e + 1]));
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     SYNC::sync();

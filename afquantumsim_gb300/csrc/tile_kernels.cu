@@ -327,8 +327,9 @@ __device__ __forceinline__ void tc_compute_group(unsigned char* smem_raw, const 
                                                  float2* __restrict__ sv0, uint64_t reg_stride,
                                                  const unsigned char* __restrict__ dev0, uint64_t dev_stride,
                                                  uint32_t op_first, int nops, uint64_t pool_off, const TileOp* sops,
-                                                 bool ops_in_smem, uint64_t* full, uint64_t* done,
-                                                 uint64_t* blob_bar, const TcSmem& tcs_in, int* err) {
+                                                 uint64_t* full, uint64_t* done, uint64_t* blob_bar,
+                                                 const TcSmem& tcs_in, int* err, uint32_t norm_flags, double& nin,
+                                                 double& nout) {
     constexpr int NB = TcStreamSmem::kBufs, M = kTcTileBits;
     constexpr uint32_t kBufBytes = TcStreamSmem::kBufBytes;
     using SYNC = GroupSync<NT>;
@@ -339,6 +340,16 @@ __device__ __forceinline__ void tc_compute_group(unsigned char* smem_raw, const 
     TcPhase tph;
     uint32_t blob_par = 0;
     uint32_t cur = (MULTI && tl.count) ? tl.tile(0, true) / tl.ntiles : 0u;
+    // |a|^2 of the tiles before the ops (norm_flags bit 0) and after them
+    // (bit 1), over the 16-byte chunks this thread writes back
+    FAcc fin, fout;
+    auto add_norm = [&](FAcc& f, const uint4& v) {
+        float h, l;
+        norm2_ff(__uint_as_float(v.x), __uint_as_float(v.y), h, l);
+        f.add(h, l);
+        norm2_ff(__uint_as_float(v.z), __uint_as_float(v.w), h, l);
+        f.add(h, l);
+    };
     bool ok = !group_any<NT>(!mbar_wait_bounded(blob_bar, 0, err));
     for (uint32_t i = G; ok && i < tl.count; i += GROUPS) {
         const uint32_t buf = i % NB;
@@ -359,8 +370,15 @@ __device__ __forceinline__ void tc_compute_group(unsigned char* smem_raw, const 
             base = ((base - lo) << 1) | lo;
         }
         const unsigned char* dev = dev0 + (uint64_t)m * dev_stride;
-        const TileOp* optab = ops_in_smem ? sops : reinterpret_cast<const TileOp*>(dev) + op_first;
-        tile_run_ops<float, (1 << M) / NT, true, LAY, SYNC, MATK, false, NT / 32>(s, 1u << M, NT, base, optab, nops,
+        if (norm_flags & 1u) {
+            const unsigned char* src = smem_raw + buf * kBufBytes;
+            for (uint32_t q = threadIdx.x & (NT - 1u); q < kRows * 16u; q += NT)
+                add_norm(fin, *reinterpret_cast<const uint4*>(src + (q >> 4) * TcStreamSmem::kRowStride +
+                                                              (q & 15u) * 16u));
+        }
+        // the op table is in shared memory (the planner keeps tensor-core
+        // passes within kTcMaxOps entries)
+        tile_run_ops<float, (1 << M) / NT, true, LAY, SYNC, MATK, false, NT / 32>(s, 1u << M, NT, base, sops, nops,
                                                                                 dev + pool_off, &tcs, &tph);
         // the group writes its tile back itself (16-byte chunks of the rows,
         // 2048 / NT per thread), so the buffer is free as soon as the last
@@ -374,6 +392,7 @@ __device__ __forceinline__ void tc_compute_group(unsigned char* smem_raw, const 
                 const uint32_t r = q >> 4, c = q & 15u;
                 const uint4 v = *reinterpret_cast<const uint4*>(src + r * TcStreamSmem::kRowStride + c * 16u);
                 __stcs(reinterpret_cast<uint4*>(dstg + rowoff[r]) + c, v);
+                if (norm_flags & 2u) add_norm(fout, v);
             }
         }
         fence_async_smem();
@@ -392,13 +411,16 @@ __device__ __forceinline__ void tc_compute_group(unsigned char* smem_raw, const 
             mbar_wait_timeout(tcs.mma_bar, tph.mma ^ 1u);
         }
     }
+    nin = fin.value();
+    nout = fout.value();
 }
 
 template <bool MULTI, bool MATK>
 __global__ void __launch_bounds__(kTcCta, 1)
-k_stream_tc(float2* __restrict__ sv0, const TileGeom g, const unsigned char* __restrict__ dev0, uint32_t op_first,
-            int nops, uint64_t pool_off, int* err, uint32_t ntiles, uint32_t members, uint64_t reg_stride,
-            uint64_t dev_stride, const __grid_constant__ CUtensorMap tmap, const TmaGeom tg) {
+k_stream_tc(float2* __restrict__ sv0, const __grid_constant__ TileGeom g, const unsigned char* __restrict__ dev0,
+            uint32_t op_first, int nops, uint64_t pool_off, int* err, uint32_t ntiles, uint32_t members,
+            uint64_t reg_stride, uint64_t dev_stride, double* __restrict__ norm_part, uint32_t norm_flags,
+            const __grid_constant__ CUtensorMap tmap, const __grid_constant__ TmaGeom tg) {
     using SM = TcStreamSmem;
     constexpr int NB = SM::kBufs;
     constexpr int GROUPS = kTcGroups;
@@ -414,7 +436,7 @@ k_stream_tc(float2* __restrict__ sv0, const TileGeom g, const unsigned char* __r
     uint64_t* blob_bar = mma_bar + GROUPS;
     TileOp* sops = reinterpret_cast<TileOp*>(smem_raw + SM::kOps);
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
-    const bool ops_in_smem = nops <= kTcMaxOps;
+    double nin = 0.0, nout = 0.0;  // this thread's norm sums (compute warps)
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
@@ -471,7 +493,7 @@ k_stream_tc(float2* __restrict__ sv0, const TileGeom g, const unsigned char* __r
         uint32_t blob_loads = 0;
         auto load_blob = [&](uint32_t m) {  // lane 0
             const unsigned char* pool = dev_of(m) + pool_off;
-            const uint32_t opb = ops_in_smem ? (uint32_t)nops * (uint32_t)sizeof(TileOp) : 0u;
+            const uint32_t opb = (uint32_t)nops * (uint32_t)sizeof(TileOp);
             mbar_expect_tx(blob_bar, g.tc_bytes + opb);
             for (uint32_t o = 0; o < g.tc_bytes; o += 32768u) {
                 const uint32_t len = g.tc_bytes - o < 32768u ? g.tc_bytes - o : 32768u;
@@ -535,11 +557,36 @@ k_stream_tc(float2* __restrict__ sv0, const TileGeom g, const unsigned char* __r
         tl.first = first;
         tl.ntiles = ntiles;
         tc_compute_group<NT, GROUPS, MULTI, MATK, LAY>(smem_raw, g, tl, sv0, reg_stride, dev0, dev_stride, op_first,
-                                                        nops, pool_off, sops, ops_in_smem, full, done, blob_bar, tcs,
-                                                        err);
+                                                        nops, pool_off, sops, full, done, blob_bar, tcs, err,
+                                                        MULTI ? 0u : norm_flags, nin, nout);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            nin += __shfl_down_sync(0xffffffffu, nin, o);
+            nout += __shfl_down_sync(0xffffffffu, nout, o);
+        }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
+    if (!MULTI && norm_flags) {
+        // per-CTA partials in a fixed order (the row offsets are no longer
+        // needed): the same input gives the same sums on every run
+        double* red = reinterpret_cast<double*>(rowoff);
+        constexpr int CW = kTcThreads / 32;
+        if (warp < CW && lane == 0) {
+            red[warp] = nin;
+            red[CW + warp] = nout;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double a = 0.0, b = 0.0;
+            for (int w = 0; w < CW; ++w) {
+                a += red[w];
+                b += red[CW + w];
+            }
+            if (norm_flags & 1u) norm_part[blockIdx.x] = a;
+            if (norm_flags & 2u) norm_part[gridDim.x + blockIdx.x] = b;
+        }
+    }
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(
@@ -609,6 +656,7 @@ static std::vector<Pass> plan(int n, int dtype, const std::vector<LOp>& ops, boo
         Pass cur;
         uint64_t S = rowmask, blk_any = 0, blk_nondiag = 0;
         size_t skipped = 0, blob = 0;
+        bool has_tc = false;  // a tensor-core pass holds at most kTcMaxOps ops
         left.clear();
         for (size_t i = 0; i < rest.size(); ++i) {
             const LOp* o = rest[i];
@@ -619,9 +667,11 @@ static std::vector<Pass> plan(int n, int dtype, const std::vector<LOp>& ops, boo
             const uint64_t sup = support_of(*o), t = targets_of(*o);
             const bool conflict = (sup & (o->diagonal() ? blk_nondiag : blk_any)) != 0;
             const size_t ob = (tc_budget && !whole && o->cls == L_MATK && o->k >= 3) ? tc_op_bytes(o->k) : 0;
-            if (!conflict && __builtin_popcountll(S | t) <= m && blob + ob <= kTcBlobMax) {
+            const bool fits_tc = !(has_tc || ob > 0) || cur.ops.size() < (size_t)kTcMaxOps;
+            if (!conflict && __builtin_popcountll(S | t) <= m && blob + ob <= kTcBlobMax && fits_tc) {
                 S |= t;
                 blob += ob;
+                has_tc |= ob > 0;
                 cur.ops.push_back(o);
             } else {
                 left.push_back(o);
@@ -1118,7 +1168,10 @@ int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, Tile
         for (int b : p.bits) S |= 1ull << b;
         std::vector<int> local(64, -1);
         for (size_t i = 0; i < p.bits.size(); ++i) local[p.bits[i]] = (int)i;
-        const bool tc_pass = tc_on && dtype == AQSG_C64 && tp.m == kTcTileBits;
+        // the tensor-core kernel keeps its op table in shared memory: a pass
+        // with more ops (a whole 12-qubit register; the planner keeps
+        // streaming tensor-core passes within the limit) runs on CUDA cores
+        const bool tc_pass = tc_on && dtype == AQSG_C64 && tp.m == kTcTileBits && p.ops.size() <= (size_t)kTcMaxOps;
         std::vector<unsigned char> blob;  // this pass's tensor-core operands
         if (tc_pass) blob.reserve(kTcBlobMax);
         std::vector<TileOp> pops;         // this pass's table
@@ -1287,7 +1340,7 @@ static void tile_tensor_map(void* sv, int n, const TilePass& p, uint32_t members
 
 template <typename R>
 static int launch_plan_t(void* sv, const TilePlan& plan, const void* dev, cudaStream_t stream, int* d_err,
-                         uint64_t* launches) {
+                         uint64_t* launches, double* norm_part, uint32_t* tc_grid) {
     using T = typename Cx<R>::T;
     const int n = plan.n;
     const TileOp* dops = (const TileOp*)dev;
@@ -1314,7 +1367,8 @@ static int launch_plan_t(void* sv, const TilePlan& plan, const void* dev, cudaSt
     AQSG_CUDA_TRY(cudaFuncSetAttribute(kwhole_k, cudaFuncAttributeMaxDynamicSharedMemorySize, kWholeShmMax));
     StreamShape tshape;
     bool have_t = false;
-    for (const TilePass& p : plan.passes) {
+    for (size_t pi = 0; pi < plan.passes.size(); ++pi) {
+        const TilePass& p = plan.passes[pi];
         TileGeom geo;
         std::memset(&geo, 0, sizeof(geo));
         geo.n = n;
@@ -1336,14 +1390,18 @@ static int launch_plan_t(void* sv, const TilePlan& plan, const void* dev, cudaSt
                 have_t = true;
             }
             if (p.tc_bytes > kTcBlobMax) return set_error(AQSG_ERR_RUNTIME, "Tensor-core operands exceed the blob");
+            if (p.count > (uint32_t)kTcMaxOps) return set_error(AQSG_ERR_RUNTIME, "Tensor-core pass with too many ops");
             const uint32_t tiles = 1u << (n - geo.m);
             const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)(tshape.sms * tshape.per_sm));
+            if (tc_grid) *tc_grid = grid;
+            uint32_t nf = 0;
+            if (norm_part) nf = (pi == 0 ? 1u : 0u) | (pi + 1 == plan.passes.size() ? 2u : 0u);
             CUtensorMap map;
             TmaGeom tg;
             tile_tensor_map(sv, n, p, 1u, &map, &tg);
             ktc<<<grid, kTcCta, TcStreamSmem::kBytes, stream>>>(
                 (float2*)sv, geo, (const unsigned char*)dev, p.first, (int)p.count, plan.pool_offset(), d_err, tiles,
-                1u, 0ull, 0ull, map, tg);
+                1u, 0ull, 0ull, norm_part, nf, map, tg);
         } else if (geo.m == n) {
             const int rb = phase_reg_bits(plan.dtype);
             int threads = (int)(geo.m >= rb + kPhaseMinSlotBits ? size >> rb : size / EPT_WHOLE);
@@ -1406,6 +1464,7 @@ int launch_tile_plan_multi(void* sv0, uint64_t reg_stride, int members, const Ti
                 have_t = true;
             }
             if (p.tc_bytes > kTcBlobMax) return set_error(AQSG_ERR_RUNTIME, "Tensor-core operands exceed the blob");
+            if (p.count > (uint32_t)kTcMaxOps) return set_error(AQSG_ERR_RUNTIME, "Tensor-core pass with too many ops");
             const uint32_t grid = (uint32_t)std::min<uint64_t>(blocks, (uint64_t)tshape.sms * tshape.per_sm);
             CUtensorMap map;
             TmaGeom tg;
@@ -1415,7 +1474,7 @@ int launch_tile_plan_multi(void* sv0, uint64_t reg_stride, int members, const Ti
             if (reg_stride == (1ull << n)) tile_tensor_map(sv0, n, p, (uint32_t)members, &map, &tg);
             ktc<<<grid, kTcCta, TcStreamSmem::kBytes, stream>>>(
                 (float2*)sv0, geo, (const unsigned char*)dev0, p.first, (int)p.count, plan.pool_offset(), d_err,
-                tiles, (uint32_t)members, reg_stride, dev_stride, map, tg);
+                tiles, (uint32_t)members, reg_stride, dev_stride, nullptr, 0u, map, tg);
         } else {
             const size_t ops_bytes = sizeof(TileOp) * p.count;
             const int ops_smem = ops_bytes <= kStreamOpsSmemMax ? 1 : 0;
@@ -1432,9 +1491,9 @@ int launch_tile_plan_multi(void* sv0, uint64_t reg_stride, int members, const Ti
 }
 
 int launch_tile_plan(void* sv, const TilePlan& plan, const void* dev, cudaStream_t stream, int* d_err,
-                     uint64_t* launches) {
-    return plan.dtype == AQSG_C64 ? launch_plan_t<float>(sv, plan, dev, stream, d_err, launches)
-                                  : launch_plan_t<double>(sv, plan, dev, stream, d_err, launches);
+                     uint64_t* launches, double* norm_part, uint32_t* tc_grid) {
+    return plan.dtype == AQSG_C64 ? launch_plan_t<float>(sv, plan, dev, stream, d_err, launches, norm_part, tc_grid)
+                                  : launch_plan_t<double>(sv, plan, dev, stream, d_err, launches, norm_part, tc_grid);
 }
 
 // ---- plan cache ----------------------------------------------------------------------
@@ -1467,17 +1526,46 @@ void plan_cache_free(aqsg_ctx_s* c) {
 }
 
 // Run an encoded plan whose table is on the device (dev_table): the tile
-// passes, the error-flag check, and for tensor-core passes the
-// renormalisation to the input's FP64 norm.
+// passes, for tensor-core passes the renormalisation to the input's FP64
+// norm, and the error-flag check.
 static int run_encoded(aqsg_state_s* st, const TilePlan& plan, const void* dev_table) {
     aqsg_ctx_s* c = st->ctx;
     // The tensor-core products lose a little norm in a biased way (~1e-7 per
     // fused op); a run that uses them restores the input's FP64 norm at the
-    // end (one read pass before, one read and one scale pass after).
-    double norm_before = 0;
-    if (plan.any_tc)
-        if (int rc = reduce_prob(st, 0, 0, &norm_before)) return rc;
-    if (int rc = launch_tile_plan(st->d, plan, dev_table, c->stream, c->d_err, &c->launches)) return rc;
+    // end.  The norms before and after come from the first and the last
+    // pass when those run on the tensor cores (per-CTA partials summed in a
+    // fixed order), else from a read pass of their own; the scale factor
+    // stays on the device.
+    double* norms = nullptr;  // [before, after, partials...]
+    double* parts = nullptr;
+    bool fold_in = false, fold_out = false;
+    if (plan.any_tc) {
+        fold_in = plan.passes.front().tc;
+        fold_out = plan.passes.back().tc;
+        const size_t need = sizeof(double) * (2 + 2 * (size_t)c->sm_count * 2);
+        if (int rc = ensure_scratch(c->tcnorm, need)) return rc;
+        norms = (double*)c->tcnorm.ptr;
+        parts = norms + 2;
+        if (!fold_in || !fold_out)  // the read passes' reduction scratch
+            if (int rc = reserve_scratch(c, st->n, 1)) return rc;
+        if (!fold_in)
+            if (int rc = launch_norm_to_device(st, norms)) return rc;
+    }
+    uint32_t tc_grid = 0;
+    if (int rc = launch_tile_plan(st->d, plan, dev_table, c->stream, c->d_err, &c->launches,
+                                  (fold_in || fold_out) ? parts : nullptr, &tc_grid))
+        return rc;
+    if (plan.any_tc) {
+        if (tc_grid > 2u * (uint32_t)c->sm_count) return set_error(AQSG_ERR_RUNTIME, "Norm partials exceed their scratch");
+        if (fold_in)
+            if (int rc = launch_sum_partials(c, parts, (int)tc_grid, norms)) return rc;
+        if (fold_out) {
+            if (int rc = launch_sum_partials(c, parts + tc_grid, (int)tc_grid, norms + 1)) return rc;
+        } else {
+            if (int rc = launch_norm_to_device(st, norms + 1)) return rc;
+        }
+        if (int rc = launch_renorm_device(st, norms, norms + 1)) return rc;
+    }
     if (plan.any_stream) {  // a bounded wait that gave up leaves a flag
         AQSG_CUDA_TRY(cudaMemcpyAsync(c->host_result, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
         AQSG_CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -1487,12 +1575,6 @@ static int run_encoded(aqsg_state_s* st, const TilePlan& plan, const void* dev_t
             AQSG_CUDA_TRY(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
             return set_error(AQSG_ERR_TIMEOUT, "Tile pass timed out waiting for its copies or MMAs");
         }
-    }
-    if (plan.any_tc) {
-        double norm_after = 0;
-        if (int rc = reduce_prob(st, 0, 0, &norm_after)) return rc;
-        if (norm_after > 0 && norm_before > 0)
-            if (int rc = launch_scale(st, std::sqrt(norm_before / norm_after))) return rc;
     }
     return AQSG_OK;
 }
