@@ -44,7 +44,7 @@ EXPORTS = [
     "aqsg_expect_pauli", "aqsg_autotune", "aqsg_batch_tuning", "aqsg_selftest_bounded_wait",
     "aqsg_state_download_async", "aqsg_circuit_to_text", "aqsg_circuit_from_text",
     "aqsg_debug_tile_plan", "aqsg_debug_batch_image", "aqsg_debug_ctx_scratch", "aqsg_batch_traffic",
-    "aqsg_noise_trajectory", "aqsg_noise_expect_z",
+    "aqsg_noise_trajectory", "aqsg_noise_expect_z", "aqsg_program_plan",
 ]
 
 _lib = None
@@ -573,8 +573,9 @@ def _bind_programs(lib):
     lib.aqsg_run_program.argtypes = [P, P, I]
     lib.aqsg_program_export.argtypes = [P, C.POINTER(Op), I, C.POINTER(I)]
     lib.aqsg_program_free.argtypes = [P]
+    lib.aqsg_program_plan.argtypes = [P, I, C.POINTER(I), C.POINTER(I), C.POINTER(C.c_uint64)]
     for f in ("aqsg_compile", "aqsg_program_info", "aqsg_run_program", "aqsg_program_export",
-              "aqsg_program_free"):
+              "aqsg_program_free", "aqsg_program_plan"):
         getattr(lib, f).restype = I
 
 
@@ -593,6 +594,12 @@ class Program:
         f, s = C.c_int(), C.c_int()
         _check(self.lib.aqsg_program_info(self.h, C.byref(f), C.byref(s)))
         return f.value, s.value
+
+    def plan(self, tensor_cores: bool = True):
+        """aqsg_program_plan: {passes, tc_passes, hbm_bytes} of a tiled run."""
+        p, t, b = C.c_int(), C.c_int(), C.c_uint64()
+        _check(self.lib.aqsg_program_plan(self.h, 1 if tensor_cores else 0, C.byref(p), C.byref(t), C.byref(b)))
+        return {"passes": p.value, "tc_passes": t.value, "hbm_bytes": b.value}
 
     def export(self):
         """The fused ops as aqsg_op structs (matrices point into the program)."""

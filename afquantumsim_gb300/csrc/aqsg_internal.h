@@ -194,6 +194,9 @@ int tile_max_bits(int dtype);
 // the register per tile pass; with renorm, a run with tensor-core passes
 // also reads the register twice for its norms and rescales it once.
 uint64_t plan_hbm_bytes(const TilePlan& plan, bool renorm);
+// HBM bytes of one synchronous run of the plan (run_encoded: norms folded
+// into tensor-core end passes).
+uint64_t plan_run_bytes(const TilePlan& plan);
 
 // ---- init / measurement launchers (measure_kernels.cu) -------------------------
 int launch_set_basis(aqsg_state_s* st, uint64_t k);

@@ -410,6 +410,18 @@ int aqsg_program_info(aqsg_program p, int* fused_ops, int* source_ops) {
     return AQSG_OK;
 }
 
+int aqsg_program_plan(aqsg_program p, int tensor_cores, int* passes, int* tc_passes, uint64_t* hbm_bytes) {
+    if (!p) return set_error(AQSG_ERR_NULL, "NULL program");
+    TilePlan plan;
+    if (int rc = encode_tiled(p->n, p->dtype, p->ops, tensor_cores != 0, &plan)) return rc;
+    int ntc = 0;
+    for (const TilePass& tp : plan.passes) ntc += tp.tc ? 1 : 0;
+    if (passes) *passes = (int)plan.passes.size();
+    if (tc_passes) *tc_passes = ntc;
+    if (hbm_bytes) *hbm_bytes = plan_run_bytes(plan);
+    return AQSG_OK;
+}
+
 int aqsg_run_program(aqsg_state st, aqsg_program p, int mode) {
     if (!st || !st->d) return set_error(AQSG_ERR_NULL, "NULL state");
     if (!p) return set_error(AQSG_ERR_NULL, "NULL program");

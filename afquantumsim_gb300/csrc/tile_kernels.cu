@@ -1579,10 +1579,20 @@ static int run_encoded(aqsg_state_s* st, const TilePlan& plan, const void* dev_t
     return AQSG_OK;
 }
 
+// renorm: the asynchronous renormalisation (run_plan_async: two norm reads
+// and a scale pass)
 uint64_t plan_hbm_bytes(const TilePlan& plan, bool renorm) {
     const uint64_t reg = (uint64_t)amp_bytes(plan.dtype) << plan.n;
     uint64_t b = 2 * reg * (uint64_t)plan.passes.size();
     if (renorm && plan.any_tc) b += 4 * reg;
+    return b;
+}
+
+uint64_t plan_run_bytes(const TilePlan& plan) {
+    const uint64_t reg = (uint64_t)amp_bytes(plan.dtype) << plan.n;
+    uint64_t b = 2 * reg * (uint64_t)plan.passes.size();
+    if (plan.any_tc)
+        b += 2 * reg + (plan.passes.front().tc ? 0 : reg) + (plan.passes.back().tc ? 0 : reg);
     return b;
 }
 

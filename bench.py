@@ -278,16 +278,19 @@ def bench_fused_brickwork(ctx, st, stream, n, depth):
     # HBM roofline of each mode.  One gate per pass: the algorithmic bytes of
     # each gate (the amplitudes it can change); tile passes: one read and one
     # write of the register per pass (2 x 8 B x 2^n), so no mode can exceed
-    # 1.0; the tensor-core run also reads the register twice for its FP64
-    # norms and rescales it once (4 x 8 B x 2^n, its launches = passes + 5).
+    # 1.0; the tensor-core run also rescales the register once for its FP64
+    # norm (its first and last passes carry the norm sums) -- the program's
+    # plan (aqsg_program_plan) gives the passes and bytes of both fused runs
     peak, peak_src = measured_peaks()
     reg = 8 * N
     per_gate_bytes = sum(gate_alg_bytes(o, n, 8) for o in ops)
-    tc_passes = tc_launches - 5
+    plan_tc, plan_cc = prog.plan(tensor_cores=True), prog.plan(tensor_cores=False)
+    res["fused_plan"] = {"tensor_cores": plan_tc, "cuda_cores": plan_cc, "tc_run_launches": tc_launches,
+                         "cuda_core_run_launches": fused_passes}
     modes = {"per_gate": (per_gate_bytes, res["per_gate_ms"], len(ops)),
              "tiled": (2 * reg * tiled_passes, res["tiled_ms"], tiled_passes),
-             "fused_cuda_core": (2 * reg * fused_passes, res["fused_cuda_core_ms"], fused_passes),
-             "fused_tensor_core": (2 * reg * tc_passes + 4 * reg, res["fused_tensor_core_ms"], tc_passes)}
+             "fused_cuda_core": (plan_cc["hbm_bytes"], res["fused_cuda_core_ms"], plan_cc["passes"]),
+             "fused_tensor_core": (plan_tc["hbm_bytes"], res["fused_tensor_core_ms"], plan_tc["passes"])}
     res["hbm"] = {m: {"passes": p, "bytes": b, "achieved_gbs": round(b / (ms / 1e3) / 1e9, 1), "peak_gbs": peak,
                       "frac": round(b / (ms / 1e3) / 1e9 / peak, 4), "peak_source": peak_src}
                   for m, (b, ms, p) in modes.items()}

@@ -255,6 +255,14 @@ int aqsg_compile(int n, int dtype, const aqsg_op* ops, int count, int max_qubits
 /* Number of fused ops and of source ops of a program. */
 int aqsg_program_info(aqsg_program prog, int* fused_ops, int* source_ops);
 
+/* The tile plan a tiled run of the program executes (tensor cores on or
+ * off): *passes tile passes, *tc_passes of them on the tensor cores, and
+ * *hbm_bytes = the HBM bytes of one run (one read and one write of the
+ * register per pass, plus the renormalisation of a run with tensor-core
+ * passes: a scale pass, and a read pass for each end of the run that is not
+ * a tensor-core pass).  Host-side only; any output may be NULL. */
+int aqsg_program_plan(aqsg_program prog, int tensor_cores, int* passes, int* tc_passes, uint64_t* hbm_bytes);
+
 /* Run a compiled program on a register with the program's n and dtype
  * (QSimulator::simulate's compiled prefix, quantum.cpp:283).  mode: an
  * aqsg_exec_mode or -1 for the context default. */

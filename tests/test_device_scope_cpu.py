@@ -19,7 +19,7 @@ HOST_ONLY = {
     "aqsg_program_export", "aqsg_program_free", "aqsg_circuit_to_text", "aqsg_circuit_from_text",
     "aqsg_batch_info", "aqsg_batch_tuning", "aqsg_batch_traffic", "aqsg_debug_tile_plan", "aqsg_debug_batch_image",
     "aqsg_debug_ctx_scratch", "aqsg_server_submit", "aqsg_server_start", "aqsg_server_poll",
-    "aqsg_server_wait_idle", "aqsg_server_get_stats", "aqsg_noise_trajectory",
+    "aqsg_server_wait_idle", "aqsg_server_get_stats", "aqsg_noise_trajectory", "aqsg_program_plan",
 }
 # entry points that hand over to a function which opens the scope
 DELEGATES = {

@@ -48,3 +48,37 @@ def test_compile_validates_like_check():
         aq.Program(3, [aq.H(3)])
     with pytest.raises(aq.InvalidArgument):
         aq.Program(3, [aq.H(0)], max_qubits=6)
+
+
+def test_program_plan_traffic():
+    """aqsg_program_plan: one read + one write of the register per pass; a
+    run with tensor-core passes adds the scale pass (its first and last
+    passes carry the norm sums)."""
+    n = 20
+    prog = aq.Program(n, circuits.brickwork(n, 6, seed=4), aq.C64, max_qubits=5)
+    reg = 8 << n
+    off = prog.plan(tensor_cores=False)
+    assert off["tc_passes"] == 0 and off["passes"] > 0
+    assert off["hbm_bytes"] == 2 * reg * off["passes"]
+    on = prog.plan(tensor_cores=True)
+    assert 0 < on["tc_passes"] <= on["passes"]
+    assert on["hbm_bytes"] in (2 * reg * on["passes"] + 2 * reg, 2 * reg * on["passes"] + 3 * reg,
+                               2 * reg * on["passes"] + 4 * reg)
+    prog.free()
+
+
+def test_tensor_core_pass_op_limit():
+    """A whole 12-qubit register with more ops than the tensor-core kernel
+    holds in shared memory runs on the CUDA cores."""
+    r = np.array([[0.6, 0.8], [-0.8, 0.6]])
+    u3 = np.kron(np.kron(r, r.T), r).astype(np.complex64)  # dense, not a permutation
+    # overlapping 3-qubit windows: no two neighbours fuse within 3 qubits
+    ops = [aq.Unitary([w, w + 1, w + 2], u3) for w in [i % 10 for i in range(40)]]
+    prog = aq.Program(12, ops, aq.C64, max_qubits=3)
+    fused, _ = prog.info()
+    assert fused > 24
+    assert prog.plan(tensor_cores=True)["tc_passes"] == 0
+    prog.free()
+    few = aq.Program(12, ops[:10], aq.C64, max_qubits=3)
+    assert few.plan(tensor_cores=True)["tc_passes"] == 1
+    few.free()
