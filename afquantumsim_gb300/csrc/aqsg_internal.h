@@ -193,9 +193,12 @@ int tile_max_bits(int dtype);
 // Algorithmic HBM bytes of running a plan once: one read and one write of
 // the register per tile pass; with renorm, a run with tensor-core passes
 // also reads the register twice for its norms and rescales it once.
+// HBM bytes of the plan's passes, with renorm also its renormalisation
+// (= plan_run_bytes).
 uint64_t plan_hbm_bytes(const TilePlan& plan, bool renorm);
-// HBM bytes of one synchronous run of the plan (run_encoded: norms folded
-// into tensor-core end passes).
+// HBM bytes of one run of the plan: its passes and, for tensor-core runs,
+// the scale pass plus a norm read for each end that is not a tensor-core
+// pass.
 uint64_t plan_run_bytes(const TilePlan& plan);
 
 // ---- init / measurement launchers (measure_kernels.cu) -------------------------
@@ -220,8 +223,11 @@ int launch_renorm_device(aqsg_state_s* st, const double* n_before, const double*
 int sample_seeded_async(aqsg_state_s* st, uint64_t seed, uint64_t count, int rule, uint64_t* pinned_out);
 // Tile passes without host synchronisation; dev_table is the device copy of
 // plan.table followed by plan.pool at plan.pool_offset().  Tensor-core runs
-// renormalise on the device through d_norms[0..1].
+// renormalise on the device through d_norms (tc_norm_doubles() doubles; the
+// context's reduction scratch reserved for read passes).
 int run_plan_async(aqsg_state_s* st, const TilePlan& plan, const void* dev_table, double* d_norms);
+// Doubles of the renormalisation buffer of a tensor-core run on c.
+size_t tc_norm_doubles(const aqsg_ctx_s* c);
 // aqsg_autotune, optionally without the one-gate-per-pass candidate.
 int autotune_impl(aqsg_ctx ctx, int n, int dtype, const aqsg_op* ops, int count, int reps, bool tiled_only,
                   aqsg_tune_entry* best, aqsg_tune_entry* all, int capacity, int* count_out);

@@ -306,7 +306,7 @@ int aqsg_server_create(int device, int dtype, uint64_t hbm_budget_bytes, int lan
         cudaError_t e = cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaMallocHost((void**)&L.pinned_table, kLaneTableBytes);
         if (e == cudaSuccess) e = cudaMallocHost((void**)&L.pinned_out, sizeof(uint64_t) * (max_shots + 8));
-        if (e == cudaSuccess) e = cudaMalloc((void**)&L.d_norms, 64);
+        if (e == cudaSuccess) e = cudaMalloc((void**)&L.d_norms, sizeof(double) * tc_norm_doubles(L.ctx));
         if (e != cudaSuccess) {
             rc = cuda_error(e, "aqsg_server_create");
             break;

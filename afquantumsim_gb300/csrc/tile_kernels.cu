@@ -1525,47 +1525,52 @@ void plan_cache_free(aqsg_ctx_s* c) {
     c->plans = nullptr;
 }
 
-// Run an encoded plan whose table is on the device (dev_table): the tile
-// passes, for tensor-core passes the renormalisation to the input's FP64
-// norm, and the error-flag check.
-static int run_encoded(aqsg_state_s* st, const TilePlan& plan, const void* dev_table) {
+size_t tc_norm_doubles(const aqsg_ctx_s* c) { return 2 + 4 * (size_t)c->sm_count; }
+
+// The tile passes of a plan and, for a run with tensor-core passes, the
+// renormalisation to the input's FP64 norm, all on the context stream.  The
+// tensor-core products lose a little norm in a biased way (~1e-7 per fused
+// op).  The norms before and after come from the first and the last pass
+// when those run on the tensor cores (per-CTA partials summed in a fixed
+// order, so a run gives the same sums every time), else from a read pass of
+// their own (whose reduction scratch the caller reserved); the scale factor
+// never leaves the device.  norms: tc_norm_doubles() doubles,
+// [before, after, partials...].
+static int launch_plan_renorm(aqsg_state_s* st, const TilePlan& plan, const void* dev_table, double* norms) {
     aqsg_ctx_s* c = st->ctx;
-    // The tensor-core products lose a little norm in a biased way (~1e-7 per
-    // fused op); a run that uses them restores the input's FP64 norm at the
-    // end.  The norms before and after come from the first and the last
-    // pass when those run on the tensor cores (per-CTA partials summed in a
-    // fixed order), else from a read pass of their own; the scale factor
-    // stays on the device.
-    double* norms = nullptr;  // [before, after, partials...]
-    double* parts = nullptr;
-    bool fold_in = false, fold_out = false;
-    if (plan.any_tc) {
-        fold_in = plan.passes.front().tc;
-        fold_out = plan.passes.back().tc;
-        const size_t need = sizeof(double) * (2 + 2 * (size_t)c->sm_count * 2);
-        if (int rc = ensure_scratch(c->tcnorm, need)) return rc;
-        norms = (double*)c->tcnorm.ptr;
-        parts = norms + 2;
-        if (!fold_in || !fold_out)  // the read passes' reduction scratch
-            if (int rc = reserve_scratch(c, st->n, 1)) return rc;
-        if (!fold_in)
-            if (int rc = launch_norm_to_device(st, norms)) return rc;
-    }
+    const bool fold_in = plan.any_tc && plan.passes.front().tc;
+    const bool fold_out = plan.any_tc && plan.passes.back().tc;
+    double* parts = norms + 2;
+    if (plan.any_tc && !fold_in)
+        if (int rc = launch_norm_to_device(st, norms)) return rc;
     uint32_t tc_grid = 0;
     if (int rc = launch_tile_plan(st->d, plan, dev_table, c->stream, c->d_err, &c->launches,
                                   (fold_in || fold_out) ? parts : nullptr, &tc_grid))
         return rc;
-    if (plan.any_tc) {
-        if (tc_grid > 2u * (uint32_t)c->sm_count) return set_error(AQSG_ERR_RUNTIME, "Norm partials exceed their scratch");
-        if (fold_in)
-            if (int rc = launch_sum_partials(c, parts, (int)tc_grid, norms)) return rc;
-        if (fold_out) {
-            if (int rc = launch_sum_partials(c, parts + tc_grid, (int)tc_grid, norms + 1)) return rc;
-        } else {
-            if (int rc = launch_norm_to_device(st, norms + 1)) return rc;
-        }
-        if (int rc = launch_renorm_device(st, norms, norms + 1)) return rc;
+    if (!plan.any_tc) return AQSG_OK;
+    if (tc_grid > 2u * (uint32_t)c->sm_count) return set_error(AQSG_ERR_RUNTIME, "Norm partials exceed their scratch");
+    if (fold_in)
+        if (int rc = launch_sum_partials(c, parts, (int)tc_grid, norms)) return rc;
+    if (fold_out) {
+        if (int rc = launch_sum_partials(c, parts + tc_grid, (int)tc_grid, norms + 1)) return rc;
+    } else {
+        if (int rc = launch_norm_to_device(st, norms + 1)) return rc;
     }
+    return launch_renorm_device(st, norms, norms + 1);
+}
+
+// Run an encoded plan whose table is on the device (dev_table): the passes
+// with their renormalisation, then the error-flag check.
+static int run_encoded(aqsg_state_s* st, const TilePlan& plan, const void* dev_table) {
+    aqsg_ctx_s* c = st->ctx;
+    double* norms = nullptr;
+    if (plan.any_tc) {
+        if (int rc = ensure_scratch(c->tcnorm, sizeof(double) * tc_norm_doubles(c))) return rc;
+        norms = (double*)c->tcnorm.ptr;
+        if (!plan.passes.front().tc || !plan.passes.back().tc)  // a read pass's reduction scratch
+            if (int rc = reserve_scratch(c, st->n, 1)) return rc;
+    }
+    if (int rc = launch_plan_renorm(st, plan, dev_table, norms)) return rc;
     if (plan.any_stream) {  // a bounded wait that gave up leaves a flag
         AQSG_CUDA_TRY(cudaMemcpyAsync(c->host_result, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
         AQSG_CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -1579,13 +1584,9 @@ static int run_encoded(aqsg_state_s* st, const TilePlan& plan, const void* dev_t
     return AQSG_OK;
 }
 
-// renorm: the asynchronous renormalisation (run_plan_async: two norm reads
-// and a scale pass)
 uint64_t plan_hbm_bytes(const TilePlan& plan, bool renorm) {
     const uint64_t reg = (uint64_t)amp_bytes(plan.dtype) << plan.n;
-    uint64_t b = 2 * reg * (uint64_t)plan.passes.size();
-    if (renorm && plan.any_tc) b += 4 * reg;
-    return b;
+    return renorm ? plan_run_bytes(plan) : 2 * reg * (uint64_t)plan.passes.size();
 }
 
 uint64_t plan_run_bytes(const TilePlan& plan) {
@@ -1655,16 +1656,8 @@ int run_tiled_cached(aqsg_state_s* st, const std::vector<unsigned char>& key,
 }
 
 int run_plan_async(aqsg_state_s* st, const TilePlan& plan, const void* dev_table, double* d_norms) {
-    aqsg_ctx_s* c = st->ctx;
     if (plan.passes.empty()) return AQSG_OK;
-    if (plan.any_tc)
-        if (int rc = launch_norm_to_device(st, d_norms)) return rc;
-    if (int rc = launch_tile_plan(st->d, plan, dev_table, c->stream, c->d_err, &c->launches)) return rc;
-    if (plan.any_tc) {
-        if (int rc = launch_norm_to_device(st, d_norms + 1)) return rc;
-        if (int rc = launch_renorm_device(st, d_norms, d_norms + 1)) return rc;
-    }
-    return AQSG_OK;
+    return launch_plan_renorm(st, plan, dev_table, d_norms);
 }
 
 }  // namespace aqsg
