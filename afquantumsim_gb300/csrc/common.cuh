@@ -36,6 +36,44 @@ __device__ __forceinline__ T cmul2(T m0, T a, T m1, T b) {
     return r;
 }
 
+// ---- bounded waits ----------------------------------------------------------------
+
+constexpr uint64_t kWaitNs = 200000000ull;    // 0.2 s of waiting per bounded wait
+constexpr uint64_t kWaitStepNs = 1000000ull;  // 1 ms
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Time a bounded wait has spent, from %globaltimer read at each check: a
+// step counts at most kWaitStepNs, so a jump of the timer or a spell off
+// the SM (a preemption) counts as one step, not as a stall.
+struct WaitClock {
+    uint64_t last, spent = 0;
+    __device__ __forceinline__ WaitClock() : last(globaltimer_ns()) {}
+    __device__ __forceinline__ bool expired(uint64_t limit_ns = kWaitNs) {
+        const uint64_t now = globaltimer_ns(), dt = now - last;
+        last = now;
+        spent += dt < kWaitStepNs ? dt : kWaitStepNs;
+        return spent > limit_ns;
+    }
+};
+
+// acc += m * x (complex) as four chained fused multiply-adds (written as
+// acc += a*b - c*d the compiler emits a multiply, an FMA and an add per
+// component).
+__device__ __forceinline__ float fmadd(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fmadd(double a, double b, double c) { return __fma_rn(a, b, c); }
+template <typename T>
+__device__ __forceinline__ void cmac(T& acc, T m, T x) {
+    acc.x = fmadd(m.x, x.x, acc.x);
+    acc.x = fmadd(-m.y, x.y, acc.x);
+    acc.y = fmadd(m.x, x.y, acc.y);
+    acc.y = fmadd(m.y, x.x, acc.y);
+}
+
 // Compensated sums on the FP32 pipe (GB300's FP64 rate is a small fraction
 // of its FP32 rate).  FAcc holds an unevaluated float sum hi + lo: add() is
 // Knuth's TwoSum (the rounding error of each addition is kept in lo), and

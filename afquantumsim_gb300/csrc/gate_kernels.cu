@@ -304,8 +304,7 @@ k_matk(typename Cx<R>::T* __restrict__ sv, FX fx, uint64_t units, const MK<R, K>
 #pragma unroll
         for (int c = 0; c < D; ++c) {
             const T mm = mk.m[r * D + c];
-            acc.x += mm.x * v[c].x - mm.y * v[c].y;
-            acc.y += mm.x * v[c].y + mm.y * v[c].x;
+            cmac(acc, mm, v[c]);
         }
         sv[base + mk.off[r]] = acc;
     }

@@ -1233,8 +1233,7 @@ __global__ void k_wait_selftest(uint64_t limit_ns, int* timed_out) {
     __shared__ uint64_t bar;
     const uint32_t a = (uint32_t)__cvta_generic_to_shared(&bar);
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(1) : "memory");
-    uint64_t t0;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    WaitClock clk;
     uint32_t ok = 0;
     for (uint32_t it = 0;; ++it) {
         asm volatile(
@@ -1243,9 +1242,7 @@ __global__ void k_wait_selftest(uint64_t limit_ns, int* timed_out) {
             "selp.u32 %0, 1, 0, p;\n\t}"
             : "=r"(ok) : "r"(a), "r"(0u) : "memory");
         if (ok) break;
-        uint64_t t;
-        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-        if (t - t0 > limit_ns) break;
+        if ((it & 63u) == 63u && clk.expired(limit_ns)) break;
     }
     *timed_out = ok ? 0 : 1;
 }

@@ -74,14 +74,6 @@ __device__ __forceinline__ uint32_t tile_tid(uint32_t nthr) { return threadIdx.x
 
 // ---- asynchronous copies and barriers (sm_90+ bulk copies, mbarriers) -----------
 
-constexpr uint64_t kWaitNs = 200000000ull;  // 0.2 s per bounded wait
-
-__device__ __forceinline__ uint64_t globaltimer_ns() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
@@ -109,26 +101,25 @@ __device__ __forceinline__ uint32_t mbar_try_wait(uint64_t* bar, uint32_t parity
     return ok;
 }
 
-// Wait for the phase of `bar` with the given parity, at most kWaitNs of wall
-// time (for winding down: copies or MMAs already issued must land before
+// Wait for the phase of `bar` with the given parity, at most kWaitNs of
+// waiting (for winding down: copies or MMAs already issued must land before
 // the shared or tensor memory goes, whatever the error flag says).
 __device__ __forceinline__ bool mbar_wait_timeout(uint64_t* bar, uint32_t parity) {
-    const uint64_t t0 = globaltimer_ns();
+    WaitClock clk;
     for (uint32_t it = 0;; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 63u) == 63u && globaltimer_ns() - t0 > kWaitNs) return false;
+        if ((it & 63u) == 63u && clk.expired()) return false;
     }
 }
 
 // Wait for the phase of `bar` with the given parity; gives up after kWaitNs
-// of wall time, or early once the device error flag is set.  Returns whether
+// of waiting, or early once the device error flag is set.  Returns whether
 // the phase completed.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, const int* err) {
-    const uint64_t t0 = globaltimer_ns();
+    WaitClock clk;
     for (uint32_t it = 0;; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 63u) == 63u && (globaltimer_ns() - t0 > kWaitNs || *(volatile const int*)err != 0))
-            return false;
+        if ((it & 63u) == 63u && (clk.expired() || *(volatile const int*)err != 0)) return false;
     }
 }
 
@@ -467,8 +458,7 @@ __device__ __noinline__ void matk_apply(T* s, uint32_t size, uint32_t nthr, cons
                 const T mm = mat[r * D + c];
 #pragma unroll
                 for (int g = 0; g < G; ++g) {
-                    acc[g].x += mm.x * v[g][c].x - mm.y * v[g][c].y;
-                    acc[g].y += mm.x * v[g][c].y + mm.y * v[g][c].x;
+                    cmac(acc[g], mm, v[g][c]);
                 }
             }
             uint32_t off = 0;
@@ -791,8 +781,7 @@ __device__ __forceinline__ void r_matk(T (&vv)[SL][1 << RB], const bool (&on)[SL
 #pragma unroll
                 for (int c = 0; c < D; ++c) {
                     const T x = a[e0 | r_dep<RM, K>(c)];
-                    acc.x += row[c].x * x.x - row[c].y * x.y;
-                    acc.y += row[c].x * x.y + row[c].y * x.x;
+                    cmac(acc, row[c], x);
                 }
                 v[e0 | r_dep<RM, K>(r)] = acc;
             }

@@ -50,7 +50,7 @@ def parse_args():
     ap.add_argument("--dtype", choices=["c64", "c128"], default="c64")
     ap.add_argument("--mode", choices=["per_gate", "tiled"], default="per_gate")
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--only", choices=["fused_brickwork", "fused_tc", "tiled_brickwork", "plain12", "vqe_batch", "vqe_ansatz", "serving",
+    ap.add_argument("--only", choices=["fused_brickwork", "fused_tc", "fused_cc", "tiled_brickwork", "plain12", "vqe_batch", "vqe_ansatz", "serving",
                                        "qft_grid", "noise"],
                     help="run one secondary workload alone (at --n qubits where it takes a size) "
                          "and print its JSON; for profiling")
@@ -348,6 +348,27 @@ def bench_fused_tc(ctx, stream, n, depth):
     fused, src = prog.info()
     prog.free()
     return {"workload": f"brickwork{n}x{depth}", "gates": src, "fused_ops": fused, "fused_tensor_core_ms": round(ms, 2)}
+
+
+def bench_fused_cc(ctx, stream, n, depth, width=3):
+    """Only the brick-work program fused to `width` qubits on the CUDA cores
+    (tensor cores off; two untimed runs, then three timed): the launches a
+    profiler of the dense k-qubit tile path captures."""
+    import afquantumsim_gb300 as aq
+    from afquantumsim_gb300 import circuits
+    prog = aq.Program(n, circuits.brickwork(n, depth, seed=4), aq.C64, max_qubits=width)
+    ctx.set_tensor_cores(False)
+    with aq.State(ctx, n, aq.C64) as st:
+        st.set_basis(0)
+        prog.run(st, aq.EXEC_TILED)
+        prog.run(st, aq.EXEC_TILED)
+        ms = _time_ms(stream, lambda: prog.run(st, aq.EXEC_TILED), 3)
+    ctx.set_tensor_cores(True)
+    fused, src = prog.info()
+    plan = prog.plan(tensor_cores=False)
+    prog.free()
+    return {"workload": f"brickwork{n}x{depth}", "fuse_qubits": width, "gates": src, "fused_ops": fused,
+            "passes": plan["passes"], "fused_cuda_core_ms": round(ms, 2)}
 
 
 def bench_tiled_brickwork(ctx, stream, n, depth):
@@ -998,6 +1019,8 @@ def run_only(args):
             res = bench_fused_brickwork(ctx, st, stream, args.n, args.depth)
     elif args.only == "fused_tc":
         res = bench_fused_tc(ctx, stream, args.n, args.depth)
+    elif args.only == "fused_cc":
+        res = bench_fused_cc(ctx, stream, args.n, args.depth)
     elif args.only == "tiled_brickwork":
         res = bench_tiled_brickwork(ctx, stream, args.n, args.depth)
     elif args.only == "plain12":
