@@ -28,7 +28,7 @@ LIB_PATH = PKG_DIR / "_build" / "libaqsg.so"
 
 EXPORTS = [
     "aqsg_version", "aqsg_last_error", "aqsg_init", "aqsg_shutdown",
-    "aqsg_set_exec_mode", "aqsg_set_tensor_cores", "aqsg_synchronize", "aqsg_ctx_after", "aqsg_ctx_stream",
+    "aqsg_set_exec_mode", "aqsg_set_tensor_cores", "aqsg_set_whole_tile_max", "aqsg_synchronize", "aqsg_ctx_after", "aqsg_ctx_stream",
     "aqsg_launch_count",
     "aqsg_state_alloc", "aqsg_state_free", "aqsg_state_info",
     "aqsg_state_set_basis_index", "aqsg_state_set_product", "aqsg_state_upload",
@@ -93,6 +93,7 @@ def load_library(path: os.PathLike | str | None = None) -> C.CDLL:
         "aqsg_shutdown": ([P], I),
         "aqsg_set_exec_mode": ([P, I], I),
         "aqsg_set_tensor_cores": ([P, I], I),
+        "aqsg_set_whole_tile_max": ([P, I], I),
         "aqsg_synchronize": ([P], I),
         "aqsg_ctx_after": ([P, P], I),
         "aqsg_ctx_stream": ([P, C.POINTER(P)], I),
@@ -278,6 +279,12 @@ class Context:
 
     def set_tensor_cores(self, enable: bool) -> None:
         _check(self.lib.aqsg_set_tensor_cores(self.h, 1 if enable else 0))
+
+    def set_whole_tile_max(self, qubits: int) -> None:
+        """aqsg_set_whole_tile_max: registers of at most `qubits` qubits run
+        as one whole-register tile, larger ones in streaming tiles (0: the
+        default, 14 qubits c64 / 13 c128)."""
+        _check(self.lib.aqsg_set_whole_tile_max(self.h, qubits))
 
     def synchronize(self) -> None:
         _check(self.lib.aqsg_synchronize(self.h))
@@ -502,24 +509,25 @@ class TilePass(C.Structure):
                 ("tbits", C.c_int32 * 16)]
 
 
-def debug_tile_plan(n: int, ops, dtype: int = C64, fuse_qubits: int = 0):
+def debug_tile_plan(n: int, ops, dtype: int = C64, fuse_qubits: int = 0, whole_tile_max: int = 0):
     """aqsg_debug_tile_plan: (passes, table bytes, pool bytes) of the CUDA-core
-    tile plan the engine would run for ops (a testing aid)."""
+    tile plan the engine would run for ops (a testing aid); whole_tile_max as
+    set by Context.set_whole_tile_max (0: the default)."""
     lib = load_library()
     f = lib.aqsg_debug_tile_plan
-    f.argtypes = [C.c_int, C.c_int, C.POINTER(Op), C.c_int, C.c_int, C.POINTER(TilePass), C.c_int,
+    f.argtypes = [C.c_int, C.c_int, C.POINTER(Op), C.c_int, C.c_int, C.c_int, C.POINTER(TilePass), C.c_int,
                   C.POINTER(C.c_int), C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t), C.c_void_p, C.c_size_t,
                   C.POINTER(C.c_size_t)]
     f.restype = C.c_int
     arr = op_array(list(ops)) if not isinstance(ops, C.Array) else ops
     npass, tb, pb = C.c_int(), C.c_size_t(), C.c_size_t()
-    _check(f(n, dtype, arr, len(arr), fuse_qubits, None, 0, C.byref(npass), None, 0, C.byref(tb), None, 0,
-             C.byref(pb)))
+    _check(f(n, dtype, arr, len(arr), fuse_qubits, whole_tile_max, None, 0, C.byref(npass), None, 0, C.byref(tb),
+             None, 0, C.byref(pb)))
     passes = (TilePass * max(npass.value, 1))()
     table = C.create_string_buffer(max(tb.value, 1))
     pool = C.create_string_buffer(max(pb.value, 1))
-    _check(f(n, dtype, arr, len(arr), fuse_qubits, passes, npass.value, C.byref(npass), table, tb.value,
-             C.byref(tb), pool, pb.value, C.byref(pb)))
+    _check(f(n, dtype, arr, len(arr), fuse_qubits, whole_tile_max, passes, npass.value, C.byref(npass), table,
+             tb.value, C.byref(tb), pool, pb.value, C.byref(pb)))
     return list(passes[:npass.value]), table.raw[:tb.value], pool.raw[:pb.value]
 
 
@@ -872,7 +880,7 @@ class Server:
 class TuneEntry(C.Structure):
     """struct aqsg_tune_entry."""
     _fields_ = [("exec_mode", C.c_int32), ("fuse_qubits", C.c_int32), ("tensor_cores", C.c_int32),
-                ("ops", C.c_int32), ("ms", C.c_double)]
+                ("ops", C.c_int32), ("ms", C.c_double), ("tile_bits", C.c_int32), ("reserved", C.c_int32)]
 
 
 def autotune(ctx: Context, n: int, ops, dtype: int = C64, reps: int = 2, all_timings: bool = True):
@@ -888,9 +896,9 @@ def autotune(ctx: Context, n: int, ops, dtype: int = C64, reps: int = 2, all_tim
         a = ops if isinstance(ops, C.Array) else op_array(list(ops))
         ptr, count = C.cast(a, C.POINTER(Op)), len(a)
     best = TuneEntry()
-    buf = (TuneEntry * 16)()
+    buf = (TuneEntry * 32)()
     k = C.c_int()
     _check(lib.aqsg_autotune(ctx.h, n, dtype, ptr, count, reps, C.byref(best), buf if all_timings else None,
-                             16, C.byref(k)))
+                             32, C.byref(k)))
     conv = lambda e: {f: getattr(e, f) for f, _ in TuneEntry._fields_}
     return conv(best), [conv(e) for e in buf[:k.value]]

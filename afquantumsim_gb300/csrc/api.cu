@@ -361,6 +361,13 @@ int aqsg_set_tensor_cores(aqsg_ctx ctx, int enable) {
     return AQSG_OK;
 }
 
+int aqsg_set_whole_tile_max(aqsg_ctx ctx, int qubits) {
+    if (!ctx) return set_error(AQSG_ERR_NULL, "NULL context");
+    if (qubits < 0) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Negative whole-tile qubit count");
+    ctx->whole_tile_max = qubits;
+    return AQSG_OK;
+}
+
 int aqsg_synchronize(aqsg_ctx ctx) {
     if (!ctx) return set_error(AQSG_ERR_NULL, "NULL context");
     AQSG_ON_DEVICE(ctx->device);

@@ -119,6 +119,7 @@ struct aqsg_ctx_s {
     double* host_result = nullptr;  // pinned FP64 results
     int* d_err = nullptr;           // device flag: a bounded kernel wait gave up
     int tensor_cores = 1;           // fused unitaries on tcgen05 (c64 tiles)
+    int whole_tile_max = 0;         // largest register run as one tile (0: the dtype's maximum)
     cudaEvent_t order = nullptr;    // marks this stream's queue for aqsg_ctx_after
     aqsg::PlanCache* plans = nullptr;  // recently run tile plans (host + device copies)
 };
@@ -166,7 +167,10 @@ struct TilePlan {
 // exact_perm: fused permutation matrices stay off the tensor cores (bit-exact
 // moves); false makes the choice depend on the op structure only.
 bool relocate_tile_matrices(unsigned char* table, size_t count, int32_t delta);
-int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, TilePlan* plan, bool exact_perm = true);
+// whole_max: the largest register encoded as one whole-register tile (0: the
+// dtype's maximum, tile_max_bits; clamped to [stream_tile_bits, tile_max_bits]).
+int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, TilePlan* plan, bool exact_perm = true,
+                 int whole_max = 0);
 // Launch the passes on `stream`; dev = device copy of table + pool.
 // norm_part (optional, 2 x tc_grid doubles): the first pass, when it runs on
 // the tensor cores, writes per-CTA FP64 partial sums of |a|^2 of its input
@@ -190,6 +194,10 @@ int run_tiled_cached(aqsg_state_s* st, const std::vector<unsigned char>& key,
 void plan_cache_free(aqsg_ctx_s* c);
 // Largest tile (log2 amplitudes) the tile kernel holds for a dtype.
 int tile_max_bits(int dtype);
+// Tile of a streaming pass (log2 amplitudes) for a dtype.
+int stream_tile_bits(int dtype);
+// The whole-register limit a setting of aqsg_set_whole_tile_max gives.
+int whole_tile_limit(int dtype, int setting);
 // Algorithmic HBM bytes of running a plan once: one read and one write of
 // the register per tile pass; with renorm, a run with tensor-core passes
 // also reads the register twice for its norms and rescales it once.

@@ -28,7 +28,11 @@
 namespace aqsg {
 
 int tile_max_bits(int dtype) { return dtype == AQSG_C64 ? 14 : 13; }
-static int stream_tile_bits(int dtype) { return dtype == AQSG_C64 ? 12 : 11; }
+int stream_tile_bits(int dtype) { return dtype == AQSG_C64 ? 12 : 11; }
+int whole_tile_limit(int dtype, int setting) {
+    if (setting <= 0) return tile_max_bits(dtype);
+    return std::max(stream_tile_bits(dtype), std::min(setting, tile_max_bits(dtype)));
+}
 static int row_bits(int dtype) { return dtype == AQSG_C64 ? 5 : 4; }
 
 // Shared-memory layout of the CUDA-core tile kernels: XOR-swizzled in groups
@@ -641,9 +645,9 @@ static size_t tc_op_bytes(int k);
 // tc_budget: tensor-core passes (c64): a pass also stops taking fused
 // unitaries of 3+ qubits once their operands would exceed the shared-memory
 // blob of the kernel.
-static std::vector<Pass> plan(int n, int dtype, const std::vector<LOp>& ops, bool tc_budget) {
+static std::vector<Pass> plan(int n, int dtype, const std::vector<LOp>& ops, bool tc_budget, int whole_max) {
     std::vector<Pass> passes;
-    const bool whole = n <= tile_max_bits(dtype);
+    const bool whole = n <= whole_tile_limit(dtype, whole_max);
     const int m = whole ? n : stream_tile_bits(dtype);
     const int L = whole ? n : row_bits(dtype);
     const uint64_t rowmask = (L >= 64) ? ~0ull : ((1ull << L) - 1ull);
@@ -1147,7 +1151,8 @@ bool relocate_tile_matrices(unsigned char* table, size_t count, int32_t delta) {
     return any;
 }
 
-int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, TilePlan* plan, bool exact_perm) {
+int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, TilePlan* plan, bool exact_perm,
+                 int whole_max) {
     plan->table.clear();
     plan->pool.clear();
     plan->passes.clear();
@@ -1155,7 +1160,7 @@ int encode_tiled(int n, int dtype, const std::vector<LOp>& ops, bool tc_on, Tile
     plan->any_stream = false;
     plan->n = n;
     plan->dtype = dtype;
-    std::vector<Pass> passes = aqsg::plan(n, dtype, ops, tc_on && dtype == AQSG_C64);
+    std::vector<Pass> passes = aqsg::plan(n, dtype, ops, tc_on && dtype == AQSG_C64, whole_max);
     const size_t tsize = sizeof(TileOp);
     for (const Pass& p : passes) {
         TilePass tp;
@@ -1597,11 +1602,15 @@ uint64_t plan_run_bytes(const TilePlan& plan) {
     return b;
 }
 
-int run_tiled_cached(aqsg_state_s* st, const std::vector<unsigned char>& key,
+int run_tiled_cached(aqsg_state_s* st, const std::vector<unsigned char>& key_ops,
                      const std::function<int(std::vector<LOp>*)>& lower) {
     aqsg_ctx_s* c = st->ctx;
     if (!c->plans) c->plans = new PlanCache();
     PlanCache& pc = *c->plans;
+    // the tile shape is part of the plan
+    const int32_t whole_max = whole_tile_limit(st->dtype, c->whole_tile_max);
+    std::vector<unsigned char> key = key_ops;
+    key.insert(key.end(), (const unsigned char*)&whole_max, (const unsigned char*)&whole_max + sizeof(whole_max));
     for (auto& en : pc.e)
         if (en.key == key) {
             en.last = ++pc.tick;
@@ -1612,7 +1621,7 @@ int run_tiled_cached(aqsg_state_s* st, const std::vector<unsigned char>& key,
     if (int rc = lower(&ops)) return rc;
     PlanCache::Entry fresh;
     fresh.key = key;
-    if (int rc = encode_tiled(st->n, st->dtype, ops, c->tensor_cores != 0, &fresh.plan)) return rc;
+    if (int rc = encode_tiled(st->n, st->dtype, ops, c->tensor_cores != 0, &fresh.plan, true, whole_max)) return rc;
     // the slot: a free one, else the least recently used (its device table
     // is reused when large enough)
     PlanCache::Entry* slot = nullptr;
@@ -1667,7 +1676,7 @@ int run_plan_async(aqsg_state_s* st, const TilePlan& plan, const void* dev_table
 #include "../../include/aqsg_debug.h"
 
 extern "C" int aqsg_debug_tile_plan(int n, int dtype, const aqsg_op* ops, int count, int fuse_qubits,
-                                    aqsg_tile_pass* passes, int pass_capacity, int* pass_count,
+                                    int whole_tile_max, aqsg_tile_pass* passes, int pass_capacity, int* pass_count,
                                     void* table, size_t table_capacity, size_t* table_bytes, void* pool,
                                     size_t pool_capacity, size_t* pool_bytes) {
     using namespace aqsg;
@@ -1688,7 +1697,8 @@ extern "C" int aqsg_debug_tile_plan(int n, int dtype, const aqsg_op* ops, int co
         }
     }
     TilePlan plan;
-    if (int rc = encode_tiled(n, dtype, low, false, &plan)) return rc;
+    if (whole_tile_max < 0) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Negative whole-tile qubit count");
+    if (int rc = encode_tiled(n, dtype, low, false, &plan, true, whole_tile_max)) return rc;
     if (pass_count) *pass_count = (int)plan.passes.size();
     if (table_bytes) *table_bytes = plan.table.size();
     if (pool_bytes) *pool_bytes = plan.pool.size();

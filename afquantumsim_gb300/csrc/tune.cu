@@ -1,7 +1,9 @@
 // Autotuner: picks how a circuit runs — one kernel pass per gate, tile passes,
 // or tile passes over a program fused into unitaries of 2..5 qubits (with or
-// without the tensor cores) — by timing each choice on a scratch register of
-// the circuit's size.  Results are cached per context by the circuit's
+// without the tensor cores), and for registers of 13-14 qubits (c64) / 12-13
+// (c128) the tile shape: the whole register in one CTA's tile, or streaming
+// tiles of 2^12 / 2^11 amplitudes over several CTAs — by timing each choice
+// on a scratch register of the circuit's size.  Results are cached per context by the circuit's
 // structure (gate kinds and operands, not angles or matrix entries), so a
 // parameter sweep tunes once.
 #include <algorithm>
@@ -87,16 +89,24 @@ int autotune_impl(aqsg_ctx ctx, int n, int dtype, const aqsg_op* ops, int count,
         }
     }
 
+    // tile: the largest register run as one tile (aqsg_set_whole_tile_max);
+    // a register of more qubits than a streaming tile that still fits one
+    // whole-register tile is timed in both shapes
     struct Cand {
-        int mode, fuse, tc;
+        int mode, fuse, tc, tile;
     };
+    const int whole = tile_max_bits(dtype), stream = stream_tile_bits(dtype);
+    std::vector<int> shapes = {whole};
+    if (n > stream && n <= whole) shapes.push_back(stream);
     std::vector<Cand> cands;
-    if (!tiled_only) cands.push_back({AQSG_EXEC_PER_GATE, 0, 0});
-    cands.push_back({AQSG_EXEC_TILED, 0, 0});
-    cands.push_back({AQSG_EXEC_TILED, 1, 0});  // consecutive 1-qubit gates merged
-    for (int k = 2; k <= AQSG_MAX_UNITARY_QUBITS; ++k) {
-        cands.push_back({AQSG_EXEC_TILED, k, 0});
-        if (dtype == AQSG_C64) cands.push_back({AQSG_EXEC_TILED, k, 1});
+    if (!tiled_only) cands.push_back({AQSG_EXEC_PER_GATE, 0, 0, 0});
+    for (int shape : shapes) {
+        cands.push_back({AQSG_EXEC_TILED, 0, 0, shape});
+        cands.push_back({AQSG_EXEC_TILED, 1, 0, shape});  // consecutive 1-qubit gates merged
+        for (int k = 2; k <= AQSG_MAX_UNITARY_QUBITS; ++k) {
+            cands.push_back({AQSG_EXEC_TILED, k, 0, shape});
+            if (dtype == AQSG_C64) cands.push_back({AQSG_EXEC_TILED, k, 1, shape});
+        }
     }
 
     aqsg_state st = nullptr;
@@ -106,7 +116,7 @@ int autotune_impl(aqsg_ctx ctx, int n, int dtype, const aqsg_op* ops, int count,
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
         rc = set_error(AQSG_ERR_CUDA, "cudaEventCreate failed");
     if (rc == AQSG_OK) rc = aqsg_state_set_basis_index(st, 0);
-    const int saved_tc = ctx->tensor_cores;
+    const int saved_tc = ctx->tensor_cores, saved_tile = ctx->whole_tile_max;
     std::vector<aqsg_tune_entry> results;
     for (const Cand& c : cands) {
         if (rc != AQSG_OK) break;
@@ -117,6 +127,7 @@ int autotune_impl(aqsg_ctx ctx, int n, int dtype, const aqsg_op* ops, int count,
             aqsg_program_info(prog, &fused, nullptr);
         }
         ctx->tensor_cores = c.tc;
+        ctx->whole_tile_max = c.tile;
         auto run = [&]() {
             return prog ? aqsg_run_program(st, prog, c.mode) : aqsg_apply_ops(st, ops, count, c.mode);
         };
@@ -137,11 +148,13 @@ int autotune_impl(aqsg_ctx ctx, int n, int dtype, const aqsg_op* ops, int count,
             en.tensor_cores = c.tc;
             en.ops = fused;
             en.ms = (double)ms / reps;
+            en.tile_bits = c.mode == AQSG_EXEC_PER_GATE ? 0 : (n <= c.tile ? n : stream);
             results.push_back(en);
         }
         if (prog) aqsg_program_free(prog);
     }
     ctx->tensor_cores = saved_tc;
+    ctx->whole_tile_max = saved_tile;
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     aqsg_state_free(st);
@@ -295,6 +308,7 @@ int autotune_grouped(aqsg_ctx ctx, int n, const aqsg_op* ops, int count, int* fu
     en.fuse_qubits = best_fuse;
     en.tensor_cores = best_tc;
     en.ms = best_ms / replicas;
+    en.tile_bits = n <= tile_max_bits(AQSG_C64) ? n : stream_tile_bits(AQSG_C64);
     {
         std::lock_guard<std::mutex> g(cache.mu);
         cache.best[{(const void*)ctx, key}] = en;

@@ -50,7 +50,7 @@ def parse_args():
     ap.add_argument("--dtype", choices=["c64", "c128"], default="c64")
     ap.add_argument("--mode", choices=["per_gate", "tiled"], default="per_gate")
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--only", choices=["fused_brickwork", "fused_tc", "fused_cc", "tiled_brickwork", "plain12", "vqe_batch", "vqe_ansatz", "serving",
+    ap.add_argument("--only", choices=["fused_brickwork", "fused_tc", "fused_cc", "tiled_brickwork", "plain12", "tile_shape", "vqe_batch", "vqe_ansatz", "serving",
                                        "qft_grid", "noise"],
                     help="run one secondary workload alone (at --n qubits where it takes a size) "
                          "and print its JSON; for profiling")
@@ -408,6 +408,30 @@ def bench_noise(ctx, n=12, layers=8, trajectories=4096, seed=7):
     return {"workload": f"ansatz{n}x{layers}_depolarizing", "gates": len(ops), "trajectories": trajectories,
             "seconds": round(dt, 3), "trajectories_per_s": round(trajectories / dt, 1),
             "max_std_err_z": float(np.max(ze)), "mean_z": float(np.mean(z))}
+
+
+def bench_tile_shape(ctx, sizes=(13, 14), depth=20, seed=4):
+    """Tile shape as the autotuner times it: a brick-work circuit on a
+    register that fits one whole-register tile (one CTA, one launch) run in
+    that shape and in streaming 4096-amplitude tiles (several CTAs, one
+    launch per pass), every execution choice in each; c64."""
+    import afquantumsim_gb300 as aq
+    from afquantumsim_gb300 import circuits
+    out = {}
+    for n in sizes:
+        ops = aq.op_array(circuits.brickwork(n, depth, seed=seed))
+        best, every = aq.autotune(ctx, n, ops, aq.C64, reps=3)
+        per_shape = {}
+        for e in every:
+            if e["exec_mode"] != aq.EXEC_TILED:
+                continue
+            key = "whole" if e["tile_bits"] == n else f"stream{e['tile_bits']}"
+            name = f"fuse{e['fuse_qubits']}{'_tc' if e['tensor_cores'] else ''}"
+            per_shape.setdefault(key, {})[name] = round(e["ms"] * 1e3, 1)
+        out[f"brickwork{n}x{depth}"] = {
+            "best": {k: best[k] for k in ("exec_mode", "fuse_qubits", "tensor_cores", "tile_bits")},
+            "best_us": round(best["ms"] * 1e3, 1), "tiled_us": per_shape}
+    return out
 
 
 def bench_qft_grid(ctx, stream, sizes=((24, "c64"), (28, "c64"), (24, "c128"), (28, "c128"), (30, "c128"))):
@@ -885,6 +909,7 @@ def run_ours(args, rank, world, local_rank):
             extras["fused_brickwork"] = bench_fused_brickwork(ctx, st, stream, n, depth=20)
         extras["qft_grid"] = bench_qft_grid(ctx, stream)
         extras["plain12"] = bench_plain12(ctx, stream)
+        extras["tile_shape"] = bench_tile_shape(ctx)
         extras["vqe_batch"] = bench_vqe_batch(ctx)
         extras["noise"] = bench_noise(ctx)
         if args.dtype == "c64":
@@ -1029,6 +1054,8 @@ def run_only(args):
         res = bench_noise(ctx)
     elif args.only == "qft_grid":
         res = bench_qft_grid(ctx, stream)
+    elif args.only == "tile_shape":
+        res = bench_tile_shape(ctx)
     elif args.only == "vqe_batch":
         res = bench_vqe_batch(ctx, count=args.count or 4096)
     elif args.only == "vqe_ansatz":

@@ -159,6 +159,17 @@ int aqsg_set_exec_mode(aqsg_ctx ctx, int mode);
  * is non-zero (the default); otherwise on the CUDA cores in FP32. */
 int aqsg_set_tensor_cores(aqsg_ctx ctx, int enable);
 
+/* Tile shape of tile passes on this context.  A register of at most
+ * `qubits` qubits runs as ONE tile: one CTA holds the whole register in
+ * shared memory and runs every op of the circuit in a single launch.  A
+ * larger register streams through tiles of 2^12 (c64) / 2^11 (c128)
+ * amplitudes, one CTA per tile and one launch per pass; only streaming
+ * tiles of 2^12 c64 amplitudes run fused unitaries on the tensor cores.
+ * qubits is clamped at use to [12, 14] for c64 and [11, 13] for c128;
+ * 0 restores the default (14 / 13).  Negative: AQSG_ERR_INVALID_ARGUMENT.
+ * The reference has no counterpart (it has no tiles). */
+int aqsg_set_whole_tile_max(aqsg_ctx ctx, int qubits);
+
 /* Wait for all work queued on the context's stream. */
 int aqsg_synchronize(aqsg_ctx ctx);
 
@@ -317,12 +328,19 @@ typedef struct aqsg_tune_entry {
     int32_t tensor_cores;  /* fused unitaries on the tensor cores (c64)         */
     int32_t ops;           /* ops after fusion                                  */
     double ms;             /* device time of one run                           */
+    int32_t tile_bits;     /* tile passes: log2 of the amplitudes one CTA holds
+                            * (n = the whole register in one tile; to run this
+                            * way set aqsg_set_whole_tile_max below n);
+                            * 0 for one gate per pass                          */
+    int32_t reserved;      /* 0                                                */
 } aqsg_tune_entry;
 
 /* Time the circuit (on a scratch n-qubit register of dtype, from |0...0>)
  * one gate per pass, in tile passes, compiled with fusion width 1 (runs of
  * 1-qubit gates merged) and with widths 2..5 with and without the tensor
- * cores; reps timed runs each after one warm-up.
+ * cores; reps timed runs each after one warm-up.  A register that fits one
+ * whole-register tile but is larger than a streaming tile (13-14 qubits
+ * c64, 12-13 c128) has every tile-pass candidate timed in both tile shapes.
  * *best receives the fastest.  The choice is cached per context by the
  * circuit's structure (kinds and operands, not angles or matrix entries):
  * with all == NULL a cached choice returns at once.  all (capacity entries,

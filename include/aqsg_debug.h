@@ -23,12 +23,13 @@ typedef struct aqsg_tile_pass {
 
 /* The tile-pass plan aqsg_apply_ops would run for ops in AQSG_EXEC_TILED mode
  * on an n-qubit register of dtype, the CUDA-core form (no tensor cores),
- * after fusing at fuse_qubits (0: the gates as they are): the passes, the
- * op table (160-byte records: the engine's tile ops and register-phase ops)
- * and the operand pool, byte for byte as they are uploaded.  Call with NULL
- * buffers to get the counts and sizes. */
+ * after fusing at fuse_qubits (0: the gates as they are), on a context whose
+ * aqsg_set_whole_tile_max setting is whole_tile_max (0: the default): the
+ * passes, the op table (160-byte records: the engine's tile ops and
+ * register-phase ops) and the operand pool, byte for byte as they are
+ * uploaded.  Call with NULL buffers to get the counts and sizes. */
 int aqsg_debug_tile_plan(int n, int dtype, const aqsg_op* ops, int count, int fuse_qubits,
-                         aqsg_tile_pass* passes, int pass_capacity, int* pass_count,
+                         int whole_tile_max, aqsg_tile_pass* passes, int pass_capacity, int* pass_count,
                          void* table, size_t table_capacity, size_t* table_bytes,
                          void* pool, size_t pool_capacity, size_t* pool_bytes);
 

@@ -14,7 +14,8 @@ CSRC = ROOT / "afquantumsim_gb300" / "csrc"
 # on the host, or work queued by the server's own worker thread, which makes
 # its device current when it starts)
 HOST_ONLY = {
-    "aqsg_version", "aqsg_last_error", "aqsg_set_exec_mode", "aqsg_set_tensor_cores", "aqsg_ctx_stream",
+    "aqsg_version", "aqsg_last_error", "aqsg_set_exec_mode", "aqsg_set_tensor_cores", "aqsg_set_whole_tile_max",
+    "aqsg_ctx_stream",
     "aqsg_launch_count", "aqsg_state_info", "aqsg_check_ops", "aqsg_compile", "aqsg_program_info",
     "aqsg_program_export", "aqsg_program_free", "aqsg_circuit_to_text", "aqsg_circuit_from_text",
     "aqsg_batch_info", "aqsg_batch_tuning", "aqsg_batch_traffic", "aqsg_debug_tile_plan", "aqsg_debug_batch_image",

@@ -51,3 +51,70 @@ def test_autotune_c128_has_no_tensor_core_candidates(gpu_ctx):
     ops = circuits.plain_layers(10, 3, seed=2)
     best, every = aq.autotune(gpu_ctx, 10, ops, aq.C128, reps=1)
     assert len(every) == 3 + 4 and not any(e["tensor_cores"] for e in every)
+
+
+def _run_way(ctx, n, ops, dtype, npdt, v, fuse, tc, mode=aq.EXEC_TILED):
+    with aq.State(ctx, n, dtype) as st:
+        st.upload(v.astype(npdt))
+        ctx.set_tensor_cores(bool(tc))
+        try:
+            if fuse:
+                p = aq.Program(n, ops, dtype, max_qubits=fuse)
+                p.run(st, mode)
+                p.free()
+            else:
+                st.apply(ops, mode)
+        finally:
+            ctx.set_tensor_cores(True)
+        return st.download()
+
+
+@pytest.mark.parametrize("dtype,npdt,n", [(aq.C64, np.complex64, 13), (aq.C64, np.complex64, 14),
+                                          (aq.C128, np.complex128, 12), (aq.C128, np.complex128, 13)])
+def test_streaming_tile_shape_matches_oracle(gpu_ctx, dtype, npdt, n):
+    # registers that fit one whole-register tile, run in streaming tiles
+    # instead (several CTAs, one launch per pass; c64 fused unitaries on the
+    # tensor cores): the oracle's state, as in the whole-register shape
+    stream = 12 if dtype == aq.C64 else 11
+    ops = circuits.brickwork(n, 8, seed=n)
+    v = _kat.random_state(n, 7)
+    want = oracle.apply_f64(v.copy(), ops)
+    tol = 1e-5 if dtype == aq.C64 else 1e-12
+    ways = [(0, 0), (2, 0), (5, 0)] + ([(3, 1), (5, 1)] if dtype == aq.C64 else [])
+    for shape in (stream, 0):
+        gpu_ctx.set_whole_tile_max(shape)
+        try:
+            for fuse, tc in ways:
+                got = _run_way(gpu_ctx, n, ops, dtype, npdt, v, fuse, tc)
+                assert np.max(np.abs(got - want)) < tol, (shape, fuse, tc)
+        finally:
+            gpu_ctx.set_whole_tile_max(0)
+
+
+def test_autotune_times_both_tile_shapes(gpu_ctx):
+    n = 14
+    ops = circuits.brickwork(n, 10, seed=5)
+    best, every = aq.autotune(gpu_ctx, n, ops, aq.C64, reps=1)
+    tiled = [(e["fuse_qubits"], e["tensor_cores"]) for e in every if e["exec_mode"] == aq.EXEC_TILED]
+    assert len(every) == 1 + 2 * 10
+    assert {e["tile_bits"] for e in every} == {0, 12, 14}
+    for bits in (12, 14):
+        assert sorted((e["fuse_qubits"], e["tensor_cores"]) for e in every if e["tile_bits"] == bits) == \
+            sorted(set(tiled))
+    assert all(e["tile_bits"] == 0 for e in every if e["exec_mode"] == aq.EXEC_PER_GATE)
+    assert best["ms"] == min(e["ms"] for e in every)
+    # run it the chosen way, tile shape included, and compare with the oracle
+    v = _kat.random_state(n, 2)
+    want = oracle.apply_f64(v.copy(), ops)
+    gpu_ctx.set_whole_tile_max(best["tile_bits"] if 0 < best["tile_bits"] < n else 0)
+    try:
+        got = _run_way(gpu_ctx, n, ops, aq.C64, np.complex64, v, best["fuse_qubits"], best["tensor_cores"],
+                       best["exec_mode"])
+    finally:
+        gpu_ctx.set_whole_tile_max(0)
+    assert np.max(np.abs(got - want)) < 1e-5
+
+
+def test_whole_tile_max_rejects_negative(gpu_ctx):
+    with pytest.raises(aq.InvalidArgument):
+        gpu_ctx.set_whole_tile_max(-1)

@@ -38,3 +38,30 @@ def test_vqe_plan_uses_register_phases():
     v = _kat.random_state(n, 3)
     got = run_plan(v, n, passes, table, pool, c64=True)
     assert np.max(np.abs(got - oracle.apply_f64(v.copy(), ops))) < 1e-5
+
+
+@pytest.mark.parametrize("dtype,n,fuse,seed", [(aq.C64, 13, 0, 11), (aq.C64, 14, 2, 12), (aq.C64, 14, 5, 13),
+                                               (aq.C128, 12, 0, 14), (aq.C128, 13, 3, 15)])
+def test_streaming_tile_shape_for_small_registers(dtype, n, fuse, seed):
+    # a register that fits one whole-register tile, encoded with the
+    # whole-tile limit lowered to the streaming tile: streaming passes of
+    # 2^12 (c64) / 2^11 (c128) amplitudes that still give the oracle's state
+    stream = 12 if dtype == aq.C64 else 11
+    ops = _kat.random_circuit(n, 150, seed)
+    whole, _, _ = aq.debug_tile_plan(n, ops, dtype, fuse)
+    assert [p.m for p in whole] == [n]
+    passes, table, pool = aq.debug_tile_plan(n, ops, dtype, fuse, whole_tile_max=stream)
+    assert passes and all(p.m == stream and p.L == (5 if dtype == aq.C64 else 4) for p in passes)
+    # a limit above the dtype's maximum is clamped: the whole register again
+    again, _, _ = aq.debug_tile_plan(n, ops, dtype, fuse, whole_tile_max=40)
+    assert [p.m for p in again] == [n]
+    v = _kat.random_state(n, seed)
+    want = oracle.apply_f64(v.copy(), ops)
+    got = run_plan(v, n, passes, table, pool, c64=(dtype == aq.C64))
+    tol = 1e-5 if dtype == aq.C64 else 1e-12
+    assert np.max(np.abs(got - want)) < tol
+
+
+def test_whole_tile_limit_rejects_negative():
+    with pytest.raises(aq.InvalidArgument):
+        aq.debug_tile_plan(13, _kat.random_circuit(13, 10, 1), aq.C64, 0, whole_tile_max=-1)
