@@ -159,7 +159,8 @@ int aqsg_set_exec_mode(aqsg_ctx ctx, int mode);
  * is non-zero (the default); otherwise on the CUDA cores in FP32. */
 int aqsg_set_tensor_cores(aqsg_ctx ctx, int enable);
 
-/* Tile shape of tile passes on this context.  A register of at most
+/* Tile shape of the tile passes that aqsg_apply_ops and aqsg_run_program
+ * run on this context (batches and servers plan their own).  A register of at most
  * `qubits` qubits runs as ONE tile: one CTA holds the whole register in
  * shared memory and runs every op of the circuit in a single launch.  A
  * larger register streams through tiles of 2^12 (c64) / 2^11 (c128)
