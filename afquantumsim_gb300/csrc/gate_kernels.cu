@@ -252,6 +252,77 @@ k_diag1(typename Cx<R>::T* __restrict__ sv, FX fx, uint64_t units, typename Cx<R
     }
 }
 
+// DIAG1 whose pattern fixes index bit 0 or 1 (complex64) / bit 0
+// (complex128): the changed amplitudes then fill only part of each 32-byte
+// DRAM sector, which is read and written in full all the same.  Each thread
+// takes whole aligned blocks of BLK amplitudes (one sector: 4 complex64 / 2
+// complex128), multiplies the elements j of the pattern ((j & lowmask) ==
+// lowval) by the phase and writes the block back whole, so every access is
+// a 16-byte one and every sector write a full one.  fx expands the block's
+// index over the pattern's other fixed bits.
+template <typename R, int BLK, typename FX>
+__global__ void __launch_bounds__(kThreads)
+k_diag1_blk(typename Cx<R>::T* __restrict__ sv, FX fx, uint64_t blocks, typename Cx<R>::T ph, DFCoef phd,
+            uint32_t lowmask, uint32_t lowval) {
+    using T = typename Cx<R>::T;
+    constexpr int IT = 2;
+    static_assert(BLK * sizeof(T) == 32, "one block is one 32-byte sector");
+    const uint64_t first = (uint64_t)blockIdx.x * (kThreads * IT) + threadIdx.x;
+    T a[IT][BLK];
+    uint64_t idx[IT];
+    bool ok[IT];
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+        const uint64_t u = first + (uint64_t)it * kThreads;
+        ok[it] = u < blocks;
+        if (ok[it]) {
+            idx[it] = fx.expand(u * BLK);
+            if constexpr (sizeof(R) == 4) {
+                const float4* p = reinterpret_cast<const float4*>(sv) + (idx[it] >> 1);
+                const float4 f0 = __ldcs(p), f1 = __ldcs(p + 1);
+                a[it][0] = make_float2(f0.x, f0.y);
+                a[it][1] = make_float2(f0.z, f0.w);
+                a[it][2] = make_float2(f1.x, f1.y);
+                a[it][3] = make_float2(f1.z, f1.w);
+            } else {
+#pragma unroll
+                for (int j = 0; j < BLK; ++j) a[it][j] = __ldcs(sv + idx[it] + j);
+            }
+        }
+    }
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+        if (!ok[it]) continue;
+#pragma unroll
+        for (int j = 0; j < BLK; ++j) {
+            if (((uint32_t)j & lowmask) != lowval) continue;  // the same j for the whole warp
+            if constexpr (sizeof(R) == 8) {
+                bool wide = false;
+                const float2 xr = df_split(a[it][j].x, wide), xi = df_split(a[it][j].y, wide);
+                if (__any_sync(__activemask(), wide)) {
+                    diag_fp64(ph, a[it][j]);
+                } else {
+                    DFAcc re = df_mul(xr, phd.re), im = df_mul(xi, phd.re);
+                    df_madd(re, xi, df_neg(phd.im));
+                    df_madd(im, xr, phd.im);
+                    a[it][j].x = df_join(re);
+                    a[it][j].y = df_join(im);
+                }
+            } else {
+                a[it][j] = cmul(ph, a[it][j]);
+            }
+        }
+        if constexpr (sizeof(R) == 4) {
+            float4* p = reinterpret_cast<float4*>(sv) + (idx[it] >> 1);
+            __stcs(p, make_float4(a[it][0].x, a[it][0].y, a[it][1].x, a[it][1].y));
+            __stcs(p + 1, make_float4(a[it][2].x, a[it][2].y, a[it][3].x, a[it][3].y));
+        } else {
+#pragma unroll
+            for (int j = 0; j < BLK; ++j) __stcs(sv + idx[it] + j, a[it][j]);
+        }
+    }
+}
+
 // ---- PERM_SWAP: exchange (a=0,b=1) with (a=1,b=0) ---------------------------
 template <typename R, int VEC, typename FX>
 __global__ void __launch_bounds__(kThreads)
@@ -357,6 +428,7 @@ static void with_fix(const FixedBits& f, int n, Fn&& fn) {
         return;
     }
     switch (f.nf) {
+        case 0: fn(to_fix32<0>(f)); break;
         case 1: fn(to_fix32<1>(f)); break;
         case 2: fn(to_fix32<2>(f)); break;
         case 3: fn(to_fix32<3>(f)); break;
@@ -445,6 +517,19 @@ static int launch_typed(aqsg_state_s* st, const LOp& op) {
             uint64_t units = N >> f.nf;
             const T ph = cval<R>(op.m[0], op.m[1]);
             const DFCoef phd = df_coef(op.m[0], op.m[1]);
+            // the index bits inside one 32-byte sector: 0-1 (complex64), 0 (complex128)
+            constexpr int BLK = sizeof(R) == 4 ? 4 : 2;
+            const uint64_t low = (uint64_t)BLK - 1u;
+            if ((f.mask & low) != 0 && N >= (uint64_t)BLK) {
+                const FixedBits fb = make_fixed(f.mask & ~low, f.val & ~low);
+                const uint64_t blocks = (N >> fb.nf) / BLK;
+                const unsigned grid = grid_for(blocks, kThreads * 2);
+                with_fix(fb, st->n, [&](auto fx) {
+                    k_diag1_blk<R, BLK, decltype(fx)><<<grid, kThreads, 0, st->ctx->stream>>>(
+                        (T*)st->d, fx, blocks, ph, phd, (uint32_t)(f.mask & low), (uint32_t)(f.val & low));
+                });
+                break;
+            }
             const bool vec2 = is_f && (f.mask & 1ull) == 0;
             if (vec2) {
                 units >>= 1;

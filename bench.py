@@ -786,7 +786,7 @@ def run_ours(args, rank, world, local_rank):
                 "achieved": round(cp_achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(cp_achieved / peak, 4), "peak_source": peak_kind,
                 "traffic": traffic_per_launch(n, args.dtype),
-                "traffic_note": "ncu mean over the CPhase launches of a 26-qubit QFT, scaled by 2^(n-26)",
+                "traffic_note": "ncu mean over the 378 CPhase launches of a 28-qubit QFT, scaled by 2^(n-28)",
                 "algorithmic_bytes_per_launch": per_kind["CPhase"],
                 "ms_per_launch": round(cp_ms, 4)}
     kernels = {
@@ -960,17 +960,17 @@ def run_ours(args, rank, world, local_rank):
     }
 
 
-# Mean DRAM bytes (read + write) per controlled-phase launch over the 325
-# CPhase launches of one 26-qubit complex64 QFT, from an ncu capture of
+# Mean DRAM bytes (read + write) per controlled-phase launch over the 378
+# CPhase launches of one 28-qubit complex64 QFT, from an ncu capture of
 # dram__bytes_read.sum + dram__bytes_write.sum.  Traffic grows with the
 # register (2^n), so other sizes scale it.
-CPHASE_TRAFFIC_C64_26Q = 277.4e6
+CPHASE_TRAFFIC_C64_28Q = 1256.4e6
 
 
 def traffic_per_launch(n, dtype):
     if dtype != "c64":
         return None
-    return round(CPHASE_TRAFFIC_C64_26Q * 2.0 ** (n - 26))
+    return round(CPHASE_TRAFFIC_C64_28Q * 2.0 ** (n - 28))
 
 
 def run_reference(args):
