@@ -3,9 +3,9 @@
 // without the tensor cores), and for registers of 13-14 qubits (c64) / 12-13
 // (c128) the tile shape: the whole register in one CTA's tile, or streaming
 // tiles of 2^12 / 2^11 amplitudes over several CTAs — by timing each choice
-// on a scratch register of the circuit's size.  Results are cached per context by the circuit's
-// structure (gate kinds and operands, not angles or matrix entries), so a
-// parameter sweep tunes once.
+// on a scratch register of the circuit's size.  Results are cached per
+// context by the circuit's structure (gate kinds and operands, not angles or
+// matrix entries), so a parameter sweep tunes once.
 #include <algorithm>
 #include <cstring>
 #include <map>
