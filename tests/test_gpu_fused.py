@@ -87,3 +87,36 @@ def test_fused_permutation_circuit_bit_exact(gpu_ctx, n, k):
         got = st.download()
         prog.free()
     assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("tc", [True, False])
+def test_runs_are_deterministic(gpu_ctx, tc):
+    """Run-to-run determinism: the same program on the same input gives the
+    same bits on a second run and on a second context (a fresh plan cache).
+    Tile passes accumulate nothing with atomics, and the tensor-core run's
+    renormalisation adds its per-CTA partials in a fixed order."""
+    n = 20
+    ops = circuits.brickwork(n, 12, seed=11)
+    v = _kat.random_state(n, 4).astype(np.complex64)
+    prog = aq.Program(n, ops, aq.C64, max_qubits=5)
+
+    def three_runs(ctx):
+        ctx.set_tensor_cores(tc)
+        try:
+            out = [run_prog(ctx, v, prog, aq.C64, aq.EXEC_TILED) for _ in range(2)]
+            with aq.State(ctx, n, aq.C64) as st:  # the gates unfused, in tile passes
+                st.upload(v)
+                st.apply(ops, aq.EXEC_TILED)
+                out.append(st.download())
+        finally:
+            ctx.set_tensor_cores(True)
+        return out
+
+    first = three_runs(gpu_ctx)
+    with aq.Context(0) as other:
+        second = three_runs(other)
+    assert np.array_equal(first[0], first[1])
+    assert np.array_equal(first[0], second[0]) and np.array_equal(first[1], second[1])
+    assert np.array_equal(first[2], second[2])
+    assert np.max(np.abs(first[0] - first[2])) < 1e-5
+    prog.free()
