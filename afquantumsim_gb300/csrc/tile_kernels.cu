@@ -730,31 +730,41 @@ static void tc_operand(const std::vector<double>& mk, int k, std::vector<unsigne
     const size_t split = 2ull * N * K;
     const size_t at = out.size();
     out.resize(at + 2 * split, 0);
-    // each complex entry is split once; -Ui is the sign-flipped split of Ui
-    // (rounding to nearest even is symmetric)
+    // each component (Ur, Ui of every entry) is split once, in one loop over
+    // the matrix; -Ui is the sign-flipped split of Ui (rounding to nearest
+    // even is symmetric).  Tensor-core ops have k >= 3: D is a multiple of 4.
+    const uint32_t E = 2u * D * D;
+    uint16_t sh[2 * 32 * 32], sl[2 * 32 * 32];
+    for (uint32_t e = 0; e < E; ++e) {
+        const double v = mk[e];
+        const uint16_t h = host_bf16((float)v);
+        sh[e] = h;
+        sl[e] = host_bf16((float)(v - (double)host_bf16_val(h)));
+    }
     unsigned char* hi = &out[at];
     unsigned char* lo = hi + split;
-    auto split16 = [](double v, uint16_t& h, uint16_t& l) {
-        h = host_bf16((float)v);
-        l = host_bf16((float)(v - (double)host_bf16_val(h)));
-    };
     // the 2x2 real block of entry (r, c) sits in one 8x8 core matrix (2r
     // and 2c are even): (2r, 2c) and (2r, 2c+1) are adjacent halves of a
-    // 32-bit word, rows 2r and 2r+1 are 16 bytes apart
-    auto put = [](unsigned char* p, uint16_t r, uint16_t i) {
-        const uint32_t w0 = (uint32_t)r | ((uint32_t)(i ^ 0x8000u) << 16);  // Ur, -Ui
-        const uint32_t w1 = (uint32_t)i | ((uint32_t)r << 16);              // Ui, Ur
-        std::memcpy(p, &w0, 4);
-        std::memcpy(p + 16, &w1, 4);
+    // 32-bit word (Ur, -Ui), row 2r+1 holds (Ui, Ur) 16 bytes on, and
+    // entries c .. c+3 (c a multiple of 4) fill the core matrix's rows 2r and
+    // 2r+1: two 16-byte runs per split
+    auto words = [](const uint16_t* sp, uint32_t e, uint32_t* w0, uint32_t* w1) {
+        for (uint32_t j = 0; j < 4; ++j) {
+            const uint32_t r = sp[e + 2 * j], i = sp[e + 2 * j + 1];
+            w0[j] = r | ((i ^ 0x8000u) << 16);  // Ur, -Ui
+            w1[j] = i | (r << 16);              // Ui, Ur
+        }
     };
     for (uint32_t r = 0; r < D; ++r)
-        for (uint32_t c = 0; c < D; ++c) {
-            uint16_t rh, rl, ih, il;
-            split16(mk[2 * (r * D + c)], rh, rl);
-            split16(mk[2 * (r * D + c) + 1], ih, il);
-            const uint32_t off = kmajor_off(2 * r, 2 * c, K);
-            put(hi + off, rh, ih);
-            put(lo + off, rl, il);
+        for (uint32_t c = 0; c < D; c += 4) {
+            const uint32_t e = 2 * (r * D + c), off = kmajor_off(2 * r, 2 * c, K);
+            uint32_t w0[4], w1[4];
+            words(sh, e, w0, w1);
+            std::memcpy(hi + off, w0, 16);
+            std::memcpy(hi + off + 16, w1, 16);
+            words(sl, e, w0, w1);
+            std::memcpy(lo + off, w0, 16);
+            std::memcpy(lo + off + 16, w1, 16);
         }
 }
 
