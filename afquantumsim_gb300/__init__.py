@@ -506,28 +506,32 @@ def circuit_from_text(text: str):
 class TilePass(C.Structure):
     """struct aqsg_tile_pass (aqsg_debug.h)"""
     _fields_ = [("m", C.c_int32), ("L", C.c_int32), ("first", C.c_int32), ("count", C.c_int32),
-                ("tbits", C.c_int32 * 16)]
+                ("tbits", C.c_int32 * 16), ("tc", C.c_int32), ("matk", C.c_int32), ("tc_blob", C.c_uint32),
+                ("tc_bytes", C.c_uint32)]
 
 
-def debug_tile_plan(n: int, ops, dtype: int = C64, fuse_qubits: int = 0, whole_tile_max: int = 0):
-    """aqsg_debug_tile_plan: (passes, table bytes, pool bytes) of the CUDA-core
-    tile plan the engine would run for ops (a testing aid); whole_tile_max as
-    set by Context.set_whole_tile_max (0: the default)."""
+def debug_tile_plan(n: int, ops, dtype: int = C64, fuse_qubits: int = 0, whole_tile_max: int = 0,
+                    tensor_cores: bool = False):
+    """aqsg_debug_tile_plan: (passes, table bytes, pool bytes) of the tile
+    plan the engine would run for ops (a testing aid); whole_tile_max and
+    tensor_cores as set by Context.set_whole_tile_max / set_tensor_cores
+    (defaults: the whole-tile default, the CUDA-core form)."""
     lib = load_library()
     f = lib.aqsg_debug_tile_plan
-    f.argtypes = [C.c_int, C.c_int, C.POINTER(Op), C.c_int, C.c_int, C.c_int, C.POINTER(TilePass), C.c_int,
+    f.argtypes = [C.c_int, C.c_int, C.POINTER(Op), C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(TilePass), C.c_int,
                   C.POINTER(C.c_int), C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t), C.c_void_p, C.c_size_t,
                   C.POINTER(C.c_size_t)]
     f.restype = C.c_int
     arr = op_array(list(ops)) if not isinstance(ops, C.Array) else ops
     npass, tb, pb = C.c_int(), C.c_size_t(), C.c_size_t()
-    _check(f(n, dtype, arr, len(arr), fuse_qubits, whole_tile_max, None, 0, C.byref(npass), None, 0, C.byref(tb),
-             None, 0, C.byref(pb)))
+    tc = 1 if tensor_cores else 0
+    _check(f(n, dtype, arr, len(arr), fuse_qubits, whole_tile_max, tc, None, 0, C.byref(npass), None, 0,
+             C.byref(tb), None, 0, C.byref(pb)))
     passes = (TilePass * max(npass.value, 1))()
     table = C.create_string_buffer(max(tb.value, 1))
     pool = C.create_string_buffer(max(pb.value, 1))
-    _check(f(n, dtype, arr, len(arr), fuse_qubits, whole_tile_max, passes, npass.value, C.byref(npass), table,
-             tb.value, C.byref(tb), pool, pb.value, C.byref(pb)))
+    _check(f(n, dtype, arr, len(arr), fuse_qubits, whole_tile_max, tc, passes, npass.value, C.byref(npass),
+             table, tb.value, C.byref(tb), pool, pb.value, C.byref(pb)))
     return list(passes[:npass.value]), table.raw[:tb.value], pool.raw[:pb.value]
 
 

@@ -1686,7 +1686,8 @@ int run_plan_async(aqsg_state_s* st, const TilePlan& plan, const void* dev_table
 #include "../../include/aqsg_debug.h"
 
 extern "C" int aqsg_debug_tile_plan(int n, int dtype, const aqsg_op* ops, int count, int fuse_qubits,
-                                    int whole_tile_max, aqsg_tile_pass* passes, int pass_capacity, int* pass_count,
+                                    int whole_tile_max, int tensor_cores, aqsg_tile_pass* passes, int pass_capacity,
+                                    int* pass_count,
                                     void* table, size_t table_capacity, size_t* table_bytes, void* pool,
                                     size_t pool_capacity, size_t* pool_bytes) {
     using namespace aqsg;
@@ -1708,7 +1709,7 @@ extern "C" int aqsg_debug_tile_plan(int n, int dtype, const aqsg_op* ops, int co
     }
     TilePlan plan;
     if (whole_tile_max < 0) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Negative whole-tile qubit count");
-    if (int rc = encode_tiled(n, dtype, low, false, &plan, true, whole_tile_max)) return rc;
+    if (int rc = encode_tiled(n, dtype, low, tensor_cores != 0, &plan, true, whole_tile_max)) return rc;
     if (pass_count) *pass_count = (int)plan.passes.size();
     if (table_bytes) *table_bytes = plan.table.size();
     if (pool_bytes) *pool_bytes = plan.pool.size();
@@ -1723,6 +1724,10 @@ extern "C" int aqsg_debug_tile_plan(int n, int dtype, const aqsg_op* ops, int co
             o.first = (int32_t)p.first;
             o.count = (int32_t)p.count;
             for (int b = 0; b < p.m && b < 16; ++b) o.tbits[b] = p.tbits[b];
+            o.tc = p.tc;
+            o.matk = p.matk;
+            o.tc_blob = p.tc_blob;
+            o.tc_bytes = p.tc_bytes;
         }
     }
     if (table) {

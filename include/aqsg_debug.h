@@ -15,21 +15,27 @@ extern "C" {
 
 /* One tile pass of an encoded plan: tiles of 2^m amplitudes whose local
  * index bit i is global index bit tbits[i] (ascending; the L lowest are the
- * contiguous row bits), running table records [first, first + count). */
+ * contiguous row bits), running table records [first, first + count).  A
+ * tensor-core pass (tc = 1) keeps its fused unitaries' operands in the pool
+ * at [tc_blob, tc_blob + tc_bytes); matk = 1: it also has dense k-qubit
+ * ops for the CUDA cores. */
 typedef struct aqsg_tile_pass {
     int32_t m, L, first, count;
     int32_t tbits[16];
+    int32_t tc, matk;
+    uint32_t tc_blob, tc_bytes;
 } aqsg_tile_pass;
 
 /* The tile-pass plan aqsg_apply_ops would run for ops in AQSG_EXEC_TILED mode
- * on an n-qubit register of dtype, the CUDA-core form (no tensor cores),
- * after fusing at fuse_qubits (0: the gates as they are), on a context whose
- * aqsg_set_whole_tile_max setting is whole_tile_max (0: the default): the
- * passes, the op table (160-byte records: the engine's tile ops and
- * register-phase ops) and the operand pool, byte for byte as they are
- * uploaded.  Call with NULL buffers to get the counts and sizes. */
+ * on an n-qubit register of dtype, after fusing at fuse_qubits (0: the gates
+ * as they are), on a context whose aqsg_set_whole_tile_max setting is
+ * whole_tile_max (0: the default) and aqsg_set_tensor_cores setting is
+ * tensor_cores: the passes, the op table (160-byte records: the engine's
+ * tile ops and register-phase ops) and the operand pool, byte for byte as
+ * they are uploaded.  Call with NULL buffers to get the counts and sizes. */
 int aqsg_debug_tile_plan(int n, int dtype, const aqsg_op* ops, int count, int fuse_qubits,
-                         int whole_tile_max, aqsg_tile_pass* passes, int pass_capacity, int* pass_count,
+                         int whole_tile_max, int tensor_cores, aqsg_tile_pass* passes, int pass_capacity,
+                         int* pass_count,
                          void* table, size_t table_capacity, size_t* table_bytes,
                          void* pool, size_t pool_capacity, size_t* pool_bytes);
 

@@ -65,3 +65,34 @@ def test_streaming_tile_shape_for_small_registers(dtype, n, fuse, seed):
 def test_whole_tile_limit_rejects_negative():
     with pytest.raises(aq.InvalidArgument):
         aq.debug_tile_plan(13, _kat.random_circuit(13, 10, 1), aq.C64, 0, whole_tile_max=-1)
+
+
+@pytest.mark.parametrize("n,k,seed,gates,wmax", [(12, 5, 21, 40, 0), (13, 3, 22, 150, 12), (15, 5, 23, 150, 0),
+                                                  (16, 4, 24, 150, 0), (17, 5, 25, 150, 0), (15, 3, 26, 150, 0)])
+def test_tensor_core_plan_equals_oracle(n, k, seed, gates, wmax):
+    # the tensor-core form of a fused program: split-BF16 B operands in the
+    # K-major layout, the data-column and matrix-row tables, run as the
+    # tensor cores compute it, gives the FP64 oracle's state (12 qubits: the
+    # whole register as one tensor-core tile; 13 in streaming tiles)
+    ops = _kat.random_circuit(n, gates, seed)
+    passes, table, pool = aq.debug_tile_plan(n, ops, aq.C64, k, whole_tile_max=wmax, tensor_cores=True)
+    assert any(p.tc for p in passes)
+    v = _kat.random_state(n, seed)
+    want = oracle.apply_f64(v.copy(), ops)
+    got = run_plan(v, n, passes, table, pool, c64=True)
+    assert np.max(np.abs(got - want)) < 1e-5
+    # the same program's CUDA-core form agrees
+    cc = run_plan(v, n, *aq.debug_tile_plan(n, ops, aq.C64, k, whole_tile_max=wmax), c64=True)
+    assert np.max(np.abs(cc - want)) < 1e-5
+
+
+def test_tensor_core_brickwork_plan_streaming_14():
+    # a 14-qubit brick-work program in streaming tiles (the autotuner's
+    # other tile shape) on the tensor cores
+    n = 14
+    ops = circuits.brickwork(n, 10, seed=3)
+    passes, table, pool = aq.debug_tile_plan(n, ops, aq.C64, 5, whole_tile_max=12, tensor_cores=True)
+    assert all(p.m == 12 for p in passes) and sum(p.tc for p in passes) >= 3
+    v = _kat.random_state(n, 8)
+    got = run_plan(v, n, passes, table, pool, c64=True)
+    assert np.max(np.abs(got - oracle.apply_f64(v.copy(), ops))) < 1e-5

@@ -1,7 +1,7 @@
 """Test infrastructure: a numpy restatement of how the tile kernels interpret
 an encoded tile plan (aqsg_debug_tile_plan), used to check the host encoder
-(pass planning, register phases, control masks, matrix layouts) on the CPU
-against the FP64 oracle.  It restates the record semantics of
+(pass planning, register phases, control masks, matrix layouts, tensor-core
+operands and index tables) on the CPU against the FP64 oracle.  It restates the record semantics of
 afquantumsim_gb300/csrc/tile_device.cuh (tile_run_ops, rphase_run) — the
 device code itself runs only in the GPU tests."""
 import numpy as np
@@ -105,6 +105,58 @@ def _tile_op(X, base, j, op, pool, c64):
             X[:, jb | off[r]] = np.where(cond, W[..., r], X[:, jb | off[r]])
         return
     raise AssertionError(f"unexpected tile op class {cls}")
+
+
+# tensor-core ops (tile_device.cuh tc_apply_tm, tile_kernels.cu tc_operand /
+# tc_tables): in the pass's operand blob, at the op's offset, the B operand's
+# BF16 hi split, its lo split (each 2N x 2K bytes, no-swizzle K-major), then
+# the index tables (colbase: 512 x u16 byte offsets of the data columns in
+# the padded tile, offr at +1024: the matrix rows' byte offsets)
+TC_TABLE_BYTES = 1024 + 64
+TC_ROW_AMPS = 34  # padded tile row: 32 amplitudes + 2 of padding (272 bytes)
+
+
+def _bf16(x):
+    """float32 values rounded to bfloat16 (nearest even), as float64"""
+    u = np.asarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def _kmajor(raw: np.ndarray, rows: int, K: int) -> np.ndarray:
+    """rows x K bf16 matrix from its no-swizzle K-major byte image"""
+    r, kk = np.meshgrid(np.arange(rows), np.arange(K), indexing="ij")
+    off = ((r >> 3) * (K >> 3) + (kk >> 3)) * 128 + (r & 7) * 16 + (kk & 7) * 2
+    h = raw[off].astype(np.uint32) | (raw[off + 1].astype(np.uint32) << 8)
+    return (h << 16).astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def _tc_op(X, base, op, pool, blob_at):
+    """Y = U X of a fused unitary as the tensor cores compute it: the data
+    split into BF16 hi + lo, products Ahi Bhi + Ahi Blo + Alo Bhi"""
+    k = int(op["k"])
+    d = 1 << k
+    K = N = 2 * d
+    split = 2 * N * K
+    at = blob_at + int(op["mat"])
+    raw = np.frombuffer(pool, dtype=np.uint8)
+    b_hi = _kmajor(raw[at:at + split], N, K)
+    b_lo = _kmajor(raw[at + split:at + 2 * split], N, K)
+    tables = at + 2 * split
+    cols = 4096 // d
+    colbase = np.frombuffer(pool, dtype="<u2", count=cols, offset=tables).astype(np.int64)
+    offr = np.frombuffer(pool, dtype="<u2", count=d, offset=tables + 1024).astype(np.int64)
+    e = (colbase[:, None] + offr[None, :]) // 8  # amplitude slots in the padded tile
+    J = (e // TC_ROW_AMPS) * 32 + e % TC_ROW_AMPS  # tile-local indices, (cols, d)
+    x = X[:, J]
+    a = np.empty(x.shape[:-1] + (K,))
+    a[..., 0::2], a[..., 1::2] = x.real, x.imag
+    a32 = a.astype(np.float32)
+    a_hi = _bf16(a32)
+    a_lo = _bf16(a32 - a_hi.astype(np.float32))
+    y = a_hi @ b_hi.T + a_hi @ b_lo.T + a_lo @ b_hi.T
+    ext = ((base & np.uint64(op["cm_ext"])) == np.uint64(op["cv_ext"]))[:, None, None]
+    X[:, J] = np.where(ext, y[..., 0::2] + 1j * y[..., 1::2], x)
 
 
 def _phase(X, base, j, head, rops, pool, c64):
@@ -215,6 +267,9 @@ def run_plan(psi: np.ndarray, n: int, passes, table: bytes, pool: bytes, c64: bo
             if int(op["cls"]) == T_RPHASE:
                 _phase(X, base, j, op, rrecs[q + 1:q + 1 + int(op["k"])], pool, c64)
                 q += 1 + int(op["k"])
+            elif int(op["cls"]) == L_MATK and int(op["pad"]) and getattr(p, "tc", 0):
+                _tc_op(X, base, op, pool, int(p.tc_blob))
+                q += 1
             else:
                 _tile_op(X, base, j, op, pool, c64)
                 q += 1
