@@ -515,7 +515,8 @@ def debug_tile_plan(n: int, ops, dtype: int = C64, fuse_qubits: int = 0, whole_t
     """aqsg_debug_tile_plan: (passes, table bytes, pool bytes) of the tile
     plan the engine would run for ops (a testing aid); whole_tile_max and
     tensor_cores as set by Context.set_whole_tile_max / set_tensor_cores
-    (defaults: the whole-tile default, the CUDA-core form)."""
+    (defaults: the whole-tile default, the CUDA-core form; tensor_cores=2:
+    the batched engine's form, fused permutations on the tensor cores too)."""
     lib = load_library()
     f = lib.aqsg_debug_tile_plan
     f.argtypes = [C.c_int, C.c_int, C.POINTER(Op), C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(TilePass), C.c_int,
@@ -524,7 +525,7 @@ def debug_tile_plan(n: int, ops, dtype: int = C64, fuse_qubits: int = 0, whole_t
     f.restype = C.c_int
     arr = op_array(list(ops)) if not isinstance(ops, C.Array) else ops
     npass, tb, pb = C.c_int(), C.c_size_t(), C.c_size_t()
-    tc = 1 if tensor_cores else 0
+    tc = int(tensor_cores)  # False / True, or 2: the batched engine's form
     _check(f(n, dtype, arr, len(arr), fuse_qubits, whole_tile_max, tc, None, 0, C.byref(npass), None, 0,
              C.byref(tb), None, 0, C.byref(pb)))
     passes = (TilePass * max(npass.value, 1))()

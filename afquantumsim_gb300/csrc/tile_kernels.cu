@@ -1709,7 +1709,10 @@ extern "C" int aqsg_debug_tile_plan(int n, int dtype, const aqsg_op* ops, int co
     }
     TilePlan plan;
     if (whole_tile_max < 0) return set_error(AQSG_ERR_INVALID_ARGUMENT, "Negative whole-tile qubit count");
-    if (int rc = encode_tiled(n, dtype, low, tensor_cores != 0, &plan, true, whole_tile_max)) return rc;
+    if (tensor_cores < 0 || tensor_cores > 2) return set_error(AQSG_ERR_INVALID_ARGUMENT, "tensor_cores is 0, 1 or 2");
+    // 2: the batched engine's form, where a fused permutation matrix goes to
+    // the tensor cores too (the choice depends on the op structure only)
+    if (int rc = encode_tiled(n, dtype, low, tensor_cores != 0, &plan, tensor_cores != 2, whole_tile_max)) return rc;
     if (pass_count) *pass_count = (int)plan.passes.size();
     if (table_bytes) *table_bytes = plan.table.size();
     if (pool_bytes) *pool_bytes = plan.pool.size();

@@ -30,9 +30,11 @@ typedef struct aqsg_tile_pass {
  * on an n-qubit register of dtype, after fusing at fuse_qubits (0: the gates
  * as they are), on a context whose aqsg_set_whole_tile_max setting is
  * whole_tile_max (0: the default) and aqsg_set_tensor_cores setting is
- * tensor_cores: the passes, the op table (160-byte records: the engine's
- * tile ops and register-phase ops) and the operand pool, byte for byte as
- * they are uploaded.  Call with NULL buffers to get the counts and sizes. */
+ * tensor_cores (2: the form the batched engine encodes, where fused
+ * permutation matrices go to the tensor cores as well): the passes, the op
+ * table (160-byte records: the engine's tile ops and register-phase ops) and
+ * the operand pool, byte for byte as they are uploaded.  Call with NULL
+ * buffers to get the counts and sizes. */
 int aqsg_debug_tile_plan(int n, int dtype, const aqsg_op* ops, int count, int fuse_qubits,
                          int whole_tile_max, int tensor_cores, aqsg_tile_pass* passes, int pass_capacity,
                          int* pass_count,

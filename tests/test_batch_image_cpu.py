@@ -94,6 +94,25 @@ def test_large_plan_image_is_the_encoded_plan():
         assert np.max(np.abs(got - oracle.apply_f64(v.copy(), ops))) < 1e-5
 
 
+@pytest.mark.parametrize("fuse", [3, 4, 5])
+def test_tensor_core_plan_after_update_runs_to_the_oracle(fuse):
+    """A register of more than 14 qubits on the tensor cores: after an update
+    with new angles its image is the new circuit's tensor-core plan in the
+    batched engine's form, and the tile-record restatement (split-BF16
+    operands decoded from the image) runs it to the oracle's state."""
+    n = 16
+    a, b = sweep(6, [n]), sweep(7, [n])
+    image = aq.debug_batch_image(a, [fuse], [1], update=b)
+    ops = as_ops(b[0][1])
+    passes, table, pool = aq.debug_tile_plan(n, ops, aq.C64, fuse, tensor_cores=2)
+    assert all(p.tc for p in passes)
+    poff = (len(table) + 255) & ~255
+    assert image[:len(table)] == table and image[poff:poff + len(pool)] == pool
+    v = _kat.random_state(n, 2)
+    got = run_plan(v, n, passes, image[:len(table)], image[poff:], c64=True)
+    assert np.max(np.abs(got - oracle.apply_f64(v.copy(), ops))) < 1e-5
+
+
 def test_update_refuses_another_structure():
     a = sweep(1)
     fuse, tc = [2, 2, 3, 4], [0, 0, 1, 1]
